@@ -1,0 +1,224 @@
+"""ctypes binding of the CPU oracle (oracle/vf_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: the parity checker and the timed CPU baseline.
+Imported by tests/, __graft_entry__.smoke() and bench.py's CPU arms; the
+product package never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libvforacle.so")
+_lib = None
+
+OK, ERR_INVALID, ERR_SEED_SEARCH, ERR_RANGE = 0, 1, 4, 5
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (seconds)."""
+    if force or not os.path.exists(_LIB_PATH) or (
+            os.path.getmtime(_LIB_PATH) < max(
+                os.path.getmtime(os.path.join(_HERE, f))
+                for f in ("vf_oracle.c", "vf_oracle.h", "Makefile"))):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+class Params(C.Structure):
+    _fields_ = [("algorithm", C.c_int32), ("distance", C.c_int32),
+                ("num_seeds", C.c_int32), ("num_extra_seeds", C.c_int32),
+                ("merge_distance", C.c_int32), ("seed_location", C.c_int32),
+                ("seed", C.c_uint64), ("noise_amplitude", C.c_float),
+                ("noise_period", C.c_uint32), ("erode", C.c_int32),
+                ("erosion_type", C.c_int32), ("erosion_size", C.c_int32),
+                ("erosion_iterations", C.c_int32),
+                ("erosion_probability", C.c_float),
+                ("erosion_threshold", C.c_float), ("boundary_size", C.c_int32)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+        P = C.c_void_p
+        u32, u64, i32, f32 = C.c_uint32, C.c_uint64, C.c_int, C.c_float
+        sig = {
+            "vfo_hash": (u64, [u64, u32, u64]),
+            "vfo_u01": (f32, [u64]),
+            "vfo_voxelize": (i32, [P, u32, P, u32, u32, u32, u32, P, P, P, i32]),
+            "vfo_tri_box": (i32, [P, P, P, P, P]),
+            "vfo_grid_dims": (None, [P, P, u32, P]),
+            "vfo_seeder_uniform": (i32, [P, u32, u32, u32, u32, u64, i32, P]),
+            "vfo_merge_seeds": (i32, [P, u32, P, u32, i32]),
+            "vfo_fracture_seeds": (i32, [P, u32, u32, u32, u32, u32, i32, i32, u64, P, P]),
+            "vfo_flood": (i32, [P, u32, u32, u32, P, u32, i32, P]),
+            "vfo_naive": (i32, [P, u32, u32, u32, P, u32, i32]),
+            "vfo_perturb": (i32, [P, u32, u32, u32, f32, u32, u64]),
+            "vfo_detect_boundaries": (None, [P, u32, u32, u32, i32]),
+            "vfo_remove_isolated": (None, [P, u32, u32, u32]),
+            "vfo_erode": (i32, [P, u32, u32, u32, i32, u32, u32, f32, f32, u64]),
+            "vfo_undo_mask": (None, [P, u32, u32, u32]),
+            "vfo_count_values": (i32, [P, u32, u32, u32, P, u32, P]),
+            "vfo_run_job": (i32, [P, u32, P, u32, u32, u32, u32, P, P, P, P, P, u32, P, P]),
+            "vfo_rle_encode": (C.c_size_t, [P, u32, u32, u32, P, C.c_size_t]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(_lib, name)
+            fn.restype = res
+            fn.argtypes = args
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f3(v):
+    return np.ascontiguousarray(np.asarray(v, dtype=np.float32).reshape(3))
+
+
+class OracleError(RuntimeError):
+    def __init__(self, status, what):
+        super().__init__(f"{what}: oracle status {status}")
+        self.status = status
+
+
+def _check(st, what):
+    if st != OK:
+        raise OracleError(st, what)
+
+
+def voxelize(verts, faces, dims, aabb_min, aabb_max, mode=3):
+    X, Y, Z = (int(d) for d in dims)
+    v = np.ascontiguousarray(verts, dtype=np.float32)
+    f = np.ascontiguousarray(faces, dtype=np.uint32)
+    g = np.empty((X, Y, Z), dtype=np.uint16)
+    mn, mx = _f3(aabb_min), _f3(aabb_max)
+    _check(lib().vfo_voxelize(_p(v), v.shape[0], _p(f), f.shape[0], X, Y, Z,
+                              _p(mn), _p(mx), _p(g), mode), "voxelize")
+    return g
+
+
+def tri_box(p0, p1, p2, bmin, bmax):
+    a = [_f3(x) for x in (p0, p1, p2, bmin, bmax)]
+    return bool(lib().vfo_tri_box(*[_p(x) for x in a]))
+
+
+def grid_dims(aabb_min, aabb_max, max_voxels):
+    out = np.zeros(3, np.uint32)
+    mn, mx = _f3(aabb_min), _f3(aabb_max)
+    lib().vfo_grid_dims(_p(mn), _p(mx), int(max_voxels), _p(out))
+    return tuple(int(x) for x in out)
+
+
+def seeder_uniform(grid, n, seed, location):
+    g = np.ascontiguousarray(grid, dtype=np.uint16)
+    out = np.zeros((max(n, 1), 4), np.uint32)
+    _check(lib().vfo_seeder_uniform(_p(g), *g.shape, int(n), int(seed),
+                                    int(location), _p(out)), "seeder_uniform")
+    return out[:n]
+
+
+def fracture_seeds(grid, n_main, n_extra, location, merge_dfunc, seed):
+    g = np.ascontiguousarray(grid, dtype=np.uint16)
+    cap = 2 * n_main + n_extra
+    out = np.zeros((max(cap, 1), 4), np.uint32)
+    n = C.c_uint32(0)
+    _check(lib().vfo_fracture_seeds(_p(g), *g.shape, int(n_main), int(n_extra),
+                                    int(location), int(merge_dfunc), int(seed),
+                                    _p(out), C.byref(n)), "fracture_seeds")
+    return out[:n.value]
+
+
+def merge_seeds(frags, seeds, dfunc):
+    f = np.ascontiguousarray(frags, dtype=np.uint32)
+    s = np.array(seeds, dtype=np.uint32, copy=True, order="C")
+    _check(lib().vfo_merge_seeds(_p(f), f.shape[0], _p(s), s.shape[0], int(dfunc)),
+           "merge_seeds")
+    return s
+
+
+def flood(grid, seeds, dfunc):
+    g = np.array(grid, dtype=np.uint16, copy=True, order="C")
+    s = np.ascontiguousarray(seeds, dtype=np.uint32).reshape(-1, 4)
+    waves = C.c_uint32(0)
+    _check(lib().vfo_flood(_p(g), *g.shape, _p(s), s.shape[0], int(dfunc),
+                           C.byref(waves)), "flood")
+    return g, waves.value
+
+
+def naive(grid, seeds, dfunc):
+    g = np.array(grid, dtype=np.uint16, copy=True, order="C")
+    s = np.ascontiguousarray(seeds, dtype=np.uint32).reshape(-1, 4)
+    _check(lib().vfo_naive(_p(g), *g.shape, _p(s), s.shape[0], int(dfunc)), "naive")
+    return g
+
+
+def perturb(grid, amplitude, period, seed):
+    g = np.array(grid, dtype=np.uint16, copy=True, order="C")
+    _check(lib().vfo_perturb(_p(g), *g.shape, float(amplitude), int(period),
+                             int(seed)), "perturb")
+    return g
+
+
+def detect_boundaries(grid, size=1):
+    g = np.array(grid, dtype=np.uint16, copy=True, order="C")
+    lib().vfo_detect_boundaries(_p(g), *g.shape, int(size))
+    return g
+
+
+def remove_isolated(grid):
+    g = np.array(grid, dtype=np.uint16, copy=True, order="C")
+    lib().vfo_remove_isolated(_p(g), *g.shape)
+    return g
+
+
+def erode(grid, etype, size, iterations, probability, threshold, seed):
+    g = np.array(grid, dtype=np.uint16, copy=True, order="C")
+    _check(lib().vfo_erode(_p(g), *g.shape, int(etype), int(size), int(iterations),
+                           float(probability), float(threshold), int(seed)), "erode")
+    return g
+
+
+def undo_mask(grid):
+    g = np.array(grid, dtype=np.uint16, copy=True, order="C")
+    lib().vfo_undo_mask(_p(g), *g.shape)
+    return g
+
+
+def count_values(grid, ncounts=32768):
+    g = np.ascontiguousarray(grid, dtype=np.uint16)
+    c = np.zeros(ncounts, np.uint32)
+    occ = C.c_uint64(0)
+    _check(lib().vfo_count_values(_p(g), *g.shape, _p(c), ncounts, C.byref(occ)),
+           "count_values")
+    return c, occ.value
+
+
+def run_job(verts, faces, dims, aabb_min, aabb_max, params: Params, ncounts=32768):
+    X, Y, Z = (int(d) for d in dims)
+    v = np.ascontiguousarray(verts, dtype=np.float32)
+    f = np.ascontiguousarray(faces, dtype=np.uint32)
+    g = np.empty((X, Y, Z), dtype=np.uint16)
+    c = np.zeros(ncounts, np.uint32)
+    cap = 2 * params.num_seeds + params.num_extra_seeds
+    s = np.zeros((max(cap, 1), 4), np.uint32)
+    ns = C.c_uint32(0)
+    mn, mx = _f3(aabb_min), _f3(aabb_max)
+    _check(lib().vfo_run_job(_p(v), v.shape[0], _p(f), f.shape[0], X, Y, Z,
+                             _p(mn), _p(mx), C.byref(params), _p(g), _p(c), ncounts,
+                             _p(s), C.byref(ns)), "run_job")
+    return g, c, s[:ns.value]
+
+
+def rle_encode(grid):
+    g = np.ascontiguousarray(grid, dtype=np.uint16)
+    n = lib().vfo_rle_encode(_p(g), *g.shape, None, 0)
+    out = np.zeros(n, np.uint8)
+    lib().vfo_rle_encode(_p(g), *g.shape, _p(out), n)
+    return out.tobytes()
