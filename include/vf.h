@@ -1,0 +1,254 @@
+/*
+ * vf.h -- C ABI of the GB300 voxelize -> seed -> fracture -> perturb/erode
+ * -> count pipeline (library libvfgb300.so).
+ *
+ * The entry points replace the reference's fracture path, which is C++ over
+ * OpenGL compute shaders:
+ *   RegularGrid    (MeshFragments/Source/DataStructures/RegularGrid.h:142-367)
+ *   Seeder         (MeshFragments/Source/Fracturer/Seeder.h:59-76)
+ *   Fracturer      (MeshFragments/Source/Fracturer/Fracturer.h:28-57) with
+ *                  FloodFracturer / NaiveFracturer
+ *   CADScene::fractureModel (MeshFragments/Source/Graphics/Application/
+ *                  CADScene.cpp:624-691), the orchestration order.
+ *
+ * Conventions
+ *   - Plain C types only; every call returns a vf_status (0 = VF_OK).  No
+ *     exception crosses the ABI.  vf_last_error() gives a message for the
+ *     last failing call on the calling thread.
+ *   - Label grids are uint16, x-major, index x*Y*Z + y*Z + z
+ *     (RegularGrid.cpp:1031-1034).  0 EMPTY, 1 FREE, >1 labels; bits 0-7
+ *     fragment id, 8-14 sub-seed prefix, 15 boundary flag.
+ *   - Host pointers are the caller's; the library copies what it needs.
+ *     Grids live on the device, owned by the context, until destroyed.
+ *   - One context per device and per host thread at a time: calls on one
+ *     context are serialised by the caller.  Work runs on the context's
+ *     CUDA stream; calls that return host data synchronise it.
+ *   - Results are deterministic: identical inputs give identical bits, in
+ *     isolation, in a batch and under the server.
+ */
+#ifndef VF_H
+#define VF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int vf_status;
+#define VF_OK 0
+#define VF_ERR_INVALID 1     /* bad argument (dims, pointers, enum values) */
+#define VF_ERR_CUDA 2        /* CUDA runtime error; context may be unusable */
+#define VF_ERR_OOM 3         /* allocation failed or over the HBM budget */
+#define VF_ERR_SEED_SEARCH 4 /* Seeder::SeederSearchError (Seeder.h:19-22) */
+#define VF_ERR_RANGE 5       /* value out of the representable range */
+#define VF_ERR_TIMEOUT 6     /* a bounded device wait gave up */
+#define VF_ERR_NOT_BUILT 7   /* CUDA path unavailable (no device / no kernel image) */
+#define VF_ERR_BUSY 8        /* server queue full */
+
+/* FractureParameters::FractureAlgorithm (FractureParameters.h:20) */
+#define VF_NAIVE 0
+#define VF_FLOOD 1
+/* fracturer::DistanceFunction (Fracturer.h:10-14) */
+#define VF_EUCLIDEAN 0
+#define VF_MANHATTAN 1
+#define VF_CHEBYSHEV 2
+/* FractureParameters::ErosionType (FractureParameters.h:26) */
+#define VF_SQUARE 0
+#define VF_ELLIPSE 1
+#define VF_CROSS 2
+/* Seeder::Location (Seeder.h:24) */
+#define VF_INNER 0
+#define VF_OUTER 1
+#define VF_BOTH 2
+
+#define VF_MAX_SEEDS 4095u  /* seeds per fracture (12-bit seed slot) */
+#define VF_MAX_DIM 4096u    /* per axis */
+
+typedef struct vf_ctx vf_ctx;
+typedef struct vf_grid vf_grid;
+typedef struct vf_server vf_server;
+
+/* Fracture parameters: the hot-path fields of FractureParameters
+ * (FractureParameters.h:43-85, defaults :91-145). */
+typedef struct vf_params {
+  int32_t algorithm;          /* _fractureAlgorithm: VF_FLOOD | VF_NAIVE */
+  int32_t distance;           /* _distanceFunction */
+  int32_t num_seeds;          /* _numSeeds (fragments, <= 254) */
+  int32_t num_extra_seeds;    /* _numExtraSeeds (sub-seeds merged into fragments) */
+  int32_t merge_distance;     /* _mergeSeedsDistanceFunction */
+  int32_t seed_location;      /* Seeder::Location of the main seeds */
+  uint64_t seed;              /* _seed: all random draws derive from it */
+  float noise_amplitude;      /* boundary perturbation, voxels (0 = off) */
+  uint32_t noise_period;      /* perturbation noise lattice period, voxels */
+  int32_t erode;              /* _erode */
+  int32_t erosion_type;       /* _erosionConvolution */
+  int32_t erosion_size;       /* _erosionSize */
+  int32_t erosion_iterations; /* _erosionIterations */
+  float erosion_probability;  /* _erosionProbability */
+  float erosion_threshold;    /* _erosionThreshold */
+  int32_t boundary_size;      /* detectBoundaries(1) when not eroding */
+} vf_params;
+
+/* FractureParameters() defaults (FractureParameters.h:91-145), with
+ * num_extra_seeds 0 and seed_location VF_OUTER as in CADScene.cpp:633. */
+void vf_params_default(vf_params* p);
+
+const char* vf_last_error(void);
+const char* vf_status_string(vf_status s);
+/* library version string and the GPU architecture it was built for */
+const char* vf_version(void);
+
+/* ---- context ------------------------------------------------------------
+ * hbm_budget: bytes of device memory the context may hold (0 = 90% of free).
+ * Replaces the GL context + ComputeShader runtime (ComputeShader.h:74-190). */
+vf_status vf_ctx_create(int device, size_t hbm_budget, vf_ctx** out);
+vf_status vf_ctx_destroy(vf_ctx* ctx);
+vf_status vf_ctx_synchronize(vf_ctx* ctx);
+/* bytes currently held by grids and scratch */
+size_t vf_ctx_bytes_in_use(const vf_ctx* ctx);
+/* pinned host memory for fast uploads/downloads (cudaMallocHost) */
+void* vf_host_alloc(size_t bytes);
+void vf_host_free(void* p);
+
+/* ---- grid (RegularGrid) --------------------------------------------------
+ * RegularGrid(aabb, subdivisions) + setAABB (RegularGrid.cpp:21-27, 426-441):
+ * cellSize = (aabb_max - aabb_min) / dims. */
+vf_status vf_grid_create(vf_ctx* ctx, uint32_t X, uint32_t Y, uint32_t Z,
+                         const float aabb_min[3], const float aabb_max[3],
+                         vf_grid** out);
+vf_status vf_grid_destroy(vf_grid* g);
+vf_status vf_grid_dims(const vf_grid* g, uint32_t dims[3]);
+/* CADScene::allocateMeshGrid dims rule (CADScene.cpp:545-561) */
+vf_status vf_dims_for_aabb(const float aabb_min[3], const float aabb_max[3],
+                           uint32_t max_voxels, uint32_t dims_out[3]);
+/* RegularGrid::updateSSBO / updateGrid (RegularGrid.cpp:505-515) */
+vf_status vf_grid_upload(vf_grid* g, const uint16_t* host_grid);
+vf_status vf_grid_download(vf_grid* g, uint16_t* host_grid);
+
+/* RegularGrid::fill(Model3D*) (RegularGrid.cpp:173-212): occupancy = FP32
+ * tri-box SAT shell (Intersections3D.h:204-258) OR tetra-parity interior
+ * (Tetravoxelizer.cpp:42-92, 198-315).  verts: 3 floats per vertex, faces:
+ * 3 uint32 per triangle, host memory.  Writes 0/1 into the grid. */
+vf_status vf_voxelize(vf_grid* g, const float* verts, uint32_t nverts,
+                      const uint32_t* faces, uint32_t nfaces);
+
+/* Seeder::uniform (Seeder.cpp:154-208): n distinct occupied voxels, labels
+ * 2..n+1 in (x,y,z) order.  out_xyzw: 4*n uint32, host. */
+vf_status vf_sample_seeds(vf_grid* g, uint32_t n, uint64_t seed, int location,
+                          uint32_t* out_xyzw);
+/* Seeder::mergeSeeds (Seeder.cpp:115-152), host computation. */
+vf_status vf_merge_seeds(const uint32_t* frags_xyzw, uint32_t nfrags,
+                         uint32_t* seeds_xyzw, uint32_t nseeds, int distance);
+/* CADScene::fractureModel seed assembly (CADScene.cpp:628-655):
+ * uniform(main, location) [+ uniform(extra, BOTH) + mergeSeeds].  out
+ * holds 4*(2*num_seeds + num_extra_seeds) uint32; *nout gets the count. */
+vf_status vf_fracture_seeds(vf_grid* g, const vf_params* p, uint32_t* out_xyzw,
+                            uint32_t* nout);
+
+/* Fracturer::build (Fracturer.h:35): VF_FLOOD = FloodFracturer::build
+ * (FloodFracturer.cpp:98-191: homogenize, seed, BFS waves, disjoint
+ * cleanup, undoMask); VF_NAIVE = NaiveFracturer::build (CPU path
+ * NaiveFracturer.cpp:26-68).  seeds_xyzw: 4*nseeds uint32, host.
+ * Same-wave flood ties go to the lowest seed index. */
+vf_status vf_fracture(vf_grid* g, int algorithm, int distance,
+                      const uint32_t* seeds_xyzw, uint32_t nseeds);
+/* reference-shaped flood: one kernel launch and one host read of the
+ * frontier size per BFS wave, as FloodFracturer.cpp:143-158 does.  Same
+ * result as vf_fracture(VF_FLOOD); used as the plain comparator. */
+vf_status vf_fracture_plain(vf_grid* g, int distance, const uint32_t* seeds_xyzw,
+                            uint32_t nseeds, uint32_t* waves_out);
+
+/* Boundary perturbation by seeded 3-D value noise (no reference
+ * counterpart): labelled voxels take the label found at v + round(A*n(v/P)). */
+vf_status vf_perturb(vf_grid* g, float amplitude, uint32_t period, uint64_t seed);
+/* RegularGrid::detectBoundaries (RegularGrid.cpp:64-80) */
+vf_status vf_detect_boundaries(vf_grid* g, int boundary_size);
+/* RegularGrid::erode (RegularGrid.cpp:82-159) incl. removeIsolatedRegions */
+vf_status vf_erode(vf_grid* g, int type, uint32_t size, uint32_t iterations,
+                   float probability, float threshold, uint64_t seed);
+/* removeIsolatedRegionsGrid-comp.glsl:16-39 (RegularGrid.cpp:1006-1015) */
+vf_status vf_remove_isolated(vf_grid* g);
+/* RegularGrid::undoMask (RegularGrid.cpp:488-503): clear bit 15 */
+vf_status vf_undo_mask(vf_grid* g);
+/* RegularGrid::countValues (RegularGrid.cpp:601-625): counts[v] for values
+ * v = label & 0x7FFF > 1.  counts: ncounts uint32 (host); *occupied = sum.
+ * VF_ERR_RANGE if a label >= ncounts occurs (its count is dropped). */
+vf_status vf_count_values(vf_grid* g, uint32_t* counts, uint32_t ncounts,
+                          uint64_t* occupied);
+
+/* CADScene::fractureModel (CADScene.cpp:624-691) on an already voxelized
+ * grid: seeds -> fracture -> [perturb] -> erode | detectBoundaries.  The
+ * seeds used are returned when seeds_out (4*(2n+extra) uint32) is given. */
+vf_status vf_fracture_model(vf_grid* g, const vf_params* p, uint32_t* seeds_out,
+                            uint32_t* nseeds_out);
+
+/* ---- jobs: whole pipeline from a mesh ------------------------------------ */
+typedef struct vf_job {
+  const float* verts;      /* host, 3 floats per vertex */
+  uint32_t nverts;
+  const uint32_t* faces;   /* host, 3 uint32 per triangle */
+  uint32_t nfaces;
+  uint32_t dims[3];        /* grid dims; all 0 => allocateMeshGrid(max_dim) */
+  uint32_t max_dim;        /* used when dims are 0 */
+  float aabb_min[3];       /* grid AABB; min == max => mesh AABB */
+  float aabb_max[3];
+  vf_params params;
+  uint16_t* out_labels;    /* host X*Y*Z uint16 or NULL */
+  uint32_t* out_counts;    /* host ncounts uint32 or NULL */
+  uint32_t ncounts;
+  uint64_t user_tag;       /* returned in the result */
+} vf_job;
+
+typedef struct vf_job_result {
+  vf_status status;
+  uint32_t dims[3];
+  uint32_t nseeds;
+  uint64_t voxels;         /* X*Y*Z */
+  uint64_t occupied;       /* labelled voxels after the pipeline */
+  uint32_t fragments;      /* distinct labels counted */
+  uint32_t flood_passes;   /* brick passes (batched) or BFS waves (plain) */
+  double submit_ms;        /* server: submit time, ms since server start */
+  double done_ms;          /* server: result-on-host time */
+  uint64_t user_tag;
+} vf_job_result;
+
+/* Batched path: all jobs packed into one brick work-queue per stage
+ * (voxelize, seed, flood, perturb, erode/boundaries, count), persistent
+ * kernels, labels and counts copied back to the jobs' host buffers. */
+vf_status vf_batch_run(vf_ctx* ctx, const vf_job* jobs, uint32_t njobs,
+                       vf_job_result* results);
+/* Plain path: one job at a time, stage by stage, flood as one launch plus a
+ * host read per BFS wave (the reference's execution shape). */
+vf_status vf_plain_run(vf_ctx* ctx, const vf_job* jobs, uint32_t njobs,
+                       vf_job_result* results);
+/* device bytes vf_batch_run needs for these jobs (admission control) */
+size_t vf_job_footprint(const vf_job* job);
+
+/* ---- serving: continuous batching ---------------------------------------
+ * A server thread admits submitted jobs against hbm_budget, packs the
+ * admitted ones into micro-batches on up to max_inflight streams, keeps
+ * grids resident between stages and streams labels back.  The job's host
+ * buffers must stay valid until its result is polled. */
+vf_status vf_server_create(vf_ctx* ctx, size_t hbm_budget, uint32_t max_inflight,
+                           uint32_t max_batch_jobs, vf_server** out);
+vf_status vf_server_submit(vf_server* s, const vf_job* job, uint64_t* ticket);
+/* waits up to wait_ms for results; *n = results written (<= max) */
+vf_status vf_server_poll(vf_server* s, vf_job_result* out, uint32_t max,
+                         uint32_t* n, int wait_ms);
+vf_status vf_server_destroy(vf_server* s);
+
+/* ---- timing helpers for benchmarks (CUDA events on the context stream) --- */
+vf_status vf_ctx_event_record(vf_ctx* ctx, int slot);
+vf_status vf_ctx_event_elapsed(vf_ctx* ctx, int slot_a, int slot_b, float* ms);
+/* per-kernel statistics of the last vf_batch_run: launches and device ms of
+ * the flood relaxation kernel (for the roofline) */
+vf_status vf_ctx_last_stats(vf_ctx* ctx, uint64_t* kernel_launches,
+                            float* flood_ms, uint64_t* flood_bytes,
+                            uint64_t* flood_brick_visits);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,324 @@
+"""GPU parity: every stage of the CUDA path, called through the C ABI,
+bit-exact against the CPU oracle on the same seeded inputs, and every
+golden case end to end (batched and plain paths).
+
+Tolerance: none.  Labels, occupancy and counts are integer results and must
+be identical; the float parts (tri-box SAT, tetra cross-sections, noise,
+erosion activation) round exactly as the oracle does.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from voxelfragmentml_gb300 import vessel as Vs
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _mg():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLD, "make_golden.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m
+
+
+CASES = sorted(json.load(open(os.path.join(GOLD, "cases.json"))))
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _oracle(oracle_lib):
+    return oracle_lib
+
+
+# (angular, profile, mesh seed, max_dim): includes Z % 8 == 4 and dims that
+# are not multiples of the 16x16x32 brick
+VOX_CASES = [(32, 24, 1, 32), (48, 36, 2, 60), (64, 48, 3, 76), (96, 72, 4, 100), (40, 30, 5, 44)]
+
+
+def _mesh(A, P, ms, md):
+    v, f = Vs.vessel_mesh(A, P, ms)
+    mn, mx = Vs.mesh_aabb(v)
+    return v, f, mn, mx, Vs.grid_dims(mn, mx, md)
+
+
+@pytest.mark.parametrize("case", VOX_CASES)
+def test_voxelize(vf, ctx, case):
+    v, f, mn, mx, dims = _mesh(*case)
+    g = vf.RegularGrid(dims, mn, mx, ctx)
+    g.fill(v, f)
+    got = g.data()
+    exp = O.voxelize(v, f, dims, mn, mx)
+    assert np.array_equal(got, exp), f"{int((got != exp).sum())} voxels differ"
+
+
+def test_voxelize_anisotropic_cells(vf, ctx):
+    v, f = Vs.vessel_mesh(40, 30, 9)
+    mn, mx = Vs.mesh_aabb(v)
+    dims = (36, 52, 28)  # cells are not cubes
+    g = vf.RegularGrid(dims, mn, mx, ctx)
+    g.fill(v, f)
+    assert np.array_equal(g.data(), O.voxelize(v, f, dims, mn, mx))
+
+
+@pytest.fixture(scope="module")
+def occ64(vf, ctx):
+    v, f, mn, mx, dims = _mesh(64, 48, 3, 64)
+    return O.voxelize(v, f, dims, mn, mx), mn, mx
+
+
+@pytest.mark.parametrize("loc", [0, 1, 2])
+def test_seeds(vf, ctx, occ64, loc):
+    occ, mn, mx = occ64
+    g = vf.RegularGrid(occ.shape, mn, mx, ctx)
+    g.upload(occ)
+    n = 3 if loc == 0 else 24
+    got = vf.Seeder.uniform(g, n, 1234 + loc, loc)
+    exp = O.seeder_uniform(occ, n, 1234 + loc, loc)
+    assert np.array_equal(got, exp)
+
+
+def test_fracture_seeds_with_extra(vf, ctx, occ64):
+    occ, mn, mx = occ64
+    g = vf.RegularGrid(occ.shape, mn, mx, ctx)
+    g.upload(occ)
+    p = vf.Params.default(num_seeds=7, num_extra_seeds=14, seed=5, seed_location=vf.BOTH,
+                          merge_distance=vf.MANHATTAN)
+    got = vf.Seeder.fracture_seeds(g, p)
+    exp = O.fracture_seeds(occ, 7, 14, vf.BOTH, vf.MANHATTAN, 5)
+    assert np.array_equal(got, exp)
+
+
+def test_seed_search_error(vf, ctx):
+    occ = np.zeros((16, 16, 16), np.uint16)
+    occ[4, 4, 4] = 1
+    g = vf.RegularGrid(occ.shape, None, None, ctx)
+    g.upload(occ)
+    with pytest.raises(vf.VFError) as e:
+        vf.Seeder.uniform(g, 2, 1, vf.BOTH)
+    assert e.value.status == vf.ERR_SEED_SEARCH
+
+
+@pytest.mark.parametrize("dfunc", [0, 1, 2])
+@pytest.mark.parametrize("nseeds", [1, 8, 40])
+def test_flood_vessel(vf, ctx, occ64, dfunc, nseeds):
+    occ, mn, mx = occ64
+    seeds = O.seeder_uniform(occ, nseeds, 77 + nseeds, 2)
+    g = vf.RegularGrid(occ.shape, mn, mx, ctx)
+    g.upload(occ)
+    fr = vf.FloodFracturer()
+    fr.setDistanceFunction(dfunc)
+    fr.build(g, seeds)
+    exp, _ = O.flood(occ, seeds, dfunc)
+    got = g.data()
+    assert np.array_equal(got, exp), f"{int((got != exp).sum())} voxels differ"
+
+
+@pytest.mark.parametrize("dfunc", [1, 2])
+def test_flood_plain_matches_oracle(vf, ctx, occ64, dfunc):
+    occ, mn, mx = occ64
+    seeds = O.seeder_uniform(occ, 9, 5, 2)
+    g = vf.RegularGrid(occ.shape, mn, mx, ctx)
+    g.upload(occ)
+    fr = vf.FloodFracturer()
+    fr.setDistanceFunction(dfunc)
+    waves = fr.build_plain(g, seeds)
+    exp, ewaves = O.flood(occ, seeds, dfunc)
+    assert np.array_equal(g.data(), exp)
+    assert waves == ewaves  # same number of BFS waves as the oracle
+
+
+@pytest.mark.parametrize("shape,frac,gseed", [((37, 29, 45), 0.55, 0), ((70, 18, 66), 0.7, 1),
+                                              ((20, 90, 36), 0.62, 2)])
+@pytest.mark.parametrize("dfunc", [1, 2])
+def test_flood_random_grids(vf, ctx, shape, frac, gseed, dfunc):
+    rng = np.random.default_rng(gseed)
+    occ = (rng.random(shape) < frac).astype(np.uint16)
+    seeds = O.seeder_uniform(occ, 12, gseed, 2)
+    g = vf.RegularGrid(shape, None, None, ctx)
+    g.upload(occ)
+    fr = vf.FloodFracturer()
+    fr.setDistanceFunction(dfunc)
+    fr.build(g, seeds)
+    exp, _ = O.flood(occ, seeds, dfunc)
+    assert np.array_equal(g.data(), exp)
+
+
+def test_flood_maze_long_paths(vf, ctx):
+    """A serpentine corridor: geodesic distances far above the brick size,
+    many passes, and a tie in the middle."""
+    X, Y, Z = 40, 34, 70
+    occ = np.zeros((X, Y, Z), np.uint16)
+    for y in range(0, Y, 2):
+        occ[:, y, :] = 1
+        if y + 1 < Y:
+            occ[:, y + 1, (Z - 1) if (y // 2) % 2 == 0 else 0] = 1
+    seeds = np.array([[3, 0, 0, 2], [5, Y - 1, Z - 1, 3]], np.uint32)
+    g = vf.RegularGrid(occ.shape, None, None, ctx)
+    g.upload(occ)
+    fr = vf.FloodFracturer()
+    fr.setDistanceFunction(vf.MANHATTAN)
+    fr.build(g, seeds)
+    exp, waves = O.flood(occ, seeds, 1)
+    assert waves > 500
+    assert np.array_equal(g.data(), exp)
+
+
+def test_flood_extra_seed_prefixes(vf, ctx, occ64):
+    occ, mn, mx = occ64
+    seeds = O.fracture_seeds(occ, 6, 14, 2, 0, 99)
+    assert (seeds[:, 3] > 255).any()
+    for dfunc in (1, 2):
+        g = vf.RegularGrid(occ.shape, mn, mx, ctx)
+        g.upload(occ)
+        fr = vf.FloodFracturer()
+        fr.setDistanceFunction(dfunc)
+        fr.build(g, seeds)
+        exp, _ = O.flood(occ, seeds, dfunc)
+        assert np.array_equal(g.data(), exp)
+        g2 = vf.RegularGrid(occ.shape, mn, mx, ctx)
+        g2.upload(occ)
+        fr.build_plain(g2, seeds)
+        assert np.array_equal(g2.data(), exp)
+
+
+def test_flood_seed_on_empty_voxel(vf, ctx):
+    occ = np.zeros((20, 20, 40), np.uint16)
+    occ[2:18, 2:18, 2:38] = 1
+    seeds = np.array([[0, 0, 0, 2], [10, 10, 20, 3]], np.uint32)  # first seed outside
+    g = vf.RegularGrid(occ.shape, None, None, ctx)
+    g.upload(occ)
+    vf.FloodFracturer().build(g, seeds, vf.Params.default(distance=vf.CHEBYSHEV))
+    exp, _ = O.flood(occ, seeds, 2)
+    assert np.array_equal(g.data(), exp)
+
+
+@pytest.mark.parametrize("dfunc", [0, 1, 2])
+def test_naive(vf, ctx, occ64, dfunc):
+    occ, mn, mx = occ64
+    seeds = O.seeder_uniform(occ, 33, 4, 2)
+    g = vf.RegularGrid(occ.shape, mn, mx, ctx)
+    g.upload(occ)
+    vf.NaiveFracturer().build(g, seeds, vf.Params.default(distance=dfunc))
+    assert np.array_equal(g.data(), O.naive(occ, seeds, dfunc))
+
+
+@pytest.fixture(scope="module")
+def labelled64(occ64):
+    occ, mn, mx = occ64
+    seeds = O.seeder_uniform(occ, 10, 3, 2)
+    lab, _ = O.flood(occ, seeds, 2)
+    return lab, mn, mx
+
+
+@pytest.mark.parametrize("amp,period,seed", [(2.0, 16, 1), (1.0, 4, 2), (3.0, 7, 3), (0.6, 1, 4)])
+def test_perturb(vf, ctx, labelled64, amp, period, seed):
+    lab, mn, mx = labelled64
+    g = vf.RegularGrid(lab.shape, mn, mx, ctx)
+    g.upload(lab)
+    g.perturb(amp, period, seed)
+    assert np.array_equal(g.data(), O.perturb(lab, amp, period, seed))
+
+
+@pytest.mark.parametrize("bs", [0, 1, 2, 3])
+def test_detect_boundaries(vf, ctx, labelled64, bs):
+    lab, mn, mx = labelled64
+    g = vf.RegularGrid(lab.shape, mn, mx, ctx)
+    g.upload(lab)
+    g.detectBoundaries(bs)
+    assert np.array_equal(g.data(), O.detect_boundaries(lab, bs))
+
+
+@pytest.mark.parametrize("etype,size,iters,p,thr", [(0, 3, 1, 0.5, 0.5), (1, 3, 3, 0.5, 0.5),
+                                                    (2, 5, 2, 0.8, 0.4), (0, 7, 1, 1.0, 0.6),
+                                                    (1, 4, 1, 0.3, 0.5)])
+def test_erode(vf, ctx, labelled64, etype, size, iters, p, thr):
+    lab, mn, mx = labelled64
+    g = vf.RegularGrid(lab.shape, mn, mx, ctx)
+    g.upload(lab)
+    g.erode(etype, size, iters, p, thr, 17)
+    exp = O.erode(lab, etype, size, iters, p, thr, 17)
+    got = g.data()
+    assert np.array_equal(got, exp), f"{int((got != exp).sum())} voxels differ"
+
+
+def test_remove_isolated_and_undo_mask(vf, ctx, labelled64):
+    lab, mn, mx = labelled64
+    b = O.detect_boundaries(lab)
+    g = vf.RegularGrid(lab.shape, mn, mx, ctx)
+    g.upload(b)
+    g.removeIsolatedRegions()
+    assert np.array_equal(g.data(), O.remove_isolated(b))
+    g.undoMask()
+    assert np.array_equal(g.data(), O.undo_mask(O.remove_isolated(b)))
+
+
+def test_counts(vf, ctx, labelled64):
+    lab, mn, mx = labelled64
+    b = O.detect_boundaries(lab)
+    b[0, 0, 0] = 700  # a value above 255 goes through the global bins
+    g = vf.RegularGrid(lab.shape, mn, mx, ctx)
+    g.upload(b)
+    c, occ = g.countValues(1024)
+    ec, eocc = O.count_values(b, 1024)
+    assert occ == eocc and np.array_equal(c, ec)
+    with pytest.raises(vf.VFError) as e:
+        g.countValues(256)
+    assert e.value.status == vf.ERR_RANGE
+
+
+def test_fracture_model(vf, ctx):
+    mg = _mg()
+    v, f, mn, mx, dims, p, kw = mg.case_inputs("flood_euclid_noise_erode_64")
+    g = vf.RegularGrid(dims, mn, mx, ctx)
+    g.fill(v, f)
+    params = vf.Params.default(**kw)
+    seeds = vf.fracture_model(g, params)
+    gold = np.load(os.path.join(GOLD, "flood_euclid_noise_erode_64.npz"))
+    assert np.array_equal(seeds, gold["seeds"])
+    assert np.array_equal(g.data(), gold["labels"])
+
+
+# ---- golden cases end to end ------------------------------------------------
+def _spec(vf, name):
+    mg = _mg()
+    v, f, mn, mx, dims, p, kw = mg.case_inputs(name)
+    meta = json.load(open(os.path.join(GOLD, "cases.json")))[name]
+    assert mg.mesh_sha(v, f) == meta["mesh_sha256"]
+    return vf.JobSpec(v, f, vf.Params.default(**kw), dims=dims, aabb=(mn, mx), ncounts=1024)
+
+
+def _check_gold(name, spec, res):
+    gold = np.load(os.path.join(GOLD, name + ".npz"))
+    assert res.status == 0
+    assert np.array_equal(spec.labels, gold["labels"]), name
+    nz = np.nonzero(spec.counts)[0]
+    assert np.array_equal(nz, gold["count_values"]) and np.array_equal(spec.counts[nz],
+                                                                          gold["count_numbers"])
+    assert res.nseeds == gold["seeds"].shape[0]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_golden_batched(vf, ctx, name):
+    spec = _spec(vf, name)
+    (res,) = vf.batch_run([spec], ctx)
+    _check_gold(name, spec, res)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_golden_plain(vf, ctx, name):
+    spec = _spec(vf, name)
+    (res,) = vf.plain_run([spec], ctx)
+    _check_gold(name, spec, res)
+
+
+def test_golden_all_in_one_batch(vf, ctx):
+    specs = [_spec(vf, n) for n in CASES]
+    res = vf.batch_run(specs, ctx)
+    for n, s, r in zip(CASES, specs, res):
+        _check_gold(n, s, r)

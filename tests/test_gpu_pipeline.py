@@ -1,0 +1,149 @@
+"""GPU tests of the job runners: mixed batches of uneven jobs, the server
+(continuous batching), determinism alone vs in a mix, admission control and
+error statuses."""
+import os
+import time
+
+import numpy as np
+import pytest
+
+import oracle as O
+from voxelfragmentml_gb300 import vessel as Vs
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _oracle(oracle_lib):
+    return oracle_lib
+
+
+def _job(vf, i, ncounts=512):
+    """A small job of the mixed workload: uneven dims, metric and noise drawn
+    per job."""
+    rng = np.random.default_rng(1000 + i)
+    tris = int(rng.integers(1500, 12000))
+    A, P = Vs.samples_for_triangles(tris)
+    v, f = Vs.vessel_mesh(A, P, 500 + i)
+    mn, mx = Vs.mesh_aabb(v)
+    dims = tuple(int(4 * round(d / 4)) for d in np.exp(rng.uniform(np.log(24), np.log(72), 3)))
+    p = vf.Params.default(
+        algorithm=vf.FLOOD if i % 5 else vf.NAIVE, distance=int(rng.integers(0, 3)),
+        num_seeds=int(rng.integers(2, 12)), seed=7 + i, seed_location=vf.BOTH,
+        noise_amplitude=float(rng.uniform(0, 3)) if i % 3 else 0.0, noise_period=16,
+        erode=int(i % 4 == 1), erosion_type=int(rng.integers(0, 3)), erosion_iterations=1)
+    return vf.JobSpec(v, f, p, dims=dims, aabb=(mn, mx), ncounts=ncounts, tag=i)
+
+
+def _oracle_job(spec):
+    P = spec.params
+    q = O.Params()
+    for name, _ in O.Params._fields_:
+        setattr(q, name, getattr(P, name))
+    return O.run_job(spec.verts, spec.faces, spec.dims, spec.aabb[0], spec.aabb[1], q,
+                     ncounts=spec.counts.shape[0])
+
+
+def test_mixed_batch_matches_oracle_and_alone(vf, ctx):
+    specs = [_job(vf, i) for i in range(14)]
+    res = vf.batch_run(specs, ctx)
+    for s, r in zip(specs, res):
+        assert r.status == 0
+        lab, cnt, seeds = _oracle_job(s)
+        assert np.array_equal(s.labels, lab), f"job {s.tag}"
+        assert np.array_equal(s.counts, cnt)
+        assert r.voxels == int(np.prod(s.dims)) and r.occupied == int(cnt.sum())
+    # the same job alone gives the same bits
+    for i in (0, 5, 9):
+        alone = _job(vf, i)
+        (r,) = vf.batch_run([alone], ctx)
+        assert np.array_equal(alone.labels, specs[i].labels)
+
+
+def test_plain_matches_batched(vf, ctx):
+    specs = [_job(vf, i) for i in range(6)]
+    plain = [_job(vf, i) for i in range(6)]
+    vf.batch_run(specs, ctx)
+    res = vf.plain_run(plain, ctx)
+    for a, b, r in zip(specs, plain, res):
+        assert r.status == 0
+        assert np.array_equal(a.labels, b.labels) and np.array_equal(a.counts, b.counts)
+
+
+def test_server_continuous_batching_same_results(vf, ctx):
+    specs = [_job(vf, i) for i in range(20)]
+    ref = [_job(vf, i) for i in range(20)]
+    vf.batch_run(ref, ctx)
+    srv = vf.Server(ctx, max_inflight=3, max_batch=4)
+    try:
+        got = []
+        for s in specs[:8]:
+            srv.submit(s)
+        time.sleep(0.01)
+        for s in specs[8:]:  # arrive while the first micro-batches run
+            srv.submit(s)
+        deadline = time.time() + 120
+        while len(got) < len(specs) and time.time() < deadline:
+            got += srv.poll(64, wait_ms=100)
+        assert len(got) == len(specs)
+        for r in got:
+            assert r.status == 0
+            assert r.done_ms >= r.submit_ms
+            s = specs[r.user_tag]
+            assert np.array_equal(s.labels, ref[r.user_tag].labels)
+            assert np.array_equal(s.counts, ref[r.user_tag].counts)
+    finally:
+        srv.close()
+
+
+def test_server_admission_respects_budget(vf, ctx):
+    specs = [_job(vf, i) for i in range(6)]
+    srv = vf.Server(ctx, hbm_budget=1, max_inflight=2, max_batch=8)  # admits one job at a time
+    try:
+        for s in specs:
+            srv.submit(s)
+        got = []
+        deadline = time.time() + 120
+        while len(got) < len(specs) and time.time() < deadline:
+            got += srv.poll(64, wait_ms=100)
+        assert len(got) == len(specs) and all(r.status == 0 for r in got)
+    finally:
+        srv.close()
+
+
+def test_job_errors_are_statuses(vf, ctx):
+    ok = _job(vf, 2)
+    bad = _job(vf, 3)
+    bad.params.num_seeds = 300  # above 254 fragment ids
+    with pytest.raises(vf.VFError) as e:
+        vf.batch_run([ok, bad], ctx)
+    assert e.value.status == vf.ERR_RANGE
+    # a job whose seeds cannot be found fails alone; the rest of the batch is fine
+    tiny = _job(vf, 4)
+    tiny.verts = (tiny.verts * 0.01).astype(np.float32)  # mesh far smaller than its grid
+    tiny.params.num_seeds = 200
+    res = vf.batch_run([_job(vf, 6), tiny], ctx)
+    assert res[0].status == 0 and res[1].status == vf.ERR_SEED_SEARCH
+
+
+def test_context_budget_oom(vf):
+    c = vf.Context(0, hbm_budget=1 << 20)
+    try:
+        with pytest.raises(vf.VFError) as e:
+            vf.batch_run([_job(vf, 1)], c)
+        assert e.value.status == vf.ERR_OOM
+    finally:
+        c.close()
+
+
+def test_config1_vessel_128(vf, ctx):
+    """128-max-dim vessel, 8 fragments, Manhattan flood, seed 42 (the
+    CPU-runnable configuration) against the oracle."""
+    v, f = Vs.vessel_mesh(128, 96, 42)
+    mn, mx = Vs.mesh_aabb(v)
+    dims = Vs.grid_dims(mn, mx, 128)
+    p = vf.Params.default(distance=vf.MANHATTAN, num_seeds=8, seed=42, seed_location=vf.BOTH)
+    spec = vf.JobSpec(v, f, p, dims=dims, aabb=(mn, mx), ncounts=256)
+    (r,) = vf.batch_run([spec], ctx)
+    lab, cnt, _ = _oracle_job(spec)
+    assert r.status == 0 and np.array_equal(spec.labels, lab) and np.array_equal(spec.counts, cnt)

@@ -1,0 +1,442 @@
+"""GB300 voxelize -> seed -> fracture -> perturb/erode -> count pipeline.
+
+Python binding of the C ABI in include/vf.h (library
+voxelfragmentml_gb300/_build/libvfgb300.so, built by build.py for
+sm_103a).  The classes mirror the reference's interface:
+
+* :class:`RegularGrid`  -- RegularGrid (DataStructures/RegularGrid.h): fill,
+  detectBoundaries, erode, undoMask, countValues, data;
+* :class:`Seeder`       -- Seeder::uniform / mergeSeeds (Fracturer/Seeder.h);
+* :class:`FloodFracturer`, :class:`NaiveFracturer` -- Fracturer::build
+  (Fracturer/Fracturer.h:28-57);
+* :func:`fracture_model` -- CADScene::fractureModel;
+* :func:`batch_run`, :func:`plain_run`, :class:`Server` -- whole jobs.
+
+There is no CPU fallback: every call runs on the GPU through the library,
+and loading fails with an error when the library or a GPU is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import vessel  # noqa: F401  (synthetic inputs)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libvfgb300.so")
+
+OK, ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_SEED_SEARCH, ERR_RANGE, ERR_TIMEOUT, \
+    ERR_NOT_BUILT, ERR_BUSY = range(9)
+NAIVE, FLOOD = 0, 1
+EUCLIDEAN, MANHATTAN, CHEBYSHEV = 0, 1, 2
+SQUARE, ELLIPSE, CROSS = 0, 1, 2
+INNER, OUTER, BOTH = 0, 1, 2
+MAX_SEEDS = 4095
+
+
+class VFError(RuntimeError):
+    """A non-zero vf_status from the library."""
+
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"[{status}] {msg}")
+        self.status = status
+
+
+class Params(C.Structure):
+    """vf_params: the hot-path fields of FractureParameters."""
+    _fields_ = [("algorithm", C.c_int32), ("distance", C.c_int32),
+                ("num_seeds", C.c_int32), ("num_extra_seeds", C.c_int32),
+                ("merge_distance", C.c_int32), ("seed_location", C.c_int32),
+                ("seed", C.c_uint64), ("noise_amplitude", C.c_float),
+                ("noise_period", C.c_uint32), ("erode", C.c_int32),
+                ("erosion_type", C.c_int32), ("erosion_size", C.c_int32),
+                ("erosion_iterations", C.c_int32),
+                ("erosion_probability", C.c_float),
+                ("erosion_threshold", C.c_float), ("boundary_size", C.c_int32)]
+
+    @classmethod
+    def default(cls, **kw) -> "Params":
+        p = cls()
+        lib().vf_params_default(C.byref(p))
+        for k, v in kw.items():
+            setattr(p, k, v)
+        return p
+
+
+class Job(C.Structure):
+    _fields_ = [("verts", C.c_void_p), ("nverts", C.c_uint32),
+                ("faces", C.c_void_p), ("nfaces", C.c_uint32),
+                ("dims", C.c_uint32 * 3), ("max_dim", C.c_uint32),
+                ("aabb_min", C.c_float * 3), ("aabb_max", C.c_float * 3),
+                ("params", Params), ("out_labels", C.c_void_p),
+                ("out_counts", C.c_void_p), ("ncounts", C.c_uint32),
+                ("user_tag", C.c_uint64)]
+
+
+class JobResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("dims", C.c_uint32 * 3), ("nseeds", C.c_uint32),
+                ("voxels", C.c_uint64), ("occupied", C.c_uint64),
+                ("fragments", C.c_uint32), ("flood_passes", C.c_uint32),
+                ("submit_ms", C.c_double), ("done_ms", C.c_double),
+                ("user_tag", C.c_uint64)]
+
+
+EXPORTS = {
+    "vf_params_default": (None, [C.c_void_p]),
+    "vf_last_error": (C.c_char_p, []),
+    "vf_status_string": (C.c_char_p, [C.c_int]),
+    "vf_version": (C.c_char_p, []),
+    "vf_ctx_create": (C.c_int, [C.c_int, C.c_size_t, C.c_void_p]),
+    "vf_ctx_destroy": (C.c_int, [C.c_void_p]),
+    "vf_ctx_synchronize": (C.c_int, [C.c_void_p]),
+    "vf_ctx_bytes_in_use": (C.c_size_t, [C.c_void_p]),
+    "vf_host_alloc": (C.c_void_p, [C.c_size_t]),
+    "vf_host_free": (None, [C.c_void_p]),
+    "vf_grid_create": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
+                                 C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vf_grid_destroy": (C.c_int, [C.c_void_p]),
+    "vf_grid_dims": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "vf_dims_for_aabb": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "vf_grid_upload": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "vf_grid_download": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "vf_voxelize": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
+    "vf_sample_seeds": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64, C.c_int, C.c_void_p]),
+    "vf_merge_seeds": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_int]),
+    "vf_fracture_seeds": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vf_fracture": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_uint32]),
+    "vf_fracture_plain": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "vf_perturb": (C.c_int, [C.c_void_p, C.c_float, C.c_uint32, C.c_uint64]),
+    "vf_detect_boundaries": (C.c_int, [C.c_void_p, C.c_int]),
+    "vf_erode": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, C.c_uint32, C.c_float,
+                           C.c_float, C.c_uint64]),
+    "vf_remove_isolated": (C.c_int, [C.c_void_p]),
+    "vf_undo_mask": (C.c_int, [C.c_void_p]),
+    "vf_count_values": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "vf_fracture_model": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vf_job_footprint": (C.c_size_t, [C.c_void_p]),
+    "vf_batch_run": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "vf_plain_run": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "vf_server_create": (C.c_int, [C.c_void_p, C.c_size_t, C.c_uint32, C.c_uint32, C.c_void_p]),
+    "vf_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vf_server_poll": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int]),
+    "vf_server_destroy": (C.c_int, [C.c_void_p]),
+    "vf_ctx_event_record": (C.c_int, [C.c_void_p, C.c_int]),
+    "vf_ctx_event_elapsed": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+    "vf_ctx_last_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libvfgb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise VFError(ERR_NOT_BUILT,
+                          f"{LIB_PATH} is missing: run voxelfragmentml_gb300.build.build()")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in EXPORTS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status: int):
+    if status != OK:
+        msg = lib().vf_last_error()
+        raise VFError(status, msg.decode() if msg else "error")
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def _f3(v):
+    return np.ascontiguousarray(np.asarray(v, dtype=np.float32).reshape(3))
+
+
+class Context:
+    """vf_ctx: one device, one stream, an HBM budget."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        h = C.c_void_p()
+        _check(lib().vf_ctx_create(device, hbm_budget, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().vf_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def synchronize(self):
+        _check(lib().vf_ctx_synchronize(self.h))
+
+    @property
+    def bytes_in_use(self) -> int:
+        return lib().vf_ctx_bytes_in_use(self.h)
+
+    def last_stats(self):
+        la, vis, by = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        ms = C.c_float()
+        _check(lib().vf_ctx_last_stats(self.h, C.byref(la), C.byref(ms), C.byref(by), C.byref(vis)))
+        return {"launches": la.value, "flood_ms": ms.value, "flood_bytes": by.value,
+                "flood_visits": vis.value}
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+class RegularGrid:
+    """Device-resident uint16 label grid, x-major (RegularGrid.h:142-367)."""
+
+    def __init__(self, dims, aabb_min=None, aabb_max=None, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        X, Y, Z = (int(d) for d in dims)
+        mn = _f3(aabb_min if aabb_min is not None else (0, 0, 0))
+        mx = _f3(aabb_max if aabb_max is not None else (X, Y, Z))
+        h = C.c_void_p()
+        _check(lib().vf_grid_create(self.ctx.h, X, Y, Z, _p(mn), _p(mx), C.byref(h)))
+        self.h, self.dims = h, (X, Y, Z)
+        self.aabb_min, self.aabb_max = mn, mx
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().vf_grid_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def getNumSubdivisions(self):
+        return self.dims
+
+    def fill(self, verts, faces):
+        """RegularGrid::fill(Model3D*): voxelize a triangle mesh."""
+        v = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
+        f = np.ascontiguousarray(faces, dtype=np.uint32).reshape(-1, 3)
+        _check(lib().vf_voxelize(self.h, _p(v), v.shape[0], _p(f), f.shape[0]))
+
+    def upload(self, grid: np.ndarray):
+        g = np.ascontiguousarray(grid, dtype=np.uint16)
+        if g.shape != self.dims:
+            raise ValueError(f"grid shape {g.shape} != {self.dims}")
+        _check(lib().vf_grid_upload(self.h, _p(g)))
+
+    def data(self) -> np.ndarray:
+        """RegularGrid::updateGrid + data(): copy the labels to the host."""
+        g = np.empty(self.dims, dtype=np.uint16)
+        _check(lib().vf_grid_download(self.h, _p(g)))
+        return g
+
+    def detectBoundaries(self, boundary_size: int = 1):
+        _check(lib().vf_detect_boundaries(self.h, boundary_size))
+
+    def erode(self, erosion_type=ELLIPSE, size=3, iterations=3, probability=0.5,
+              threshold=0.5, seed=80):
+        _check(lib().vf_erode(self.h, erosion_type, size, iterations, probability,
+                              threshold, seed))
+
+    def removeIsolatedRegions(self):
+        _check(lib().vf_remove_isolated(self.h))
+
+    def undoMask(self):
+        _check(lib().vf_undo_mask(self.h))
+
+    def perturb(self, amplitude: float, period: int, seed: int):
+        _check(lib().vf_perturb(self.h, amplitude, period, seed))
+
+    def countValues(self, ncounts: int = 32768):
+        c = np.zeros(ncounts, np.uint32)
+        occ = C.c_uint64()
+        _check(lib().vf_count_values(self.h, _p(c), ncounts, C.byref(occ)))
+        return c, occ.value
+
+
+class Seeder:
+    """Seeder::uniform / mergeSeeds (Fracturer/Seeder.h:59-76)."""
+
+    @staticmethod
+    def uniform(grid: RegularGrid, nseeds: int, seed: int, location: int = OUTER):
+        out = np.zeros((max(nseeds, 1), 4), np.uint32)
+        _check(lib().vf_sample_seeds(grid.h, nseeds, seed, location, _p(out)))
+        return out[:nseeds]
+
+    @staticmethod
+    def mergeSeeds(frags, seeds, dfunc: int):
+        f = np.ascontiguousarray(frags, dtype=np.uint32).reshape(-1, 4)
+        s = np.array(seeds, dtype=np.uint32, copy=True, order="C").reshape(-1, 4)
+        _check(lib().vf_merge_seeds(_p(f), f.shape[0], _p(s), s.shape[0], dfunc))
+        return s
+
+    @staticmethod
+    def fracture_seeds(grid: RegularGrid, params: Params):
+        cap = 2 * params.num_seeds + params.num_extra_seeds
+        out = np.zeros((max(cap, 1), 4), np.uint32)
+        n = C.c_uint32()
+        _check(lib().vf_fracture_seeds(grid.h, C.byref(params), _p(out), C.byref(n)))
+        return out[:n.value]
+
+
+class _Fracturer:
+    algorithm = FLOOD
+
+    def __init__(self):
+        self._dfunc = MANHATTAN
+
+    def setDistanceFunction(self, dfunc: int) -> bool:
+        if dfunc not in (EUCLIDEAN, MANHATTAN, CHEBYSHEV):
+            return False
+        self._dfunc = dfunc
+        return True
+
+    def build(self, grid: RegularGrid, seeds, params: Params | None = None):
+        s = np.ascontiguousarray(seeds, dtype=np.uint32).reshape(-1, 4)
+        d = params.distance if params is not None else self._dfunc
+        _check(lib().vf_fracture(grid.h, self.algorithm, d, _p(s), s.shape[0]))
+
+
+class FloodFracturer(_Fracturer):
+    """FloodFracturer::build (Fracturer/FloodFracturer.cpp:98-191)."""
+    algorithm = FLOOD
+
+    def build_plain(self, grid: RegularGrid, seeds) -> int:
+        """Reference-shaped flood: one launch + host read per BFS wave."""
+        s = np.ascontiguousarray(seeds, dtype=np.uint32).reshape(-1, 4)
+        waves = C.c_uint32()
+        _check(lib().vf_fracture_plain(grid.h, self._dfunc, _p(s), s.shape[0], C.byref(waves)))
+        return waves.value
+
+
+class NaiveFracturer(_Fracturer):
+    """NaiveFracturer::build (Fracturer/NaiveFracturer.cpp:26-68)."""
+    algorithm = NAIVE
+
+
+def fracture_model(grid: RegularGrid, params: Params):
+    """CADScene::fractureModel on a voxelized grid; returns the seeds used."""
+    cap = 2 * params.num_seeds + params.num_extra_seeds
+    out = np.zeros((max(cap, 1), 4), np.uint32)
+    n = C.c_uint32()
+    _check(lib().vf_fracture_model(grid.h, C.byref(params), _p(out), C.byref(n)))
+    return out[:n.value]
+
+
+def dims_for_aabb(aabb_min, aabb_max, max_voxels: int):
+    out = np.zeros(3, np.uint32)
+    _check(lib().vf_dims_for_aabb(_p(_f3(aabb_min)), _p(_f3(aabb_max)), max_voxels, _p(out)))
+    return tuple(int(x) for x in out)
+
+
+# ---- whole jobs ----------------------------------------------------------------
+class JobSpec:
+    """A job with its host buffers kept alive (mesh, labels, counts)."""
+
+    def __init__(self, verts, faces, params: Params, dims=None, aabb=None, max_dim=0,
+                 want_labels=True, ncounts=256, tag=0, pinned=None):
+        self.verts = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
+        self.faces = np.ascontiguousarray(faces, dtype=np.uint32).reshape(-1, 3)
+        if aabb is None:
+            aabb = (self.verts.min(0), self.verts.max(0))
+        self.aabb = (_f3(aabb[0]), _f3(aabb[1]))
+        if dims is None:
+            dims = dims_for_aabb(self.aabb[0], self.aabb[1], max_dim)
+        self.dims = tuple(int(d) for d in dims)
+        self.params = params
+        self.labels = np.zeros(self.dims, np.uint16) if want_labels else None
+        self.counts = np.zeros(ncounts, np.uint32) if ncounts else None
+        self.tag = tag
+
+    def job(self) -> Job:
+        j = Job()
+        j.verts = self.verts.ctypes.data
+        j.nverts = self.verts.shape[0]
+        j.faces = self.faces.ctypes.data
+        j.nfaces = self.faces.shape[0]
+        for a in range(3):
+            j.dims[a] = self.dims[a]
+            j.aabb_min[a] = float(self.aabb[0][a])
+            j.aabb_max[a] = float(self.aabb[1][a])
+        j.params = self.params
+        j.out_labels = self.labels.ctypes.data if self.labels is not None else None
+        j.out_counts = self.counts.ctypes.data if self.counts is not None else None
+        j.ncounts = self.counts.shape[0] if self.counts is not None else 0
+        j.user_tag = self.tag
+        return j
+
+
+def _run(fn, specs, ctx):
+    ctx = ctx or default_context()
+    arr = (Job * len(specs))(*[s.job() for s in specs])
+    res = (JobResult * len(specs))()
+    st = fn(ctx.h, arr, len(specs), res)
+    if st != OK and all(r.status == OK for r in res):
+        _check(st)
+    return list(res)
+
+
+def batch_run(specs, ctx: Context | None = None):
+    """Batched path: every stage once over all jobs (vf_batch_run)."""
+    return _run(lib().vf_batch_run, specs, ctx)
+
+
+def plain_run(specs, ctx: Context | None = None):
+    """Plain path: one job at a time, per-wave flood (vf_plain_run)."""
+    return _run(lib().vf_plain_run, specs, ctx)
+
+
+class Server:
+    """vf_server: continuous batching with HBM admission control."""
+
+    def __init__(self, ctx: Context | None = None, hbm_budget: int = 0, max_inflight: int = 2,
+                 max_batch: int = 64):
+        self.ctx = ctx or default_context()
+        h = C.c_void_p()
+        _check(lib().vf_server_create(self.ctx.h, hbm_budget, max_inflight, max_batch, C.byref(h)))
+        self.h = h
+        self._keep = {}
+
+    def submit(self, spec: JobSpec) -> int:
+        t = C.c_uint64()
+        j = spec.job()
+        _check(lib().vf_server_submit(self.h, C.byref(j), C.byref(t)))
+        self._keep[spec.tag] = spec
+        return t.value
+
+    def poll(self, max_results: int = 256, wait_ms: int = 0):
+        out = (JobResult * max_results)()
+        n = C.c_uint32()
+        _check(lib().vf_server_poll(self.h, out, max_results, C.byref(n), wait_ms))
+        res = list(out[:n.value])
+        return res
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().vf_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,737 @@
+// vf_api.cu -- the extern "C" entry points declared in include/vf.h.
+//
+// vf_grid_* calls map a RegularGrid operation onto the batch machinery with
+// one job and a subset of stages; vf_batch_run / vf_plain_run run whole
+// jobs; vf_server_* runs the continuous-batching loop on its own thread.
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+
+#include "vf_runtime.h"
+
+namespace vfr {
+const char* last_error();
+void dims_for_aabb(const float mn[3], const float mx[3], uint32_t maxv, uint32_t out[3]);
+}  // namespace vfr
+
+using vfr::fail;
+
+#define VF_CK(call)                                                                  \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess)                                                           \
+      return fail(VF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+struct vf_ctx {
+  vfr::Ctx c;
+};
+
+struct vf_grid {
+  vf_ctx* ctx = nullptr;
+  vfr::Batch b;
+  vf_job job;
+  std::vector<uint32_t> seeds;  // last seeds used by fracture_model
+};
+
+extern "C" {
+
+void vf_params_default(vf_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->algorithm = VF_FLOOD;         // _fractureAlgorithm(FLOOD)
+  p->distance = VF_CHEBYSHEV;      // _distanceFunction(CHEBYSHEV)
+  p->num_seeds = 8;                // _numSeeds(8)
+  p->num_extra_seeds = 0;          // dataset mode sets extra seeds explicitly
+  p->merge_distance = VF_EUCLIDEAN;
+  p->seed_location = VF_OUTER;     // CADScene.cpp:633
+  p->seed = 80;                    // _seed(80)
+  p->noise_amplitude = 0.0f;
+  p->noise_period = 16;
+  p->erode = 0;
+  p->erosion_type = VF_ELLIPSE;
+  p->erosion_size = 3;
+  p->erosion_iterations = 3;
+  p->erosion_probability = 0.5f;
+  p->erosion_threshold = 0.5f;
+  p->boundary_size = 1;            // detectBoundaries(1)
+}
+
+const char* vf_last_error(void) { return vfr::last_error(); }
+
+const char* vf_status_string(vf_status s) {
+  switch (s) {
+    case VF_OK: return "ok";
+    case VF_ERR_INVALID: return "invalid argument";
+    case VF_ERR_CUDA: return "CUDA error";
+    case VF_ERR_OOM: return "out of device memory / budget";
+    case VF_ERR_SEED_SEARCH: return "seed search exceeded the try limit";
+    case VF_ERR_RANGE: return "value out of range";
+    case VF_ERR_TIMEOUT: return "bounded device wait expired";
+    case VF_ERR_NOT_BUILT: return "CUDA path unavailable";
+    case VF_ERR_BUSY: return "server queue full";
+    default: return "unknown status";
+  }
+}
+
+const char* vf_version(void) { return "vfgb300 1.0 sm_103a"; }
+
+vf_status vf_ctx_create(int device, size_t hbm_budget, vf_ctx** out) {
+  if (!out) return fail(VF_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0)
+    return fail(VF_ERR_NOT_BUILT, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  if (device < 0 || device >= n) return fail(VF_ERR_INVALID, "device index out of range");
+  VF_CK(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  VF_CK(cudaGetDeviceProperties(&prop, device));
+  if (prop.major * 10 + prop.minor < 100)
+    return fail(VF_ERR_NOT_BUILT, "this library is built for sm_103a (GB300)");
+  vf_ctx* c = new vf_ctx();
+  c->c.device = device;
+  c->c.num_sms = prop.multiProcessorCount;
+  size_t fr = 0, tot = 0;
+  cudaMemGetInfo(&fr, &tot);
+  c->c.budget = hbm_budget ? hbm_budget : (size_t)(0.9 * (double)fr);
+  if (cudaStreamCreateWithFlags(&c->c.stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return fail(VF_ERR_CUDA, "stream creation failed");
+  }
+  for (int i = 0; i < 16; ++i) cudaEventCreate(&c->c.ev[i]);
+  vf_status s = c->c.batch.init(&c->c, false);
+  if (s) {
+    delete c;
+    return s;
+  }
+  *out = c;
+  return VF_OK;
+}
+
+vf_status vf_ctx_destroy(vf_ctx* ctx) {
+  if (!ctx) return VF_OK;
+  cudaSetDevice(ctx->c.device);
+  cudaStreamSynchronize(ctx->c.stream);
+  ctx->c.batch.release();
+  for (int i = 0; i < 16; ++i) cudaEventDestroy(ctx->c.ev[i]);
+  cudaStreamDestroy(ctx->c.stream);
+  delete ctx;
+  return VF_OK;
+}
+
+vf_status vf_ctx_synchronize(vf_ctx* ctx) {
+  if (!ctx) return fail(VF_ERR_INVALID, "ctx is NULL");
+  VF_CK(cudaStreamSynchronize(ctx->c.stream));
+  return VF_OK;
+}
+
+size_t vf_ctx_bytes_in_use(const vf_ctx* ctx) { return ctx ? ctx->c.in_use : 0; }
+
+void* vf_host_alloc(size_t bytes) {
+  void* p = nullptr;
+  if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+  return p;
+}
+void vf_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+vf_status vf_dims_for_aabb(const float aabb_min[3], const float aabb_max[3], uint32_t max_voxels,
+                           uint32_t dims_out[3]) {
+  if (!aabb_min || !aabb_max || !dims_out) return fail(VF_ERR_INVALID, "NULL argument");
+  vfr::dims_for_aabb(aabb_min, aabb_max, max_voxels, dims_out);
+  return VF_OK;
+}
+
+// ---- grid -----------------------------------------------------------------
+static vf_status grid_run(vf_grid* g, uint32_t stages) {
+  cudaSetDevice(g->ctx->c.device);
+  vfr::Batch& B = g->b;
+  const vf_job* jp = &g->job;
+  B.stages = stages;
+  vf_status s = B.plan(&jp, 1);
+  if (s) return s;
+  s = B.enqueue_batched();
+  if (s) return s;
+  s = B.finish(nullptr);
+  // keep the current grid in buffer 0
+  const vfr::JobPlan& p = B.plans[0];
+  if (p.final_cur == 1 && (stages & (vfr::ST_PERTURB | vfr::ST_ERODE))) {
+    VF_CK(cudaMemcpyAsync(B.grid0.p, B.grid1.p, (size_t)p.X * p.Y * p.Zp * 2,
+                          cudaMemcpyDeviceToDevice, B.stream));
+    VF_CK(cudaStreamSynchronize(B.stream));
+  }
+  return s;
+}
+
+vf_status vf_grid_create(vf_ctx* ctx, uint32_t X, uint32_t Y, uint32_t Z, const float aabb_min[3],
+                         const float aabb_max[3], vf_grid** out) {
+  if (!ctx || !out) return fail(VF_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  if (X < 2 || Y < 2 || Z < 2 || X > VF_MAX_DIM || Y > VF_MAX_DIM || Z > VF_MAX_DIM)
+    return fail(VF_ERR_INVALID, "grid dims must be in [2, 4096]");
+  vf_grid* g = new vf_grid();
+  g->ctx = ctx;
+  std::memset(&g->job, 0, sizeof(g->job));
+  g->job.dims[0] = X; g->job.dims[1] = Y; g->job.dims[2] = Z;
+  for (int a = 0; a < 3; ++a) {
+    g->job.aabb_min[a] = aabb_min ? aabb_min[a] : 0.0f;
+    g->job.aabb_max[a] = aabb_max ? aabb_max[a] : (float)(a == 0 ? X : a == 1 ? Y : Z);
+  }
+  bool ok = false;
+  for (int a = 0; a < 3; ++a) ok |= g->job.aabb_min[a] != g->job.aabb_max[a];
+  if (!ok) {
+    delete g;
+    return fail(VF_ERR_INVALID, "degenerate AABB");
+  }
+  vf_params_default(&g->job.params);
+  g->job.params.num_seeds = 0;
+  vf_status s = g->b.init(&ctx->c, true);
+  if (!s) {
+    const vf_job* jp = &g->job;
+    s = g->b.plan(&jp, 1);
+  }
+  if (!s) {
+    const vfr::JobPlan& p = g->b.plans[0];
+    const size_t bytes = (size_t)p.X * p.Y * p.Zp * 2;
+    if (cudaMemsetAsync(g->b.grid0.p, 0, bytes, g->b.stream) != cudaSuccess ||
+        cudaMemsetAsync(g->b.grid1.p, 0, bytes, g->b.stream) != cudaSuccess ||
+        cudaStreamSynchronize(g->b.stream) != cudaSuccess)
+      s = fail(VF_ERR_CUDA, "grid clear failed");
+  }
+  if (s) {
+    g->b.release();
+    delete g;
+    return s;
+  }
+  *out = g;
+  return VF_OK;
+}
+
+vf_status vf_grid_destroy(vf_grid* g) {
+  if (!g) return VF_OK;
+  cudaSetDevice(g->ctx->c.device);
+  if (g->b.stream) cudaStreamSynchronize(g->b.stream);
+  g->b.release();
+  delete g;
+  return VF_OK;
+}
+
+vf_status vf_grid_dims(const vf_grid* g, uint32_t dims[3]) {
+  if (!g || !dims) return fail(VF_ERR_INVALID, "NULL argument");
+  for (int a = 0; a < 3; ++a) dims[a] = g->job.dims[a];
+  return VF_OK;
+}
+
+vf_status vf_grid_upload(vf_grid* g, const uint16_t* host) {
+  if (!g || !host) return fail(VF_ERR_INVALID, "NULL argument");
+  cudaSetDevice(g->ctx->c.device);
+  const vfr::JobPlan& p = g->b.plans[0];
+  const size_t bytes = (size_t)p.X * p.Y * p.Zp * 2;
+  cudaStream_t st = g->b.stream;
+  VF_CK(cudaMemsetAsync(g->b.grid0.p, 0, bytes, st));
+  VF_CK(cudaMemsetAsync(g->b.grid1.p, 0, bytes, st));
+  VF_CK(cudaMemcpy2DAsync(g->b.grid0.p, (size_t)p.Zp * 2, host, (size_t)p.Z * 2, (size_t)p.Z * 2,
+                          (size_t)p.X * p.Y, cudaMemcpyHostToDevice, st));
+  VF_CK(cudaStreamSynchronize(st));
+  return VF_OK;
+}
+
+vf_status vf_grid_download(vf_grid* g, uint16_t* host) {
+  if (!g || !host) return fail(VF_ERR_INVALID, "NULL argument");
+  cudaSetDevice(g->ctx->c.device);
+  const vfr::JobPlan& p = g->b.plans[0];
+  VF_CK(cudaMemcpy2DAsync(host, (size_t)p.Z * 2, g->b.grid0.p, (size_t)p.Zp * 2, (size_t)p.Z * 2,
+                          (size_t)p.X * p.Y, cudaMemcpyDeviceToHost, g->b.stream));
+  VF_CK(cudaStreamSynchronize(g->b.stream));
+  return VF_OK;
+}
+
+vf_status vf_voxelize(vf_grid* g, const float* verts, uint32_t nverts, const uint32_t* faces,
+                      uint32_t nfaces) {
+  if (!g) return fail(VF_ERR_INVALID, "grid is NULL");
+  if (nfaces && (!verts || !faces || !nverts)) return fail(VF_ERR_INVALID, "mesh pointers missing");
+  for (uint64_t i = 0; i < 3ull * nfaces; ++i)
+    if (faces[i] >= nverts) return fail(VF_ERR_INVALID, "face index out of range");
+  g->job.verts = verts;
+  g->job.nverts = nverts;
+  g->job.faces = faces;
+  g->job.nfaces = nfaces;
+  g->b.given.clear();
+  vf_status s = grid_run(g, vfr::ST_VOX);
+  g->job.verts = nullptr;
+  g->job.faces = nullptr;
+  g->job.nverts = g->job.nfaces = 0;
+  return s;
+}
+
+static vf_status seeds_out(vf_grid* g, uint32_t* out, uint32_t* nout) {
+  vfr::Batch& B = g->b;
+  const uint32_t n = B.h_state[0].nseeds;
+  if (out && n)
+    VF_CK(cudaMemcpy(out, static_cast<uint32_t*>(B.seeds.p) + B.plans[0].o_seeds,
+                     sizeof(uint32_t) * 4 * n, cudaMemcpyDeviceToHost));
+  if (nout) *nout = n;
+  return VF_OK;
+}
+
+vf_status vf_sample_seeds(vf_grid* g, uint32_t n, uint64_t seed, int location, uint32_t* out) {
+  if (!g || (n && !out)) return fail(VF_ERR_INVALID, "NULL argument");
+  if (n > 254) return fail(VF_ERR_RANGE, "at most 254 seeds (8-bit fragment ids 2..255)");
+  if (location < VF_INNER || location > VF_BOTH) return fail(VF_ERR_INVALID, "location out of range");
+  vf_params saved = g->job.params;
+  g->job.params.num_seeds = (int32_t)n;
+  g->job.params.num_extra_seeds = 0;
+  g->job.params.seed = seed;
+  g->job.params.seed_location = location;
+  g->b.given.clear();
+  vf_status s = grid_run(g, vfr::ST_SEED);
+  g->job.params = saved;
+  if (s) return s;
+  return seeds_out(g, out, nullptr);
+}
+
+vf_status vf_merge_seeds(const uint32_t* frags, uint32_t nfrags, uint32_t* seeds, uint32_t nseeds,
+                         int dfunc) {
+  // Seeder::mergeSeeds (Seeder.cpp:115-152) -- host bookkeeping, as in the reference
+  if (nseeds == 0) return VF_OK;
+  if (!frags || !seeds || nfrags == 0) return fail(VF_ERR_INVALID, "NULL or empty argument");
+  if (dfunc < 0 || dfunc > 2) return fail(VF_ERR_INVALID, "distance out of range");
+  uint32_t idf[256] = {0};
+  for (uint32_t k = 0; k < nseeds; ++k) {
+    float best = FLT_MAX;
+    int nearest = -1;
+    for (uint32_t i = 0; i < nfrags; ++i) {
+      const float dx = (float)seeds[4 * k] - (float)frags[4 * i];
+      const float dy = (float)seeds[4 * k + 1] - (float)frags[4 * i + 1];
+      const float dz = (float)seeds[4 * k + 2] - (float)frags[4 * i + 2];
+      float d;
+      if (dfunc == VF_EUCLIDEAN) d = std::sqrt(dx * dx + dy * dy + dz * dz);
+      else if (dfunc == VF_MANHATTAN) d = std::fabs(dx) + std::fabs(dy) + std::fabs(dz);
+      else d = std::max(std::fabs(dx), std::max(std::fabs(dy), std::fabs(dz)));
+      if (d < best) { best = d; nearest = (int)i; }
+    }
+    const uint32_t w = frags[4 * nearest + 3];
+    if (w > 255) return fail(VF_ERR_RANGE, "fragment label above 255");
+    const uint32_t pre = ++idf[w];
+    if (pre > 127) return fail(VF_ERR_RANGE, "sub-seed prefix above 127");
+    seeds[4 * k + 3] = w | (pre << 8);
+  }
+  return VF_OK;
+}
+
+vf_status vf_fracture_seeds(vf_grid* g, const vf_params* p, uint32_t* out, uint32_t* nout) {
+  if (!g || !p) return fail(VF_ERR_INVALID, "NULL argument");
+  vf_params saved = g->job.params;
+  g->job.params = *p;
+  g->b.given.clear();
+  vf_status s = grid_run(g, vfr::ST_SEED);
+  g->job.params = saved;
+  if (s) return s;
+  return seeds_out(g, out, nout);
+}
+
+vf_status vf_fracture(vf_grid* g, int algorithm, int distance, const uint32_t* seeds,
+                      uint32_t nseeds) {
+  if (!g || (nseeds && !seeds)) return fail(VF_ERR_INVALID, "NULL argument");
+  if (nseeds > VF_MAX_SEEDS) return fail(VF_ERR_RANGE, "at most 4095 seeds");
+  vf_params saved = g->job.params;
+  g->job.params.algorithm = algorithm;
+  g->job.params.distance = distance;
+  g->job.params.num_seeds = 0;
+  g->job.params.num_extra_seeds = 0;
+  g->job.params.noise_amplitude = 0.0f;
+  g->job.params.erode = 0;
+  g->b.given.assign(1, {seeds, nseeds});
+  vf_status s = nseeds ? grid_run(g, vfr::ST_SEED | vfr::ST_FRACTURE) : VF_OK;
+  g->b.given.clear();
+  g->job.params = saved;
+  return s;
+}
+
+vf_status vf_fracture_plain(vf_grid* g, int distance, const uint32_t* seeds, uint32_t nseeds,
+                            uint32_t* waves_out) {
+  if (!g || (nseeds && !seeds)) return fail(VF_ERR_INVALID, "NULL argument");
+  if (nseeds > VF_MAX_SEEDS) return fail(VF_ERR_RANGE, "at most 4095 seeds");
+  // a plain job on the grid's occupancy: the plain runner voxelizes, so run
+  // it on a copy of the job whose mesh is the grid itself: seed + flood
+  // stages of the plain path over buffer 0
+  cudaSetDevice(g->ctx->c.device);
+  vf_params saved = g->job.params;
+  g->job.params.algorithm = VF_FLOOD;
+  g->job.params.distance = distance;
+  g->job.params.num_seeds = 0;
+  g->job.params.num_extra_seeds = 0;
+  g->job.params.noise_amplitude = 0.0f;
+  g->job.params.erode = 0;
+  g->b.given.assign(1, {seeds, nseeds});
+  vfr::Batch& B = g->b;
+  const vf_job* jp = &g->job;
+  B.stages = vfr::ST_SEED | vfr::ST_FRACTURE;
+  vf_status s = B.plan(&jp, 1);
+  vf_job_result r;
+  if (!s) s = B.enqueue_plain_and_wait(&r, /*skip_vox=*/true);
+  if (!s && waves_out) *waves_out = r.flood_passes;
+  g->b.given.clear();
+  g->job.params = saved;
+  return s;
+}
+
+vf_status vf_perturb(vf_grid* g, float amplitude, uint32_t period, uint64_t seed) {
+  if (!g) return fail(VF_ERR_INVALID, "grid is NULL");
+  if (!(amplitude >= 0.0f) || amplitude > 64.0f || period == 0)
+    return fail(VF_ERR_INVALID, "amplitude must be in [0, 64] and period >= 1");
+  if (amplitude == 0.0f) return VF_OK;
+  vf_params saved = g->job.params;
+  g->job.params.noise_amplitude = amplitude;
+  g->job.params.noise_period = period;
+  g->job.params.seed = seed;
+  g->job.params.erode = 0;
+  g->b.given.clear();
+  vf_status s = grid_run(g, vfr::ST_PERTURB);
+  g->job.params = saved;
+  return s;
+}
+
+vf_status vf_detect_boundaries(vf_grid* g, int boundary_size) {
+  if (!g) return fail(VF_ERR_INVALID, "grid is NULL");
+  if (boundary_size < 0 || boundary_size > 3) return fail(VF_ERR_INVALID, "boundary_size must be in [0, 3]");
+  vf_params saved = g->job.params;
+  g->job.params.boundary_size = boundary_size;
+  g->job.params.erode = 0;
+  g->job.params.noise_amplitude = 0.0f;
+  g->b.given.clear();
+  vf_status s = grid_run(g, vfr::ST_DETECT);
+  g->job.params = saved;
+  return s;
+}
+
+vf_status vf_erode(vf_grid* g, int type, uint32_t size, uint32_t iterations, float probability,
+                   float threshold, uint64_t seed) {
+  if (!g) return fail(VF_ERR_INVALID, "grid is NULL");
+  vf_params saved = g->job.params;
+  g->job.params.erode = 1;
+  g->job.params.erosion_type = type;
+  g->job.params.erosion_size = (int32_t)size;
+  g->job.params.erosion_iterations = (int32_t)iterations;
+  g->job.params.erosion_probability = probability;
+  g->job.params.erosion_threshold = threshold;
+  g->job.params.seed = seed;
+  g->job.params.noise_amplitude = 0.0f;
+  g->b.given.clear();
+  vf_status s = grid_run(g, vfr::ST_ERODE);
+  g->job.params = saved;
+  return s;
+}
+
+vf_status vf_remove_isolated(vf_grid* g) {
+  if (!g) return fail(VF_ERR_INVALID, "grid is NULL");
+  vf_params saved = g->job.params;
+  g->job.params.erode = 1;
+  g->job.params.erosion_iterations = 0;
+  g->job.params.noise_amplitude = 0.0f;
+  g->b.given.clear();
+  vf_status s = grid_run(g, vfr::ST_ERODE);
+  g->job.params = saved;
+  return s;
+}
+
+vf_status vf_undo_mask(vf_grid* g) {
+  if (!g) return fail(VF_ERR_INVALID, "grid is NULL");
+  cudaSetDevice(g->ctx->c.device);
+  vfr::Batch& B = g->b;
+  const vf_job* jp = &g->job;
+  B.stages = 0;
+  vf_status s = B.plan(&jp, 1);
+  if (s) return s;
+  const JobDesc* T = reinterpret_cast<const JobDesc*>(B.h_tables);
+  VF_CK(cudaMemcpyAsync(B.tables.p, B.h_tables, sizeof(JobDesc), cudaMemcpyHostToDevice, B.stream));
+  vfk::plain_undo_mask(B.stream, B.dtable(0), T[0]);
+  VF_CK(cudaStreamSynchronize(B.stream));
+  VF_CK(cudaGetLastError());
+  return VF_OK;
+}
+
+vf_status vf_count_values(vf_grid* g, uint32_t* counts, uint32_t ncounts, uint64_t* occupied) {
+  if (!g || (ncounts && !counts)) return fail(VF_ERR_INVALID, "NULL argument");
+  g->job.ncounts = ncounts;
+  g->job.out_counts = counts;
+  g->b.given.clear();
+  vf_status s = grid_run(g, vfr::ST_COUNT | vfr::ST_DOWNLOAD);
+  g->job.ncounts = 0;
+  g->job.out_counts = nullptr;
+  if (occupied) *occupied = g->b.h_state[0].occupied;
+  return s;
+}
+
+vf_status vf_fracture_model(vf_grid* g, const vf_params* p, uint32_t* seeds_out_, uint32_t* nseeds_out) {
+  if (!g || !p) return fail(VF_ERR_INVALID, "NULL argument");
+  vf_params saved = g->job.params;
+  g->job.params = *p;
+  g->b.given.clear();
+  vf_status s = grid_run(g, vfr::ST_SEED | vfr::ST_FRACTURE | vfr::ST_PERTURB | vfr::ST_ERODE |
+                                vfr::ST_DETECT);
+  g->job.params = saved;
+  vf_status s2 = seeds_out(g, seeds_out_, nseeds_out);
+  return s ? s : s2;
+}
+
+// ---- whole jobs -----------------------------------------------------------
+size_t vf_job_footprint(const vf_job* job) { return job ? vfr::job_footprint(*job) : 0; }
+
+vf_status vf_batch_run(vf_ctx* ctx, const vf_job* jobs, uint32_t njobs, vf_job_result* results) {
+  if (!ctx || (njobs && !jobs)) return fail(VF_ERR_INVALID, "NULL argument");
+  if (njobs == 0) return VF_OK;
+  cudaSetDevice(ctx->c.device);
+  vfr::Batch& B = ctx->c.batch;
+  std::vector<const vf_job*> ptrs(njobs);
+  for (uint32_t i = 0; i < njobs; ++i) ptrs[i] = jobs + i;
+  B.stages = vfr::ST_ALL;
+  B.given.clear();
+  vf_status s = B.plan(ptrs.data(), njobs);
+  if (s) return s;
+  s = B.enqueue_batched();
+  if (s) return s;
+  return B.finish(results);
+}
+
+vf_status vf_plain_run(vf_ctx* ctx, const vf_job* jobs, uint32_t njobs, vf_job_result* results) {
+  if (!ctx || (njobs && !jobs)) return fail(VF_ERR_INVALID, "NULL argument");
+  cudaSetDevice(ctx->c.device);
+  vfr::Batch& B = ctx->c.batch;
+  vf_status first = VF_OK;
+  uint64_t launches = 0;
+  for (uint32_t i = 0; i < njobs; ++i) {
+    const vf_job* jp = jobs + i;
+    B.stages = vfr::ST_ALL;
+    B.given.clear();
+    vf_status s = B.plan(&jp, 1);
+    if (!s) s = B.enqueue_plain_and_wait(results ? results + i : nullptr, false);
+    launches += B.launches;
+    if (s && results) results[i].status = s;
+    if (s && !first) first = s;
+  }
+  ctx->c.last_launches = launches;
+  return first;
+}
+
+// ---- events / stats ---------------------------------------------------------
+vf_status vf_ctx_event_record(vf_ctx* ctx, int slot) {
+  if (!ctx || slot < 0 || slot >= 16) return fail(VF_ERR_INVALID, "bad slot");
+  VF_CK(cudaEventRecord(ctx->c.ev[slot], ctx->c.stream));
+  return VF_OK;
+}
+vf_status vf_ctx_event_elapsed(vf_ctx* ctx, int a, int b, float* ms) {
+  if (!ctx || !ms || a < 0 || b < 0 || a >= 16 || b >= 16) return fail(VF_ERR_INVALID, "bad slot");
+  VF_CK(cudaEventSynchronize(ctx->c.ev[b]));
+  VF_CK(cudaEventElapsedTime(ms, ctx->c.ev[a], ctx->c.ev[b]));
+  return VF_OK;
+}
+vf_status vf_ctx_last_stats(vf_ctx* ctx, uint64_t* launches, float* flood_ms, uint64_t* flood_bytes,
+                            uint64_t* flood_visits) {
+  if (!ctx) return fail(VF_ERR_INVALID, "ctx is NULL");
+  if (launches) *launches = ctx->c.last_launches;
+  if (flood_ms) *flood_ms = ctx->c.last_flood_ms;
+  // algorithmic bytes of a brick visit: every voxel's label read and written
+  if (flood_bytes) *flood_bytes = ctx->c.last_flood_visits * (uint64_t)VF_BRICK_VOXELS * 4u;
+  if (flood_visits) *flood_visits = ctx->c.last_flood_visits;
+  return VF_OK;
+}
+
+}  // extern "C"
+
+// ---- server -------------------------------------------------------------------
+struct vf_server {
+  vf_ctx* ctx = nullptr;
+  size_t budget = 0;
+  uint32_t max_inflight = 2, max_batch = 64;
+  std::thread th;
+  std::mutex mu;
+  std::condition_variable cv, cv_done;
+  struct Pending {
+    vf_job job;
+    uint64_t ticket;
+    double submit_ms;
+    size_t footprint;
+  };
+  struct Slot {
+    vfr::Batch b;
+    bool busy = false;
+    std::vector<Pending> jobs;
+    std::vector<vf_job> job_copies;
+    size_t footprint = 0;
+  };
+  std::deque<Pending> pending;
+  std::deque<vf_job_result> done;
+  std::vector<Slot> slots;
+  size_t in_flight_bytes = 0;
+  uint64_t next_ticket = 1;
+  bool stop = false;
+  vf_status fatal = VF_OK;
+  std::chrono::steady_clock::time_point t0;
+  double now_ms() const {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  void loop();
+};
+
+void vf_server::loop() {
+  cudaSetDevice(ctx->c.device);
+  std::unique_lock<std::mutex> lk(mu);
+  for (;;) {
+    bool progressed = false;
+    // completions
+    for (Slot& s : slots) {
+      if (!s.busy) continue;
+      if (cudaEventQuery(s.b.ev_done) == cudaErrorNotReady) continue;
+      lk.unlock();
+      std::vector<vf_job_result> res(s.jobs.size());
+      vf_status st = s.b.finish(res.data());
+      const double t = now_ms();
+      lk.lock();
+      for (size_t i = 0; i < s.jobs.size(); ++i) {
+        if (st && !res[i].status) res[i].status = st == VF_ERR_CUDA ? st : res[i].status;
+        res[i].submit_ms = s.jobs[i].submit_ms;
+        res[i].done_ms = t;
+        res[i].user_tag = s.jobs[i].job.user_tag;
+        done.push_back(res[i]);
+      }
+      in_flight_bytes -= s.footprint;
+      s.busy = false;
+      s.jobs.clear();
+      progressed = true;
+    }
+    if (!done.empty()) cv_done.notify_all();
+    // admission: FIFO jobs that fit the free budget go to a free slot
+    for (Slot& s : slots) {
+      if (s.busy || pending.empty()) continue;
+      std::vector<Pending> take;
+      size_t fp = 0;
+      while (!pending.empty() && take.size() < max_batch &&
+             (take.empty() ? in_flight_bytes + pending.front().footprint <= budget || in_flight_bytes == 0
+                           : in_flight_bytes + fp + pending.front().footprint <= budget)) {
+        fp += pending.front().footprint;
+        take.push_back(pending.front());
+        pending.pop_front();
+      }
+      if (take.empty()) break;
+      in_flight_bytes += fp;
+      s.footprint = fp;
+      s.jobs = take;
+      s.busy = true;
+      lk.unlock();
+      s.job_copies.resize(take.size());
+      std::vector<const vf_job*> ptrs(take.size());
+      for (size_t i = 0; i < take.size(); ++i) {
+        s.job_copies[i] = take[i].job;
+        ptrs[i] = &s.job_copies[i];
+      }
+      s.b.stages = vfr::ST_ALL;
+      s.b.given.clear();
+      vf_status st = s.b.plan(ptrs.data(), (uint32_t)ptrs.size());
+      if (!st) st = s.b.enqueue_batched();
+      lk.lock();
+      if (st) {
+        const double t = now_ms();
+        for (const Pending& p : take) {
+          vf_job_result r;
+          std::memset(&r, 0, sizeof(r));
+          r.status = st;
+          r.submit_ms = p.submit_ms;
+          r.done_ms = t;
+          r.user_tag = p.job.user_tag;
+          done.push_back(r);
+        }
+        in_flight_bytes -= fp;
+        s.busy = false;
+        s.jobs.clear();
+        cv_done.notify_all();
+      }
+      progressed = true;
+    }
+    bool any_busy = false;
+    for (Slot& s : slots) any_busy |= s.busy;
+    if (stop && !any_busy && pending.empty()) break;
+    if (!progressed) {
+      if (any_busy) cv.wait_for(lk, std::chrono::microseconds(50));
+      else cv.wait_for(lk, std::chrono::milliseconds(5));
+    }
+  }
+}
+
+extern "C" {
+
+vf_status vf_server_create(vf_ctx* ctx, size_t hbm_budget, uint32_t max_inflight,
+                           uint32_t max_batch_jobs, vf_server** out) {
+  if (!ctx || !out) return fail(VF_ERR_INVALID, "NULL argument");
+  vf_server* s = new vf_server();
+  s->ctx = ctx;
+  s->budget = hbm_budget ? hbm_budget : ctx->c.budget / 2;
+  s->max_inflight = std::max(1u, std::min(max_inflight ? max_inflight : 2u, 8u));
+  s->max_batch = std::max(1u, max_batch_jobs ? max_batch_jobs : 64u);
+  s->slots.resize(s->max_inflight);
+  for (auto& sl : s->slots) {
+    vf_status st = sl.b.init(&ctx->c, true);
+    if (st) {
+      for (auto& x : s->slots) x.b.release();
+      delete s;
+      return st;
+    }
+  }
+  s->t0 = std::chrono::steady_clock::now();
+  s->th = std::thread([s] { s->loop(); });
+  *out = s;
+  return VF_OK;
+}
+
+vf_status vf_server_submit(vf_server* s, const vf_job* job, uint64_t* ticket) {
+  if (!s || !job) return fail(VF_ERR_INVALID, "NULL argument");
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->pending.size() > 1000000) return fail(VF_ERR_BUSY, "server queue full");
+  vf_server::Pending p;
+  p.job = *job;
+  p.ticket = s->next_ticket++;
+  p.submit_ms = s->now_ms();
+  p.footprint = vfr::job_footprint(*job);
+  s->pending.push_back(p);
+  if (ticket) *ticket = p.ticket;
+  s->cv.notify_all();
+  return VF_OK;
+}
+
+vf_status vf_server_poll(vf_server* s, vf_job_result* out, uint32_t max, uint32_t* n, int wait_ms) {
+  if (!s || !n || (max && !out)) return fail(VF_ERR_INVALID, "NULL argument");
+  std::unique_lock<std::mutex> lk(s->mu);
+  if (s->done.empty() && wait_ms > 0)
+    s->cv_done.wait_for(lk, std::chrono::milliseconds(wait_ms), [s] { return !s->done.empty(); });
+  uint32_t k = 0;
+  while (k < max && !s->done.empty()) {
+    out[k++] = s->done.front();
+    s->done.pop_front();
+  }
+  *n = k;
+  return VF_OK;
+}
+
+vf_status vf_server_destroy(vf_server* s) {
+  if (!s) return VF_OK;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+    s->cv.notify_all();
+  }
+  if (s->th.joinable()) s->th.join();
+  for (auto& sl : s->slots) sl.b.release();
+  delete s;
+  return VF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,647 @@
+// vf_flood.cu -- FloodFracturer (FloodFracturer.cpp:98-191) on sm_103a.
+//
+// The reference runs a breadth-first flood, one compute dispatch and one
+// host read-back per wave, and lets the last writer win a tie.  With the
+// rule "a voxel claimed in wave t takes the claim of the lowest seed index
+// among its wave-(t-1) neighbours", the label of every voxel is the label of
+// the seed nearest to it in grid-graph distance through occupied voxels
+// (6-neighbourhood for Manhattan, 26 for Euclidean and Chebyshev), ties to
+// the lowest seed index.  That fixed point does not depend on the order in
+// which voxels are relaxed, so the GPU computes it by relaxation:
+//
+//   key(v) = ~((dist << 12) | seed_slot)      (0 = EMPTY, 1 = unreached)
+//   key(v) <- max(key(v), max_{u in N(v)} key(u) - 4096)
+//
+// Bricks of 16x16x32 voxels are relaxed to local convergence in shared
+// memory (many BFS waves per visit), and a brick whose face voxels changed
+// puts its neighbours on the next pass's queue (deduplicated by a pass
+// epoch, appended with warp ballot/popc).  All passes of all jobs of a batch
+// run in ONE cooperative persistent kernel; passes are separated by a
+// software grid barrier whose spin is bounded (it sets an error word and the
+// kernel returns instead of hanging).
+//
+// Sub-seed prefixes (extra seeds merged into fragments, Seeder.cpp:115-152)
+// then go through the reference's competition and disjoint cleanup
+// (floodFracturer-comp.glsl:49-62, disjointSet*-comp.glsl): within a
+// connected component of one fragment the lowest prefix wins; per fragment
+// only voxels with the fragment's minimum prefix survive; the rest is
+// re-flooded from all survivors (ties to the lowest label value).
+#include "vf_kernels.h"
+
+namespace {
+
+constexpr int KP = 44;                 // smem row pitch (u32): conflict-free 16 B loads
+constexpr int KNX = VF_BX + 2, KNY = VF_BY + 2;
+constexpr int KROWS = KNX * KNY;
+constexpr int KZW = 10;                // 16-byte chunks per staged row: z in [z0-4, z0+36)
+constexpr int TILE_BYTES = KROWS * KP * 4;
+constexpr int MAXIT = 96;              // relaxation sweeps per brick visit
+
+struct FloodArgs {
+  const JobDesc* jobs;
+  JobState* st;
+  const uint32_t* brick_job;
+  const uint8_t* live;
+  uint32_t* queue[3];
+  uint32_t* qcount;  // [3]
+  uint32_t* qhead;   // [3]
+  uint32_t* epoch;
+  uint32_t* bar;     // [2]
+  uint32_t* err;
+  uint32_t* stats;   // [0] visits, [1] passes, [2] overflow, [3] timeout
+  uint32_t max_passes;
+};
+
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// software grid barrier with a bounded spin (~4 s); false on timeout
+__device__ bool grid_sync(uint32_t* bar, uint32_t nblocks, uint32_t* err, uint32_t* stats) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    const uint32_t gen = ld_acquire(bar + 1);
+    __threadfence();
+    const uint32_t arrived = atomicAdd(bar, 1u) + 1u;
+    if (arrived == nblocks) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      uint32_t spins = 0;
+      while (ld_acquire(bar + 1) == gen) {
+        if (++spins > (1u << 26) || ld_acquire(err) != 0) {
+          atomicOr(err, 2u);
+          atomicAdd(stats + 3, 1u);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+__device__ __forceinline__ uint32_t brick_id(const JobDesc& J, int bx, int by, int bz) {
+  return J.brick_base + ((uint32_t)bx * J.nby + (uint32_t)by) * J.nbz + (uint32_t)bz;
+}
+
+__device__ __forceinline__ void enqueue(const FloodArgs& a, uint32_t b, uint32_t next_pass,
+                                        bool want) {
+  // warp-aggregated append of the bricks this warp wants on the next queue
+  const int lane = threadIdx.x & 31;
+  bool push = false;
+  if (want) push = atomicMax(&a.epoch[b], next_pass + 1u) < next_pass + 1u;
+  const unsigned m = __ballot_sync(0xFFFFFFFFu, push);
+  if (!m) return;
+  const uint32_t q = next_pass % 3u;
+  uint32_t base = 0;
+  const int leader = __ffs(m) - 1;
+  if (lane == leader) base = atomicAdd(&a.qcount[q], (uint32_t)__popc(m));
+  base = __shfl_sync(0xFFFFFFFFu, base, leader);
+  if (push) a.queue[q][base + __popc(m & ((1u << lane) - 1u))] = b;
+}
+
+template <int CONN>
+__device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, uint32_t b,
+                            uint32_t pass, uint32_t* tile, uint32_t* live27, uint32_t* dirs,
+                            int* reenq) {
+  const uint32_t lb = b - J.brick_base;
+  const int bz = lb % J.nbz, by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
+  const int x0 = bx * VF_BX, y0 = by * VF_BY, z0 = bz * VF_BZ;
+  const int t = threadIdx.x;
+  if (t < 27) {
+    const int dx = t / 9 - 1, dy = (t / 3) % 3 - 1, dz = t % 3 - 1;
+    const int nx = bx + dx, ny = by + dy, nz = bz + dz;
+    uint32_t l = 0;
+    if (nx >= 0 && ny >= 0 && nz >= 0 && nx < (int)J.nbx && ny < (int)J.nby && nz < (int)J.nbz)
+      l = a.live[brick_id(J, nx, ny, nz)];
+    live27[t] = l;
+  }
+  if (t == 0) { *dirs = 0; *reenq = 0; }
+  __syncthreads();
+  // stage keys: rows [x0-1, x0+17) x [y0-1, y0+17), z [z0-4, z0+36)
+  for (int q = t; q < KROWS * KZW; q += blockDim.x) {
+    const int row = q / KZW, part = q % KZW;
+    const int lx = row / KNY - 1, ly = row % KNY - 1, lz = part * 4 - 4;
+    const int x = x0 + lx, y = y0 + ly, z = z0 + lz;
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (x >= 0 && y >= 0 && z >= 0 && x < (int)J.X && y < (int)J.Y && z < (int)J.Zk) {
+      const int dx = lx < 0 ? 0 : (lx >= VF_BX ? 2 : 1);
+      const int dy = ly < 0 ? 0 : (ly >= VF_BY ? 2 : 1);
+      const int dz = lz < 0 ? 0 : (lz >= VF_BZ ? 2 : 1);
+      if (live27[dx * 9 + dy * 3 + dz])
+        v = __ldcg(reinterpret_cast<const uint4*>(J.keys + vf_kidx(J, x, y, z)));
+    }
+    *reinterpret_cast<uint4*>(tile + row * KP + part * 4) = v;
+  }
+  __syncthreads();
+  const int tx = t / VF_BY, ty = t % VF_BY;
+  uint32_t* own_row = tile + ((tx + 1) * KNY + (ty + 1)) * KP;
+  uint32_t k[VF_BZ];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const uint4 w = *reinterpret_cast<const uint4*>(own_row + 4 + 4 * q);
+    k[4 * q] = w.x; k[4 * q + 1] = w.y; k[4 * q + 2] = w.z; k[4 * q + 3] = w.w;
+  }
+  uint32_t changed = 0, overflow = 0;
+  int it = 0;
+  for (; it < MAXIT; ++it) {
+    uint32_t c[VF_BZ + 2];
+#pragma unroll
+    for (int j = 0; j < VF_BZ + 2; ++j) c[j] = 0;
+    if (CONN == 26) {
+#pragma unroll
+      for (int r = 0; r < 9; ++r) {
+        const uint32_t* rp = tile + ((tx + r / 3) * KNY + (ty + r % 3)) * KP;
+        c[0] = max(c[0], rp[3]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const uint4 w = *reinterpret_cast<const uint4*>(rp + 4 + 4 * q);
+          c[1 + 4 * q] = max(c[1 + 4 * q], w.x);
+          c[2 + 4 * q] = max(c[2 + 4 * q], w.y);
+          c[3 + 4 * q] = max(c[3 + 4 * q], w.z);
+          c[4 + 4 * q] = max(c[4 + 4 * q], w.w);
+        }
+        c[VF_BZ + 1] = max(c[VF_BZ + 1], rp[4 + VF_BZ]);
+      }
+    } else {
+      const int rs[4][2] = {{0, 1}, {2, 1}, {1, 0}, {1, 2}};
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const uint32_t* rp = tile + ((tx + rs[r][0]) * KNY + (ty + rs[r][1])) * KP;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const uint4 w = *reinterpret_cast<const uint4*>(rp + 4 + 4 * q);
+          c[1 + 4 * q] = max(c[1 + 4 * q], w.x);
+          c[2 + 4 * q] = max(c[2 + 4 * q], w.y);
+          c[3 + 4 * q] = max(c[3 + 4 * q], w.z);
+          c[4 + 4 * q] = max(c[4 + 4 * q], w.w);
+        }
+      }
+    }
+    const uint32_t zlo = own_row[3], zhi = own_row[4 + VF_BZ];
+    uint32_t chg = 0;
+#pragma unroll
+    for (int z = 0; z < VF_BZ; ++z) {
+      uint32_t m;
+      if (CONN == 26) {
+        m = max(c[z], max(c[z + 1], c[z + 2]));
+      } else {
+        const uint32_t lo = z == 0 ? zlo : k[z - 1];
+        const uint32_t hi = z == VF_BZ - 1 ? zhi : k[z + 1];
+        m = max(c[z + 1], max(lo, hi));
+      }
+      const uint32_t cand = m >= 2u * VF_KEY_STEP ? m - VF_KEY_STEP : 0u;
+      const uint32_t kk = k[z];
+      if (kk == VF_KEY_UNREACHED && m >= VF_KEY_MIN_REACHED && m < 2u * VF_KEY_STEP) overflow = 1;
+      const uint32_t nk = kk ? max(kk, cand) : 0u;
+      if (nk != kk) { k[z] = nk; chg |= 1u << z; }
+    }
+    if (chg) {
+#pragma unroll
+      for (int z = 0; z < VF_BZ; ++z)
+        if (chg & (1u << z)) own_row[4 + z] = k[z];
+    }
+    changed |= chg;
+    if (!__syncthreads_or(chg != 0)) break;
+  }
+  const int x = x0 + tx, y = y0 + ty;
+  if (changed && x < (int)J.X && y < (int)J.Y) {
+    const int nq = min(VF_BZ, (int)J.Zk - z0) / 4;
+    uint4* dst = reinterpret_cast<uint4*>(J.keys + vf_kidx(J, x, y, z0));
+    for (int q = 0; q < nq; ++q) __stcg(dst + q, make_uint4(k[4 * q], k[4 * q + 1], k[4 * q + 2], k[4 * q + 3]));
+  }
+  if (overflow) atomicOr(&a.st[jid].err, VF_JERR_DIST_OVERFLOW);
+  // neighbour bricks touched by changed boundary voxels
+  if (changed) {
+    uint32_t dm = 0;
+    const int lastz = min(VF_BZ, (int)J.Z - z0) - 1;
+    const bool zl = (changed & 1u) != 0, zh = lastz >= 0 && (changed >> lastz) & 1u;
+    const bool xl = tx == 0, xh = tx == VF_BX - 1 || x == (int)J.X - 1;
+    const bool yl = ty == 0, yh = ty == VF_BY - 1 || y == (int)J.Y - 1;
+    if (CONN == 6) {
+      if (xl) dm |= 1u << (0 * 9 + 1 * 3 + 1);
+      if (xh) dm |= 1u << (2 * 9 + 1 * 3 + 1);
+      if (yl) dm |= 1u << (1 * 9 + 0 * 3 + 1);
+      if (yh) dm |= 1u << (1 * 9 + 2 * 3 + 1);
+      if (zl) dm |= 1u << (1 * 9 + 1 * 3 + 0);
+      if (zh) dm |= 1u << (1 * 9 + 1 * 3 + 2);
+    } else {
+      for (int dx = 0; dx < 3; ++dx) {
+        if ((dx == 0 && !xl) || (dx == 2 && !xh)) continue;
+        for (int dy = 0; dy < 3; ++dy) {
+          if ((dy == 0 && !yl) || (dy == 2 && !yh)) continue;
+          for (int dz = 0; dz < 3; ++dz) {
+            if ((dz == 0 && !zl) || (dz == 2 && !zh)) continue;
+            dm |= 1u << (dx * 9 + dy * 3 + dz);
+          }
+        }
+      }
+    }
+    dm &= ~(1u << 13);  // self
+    if (dm) atomicOr(dirs, dm);
+  }
+  if (t == 0 && it == MAXIT) *reenq = 1;
+  __syncthreads();
+  if (t < 32) {
+    const uint32_t dm = *dirs;
+    bool want = false;
+    uint32_t nb = 0;
+    if (t < 27 && ((dm >> t) & 1u) && live27[t]) {
+      want = true;
+      nb = brick_id(J, bx + t / 9 - 1, by + (t / 3) % 3 - 1, bz + t % 3 - 1);
+    }
+    if (t == 27 && *reenq) { want = true; nb = b; }
+    enqueue(a, nb, pass + 1, want);
+  }
+}
+
+__global__ void __launch_bounds__(256, 2) k_relax(FloodArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint32_t* tile = reinterpret_cast<uint32_t*>(smem_raw);
+  __shared__ uint32_t live27[27];
+  __shared__ uint32_t dirs;
+  __shared__ int reenq;
+  __shared__ uint32_t item;
+  for (uint32_t p = 0; p < a.max_passes; ++p) {
+    const uint32_t cur = p % 3u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      a.qcount[(p + 2) % 3] = 0;
+      a.qhead[(p + 2) % 3] = 0;
+    }
+    const uint32_t qn = ld_acquire(&a.qcount[cur]);
+    uint32_t visits = 0;
+    for (;;) {
+      __syncthreads();
+      if (threadIdx.x == 0) item = atomicAdd(&a.qhead[cur], 1u);
+      __syncthreads();
+      const uint32_t i = item;
+      if (i >= qn) break;
+      const uint32_t b = a.queue[cur][i];
+      const uint32_t jid = a.brick_job[b];
+      const JobDesc& J = a.jobs[jid];
+      if (J.distance == 1) relax_brick<6>(a, J, jid, b, p, tile, live27, &dirs, &reenq);
+      else relax_brick<26>(a, J, jid, b, p, tile, live27, &dirs, &reenq);
+      if (threadIdx.x == 0) atomicMax(&a.st[jid].passes, p + 1);
+      ++visits;
+    }
+    if (threadIdx.x == 0 && visits) atomicAdd(&a.stats[0], visits);
+    if (!grid_sync(a.bar, gridDim.x, a.err, a.stats)) return;
+    const uint32_t nn = ld_acquire(&a.qcount[(p + 1) % 3]);
+    if (nn == 0 || ld_acquire(a.err) != 0) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) a.stats[1] = p + 1;
+      return;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.stats[1] = a.max_passes;
+    atomicOr(a.err, 4u);  // did not converge
+  }
+}
+
+// ---------------------------------------------------------------------------
+// keys from the label grid: EMPTY -> 0, occupied -> 1 (unreached)
+__global__ void __launch_bounds__(256) k_init_keys(const JobDesc* jobs, const uint32_t* list,
+                                                   const uint32_t* count, const uint32_t* brick_job) {
+  const uint32_t n = *count;
+  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+    const uint32_t b = list[it];
+    const JobDesc& J = jobs[brick_job[b]];
+    if (!J.active) continue;
+    const uint32_t lb = b - J.brick_base;
+    const uint32_t bz = lb % J.nbz, by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
+    const uint32_t x = bx * VF_BX + threadIdx.x / VF_BY, y = by * VF_BY + threadIdx.x % VF_BY;
+    const uint32_t z0 = bz * VF_BZ;
+    if (x >= J.X || y >= J.Y) continue;
+    const uint32_t* g = reinterpret_cast<const uint32_t*>(J.grid + vf_gidx(J, x, y, z0));
+    uint4* d = reinterpret_cast<uint4*>(J.keys + vf_kidx(J, x, y, z0));
+    const uint32_t nq = min((uint32_t)VF_BZ, J.Zk - z0) / 4;
+    for (uint32_t q = 0; q < nq; ++q) {
+      const uint32_t a0 = g[2 * q], a1 = g[2 * q + 1];  // Zp >= Zk, both multiples of 4
+      __stcg(d + q, make_uint4((a0 & 0xFFFFu) ? 1u : 0u, (a0 >> 16) ? 1u : 0u,
+                               (a1 & 0xFFFFu) ? 1u : 0u, (a1 >> 16) ? 1u : 0u));
+    }
+  }
+}
+
+// seed bricks must be live (a caller may seed an EMPTY voxel)
+__global__ void k_seed_bricks(const JobDesc* jobs, JobState* st, int njobs, uint8_t* live,
+                              uint32_t* list, uint32_t* count) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= njobs) return;
+  const JobDesc& J = jobs[j];
+  if (!J.active) return;
+  JobState& s = st[j];
+  for (int f = 0; f < 256; ++f) s.minprefix[f] = 0xFFFFFFFFu;
+  s.passes = 0;
+  s.disjoint = 0;
+  const uint32_t ns = s.nseeds;
+  for (uint32_t i = 0; i < ns; ++i) {
+    const uint32_t x = J.seeds[4 * i], y = J.seeds[4 * i + 1], z = J.seeds[4 * i + 2],
+                   w = J.seeds[4 * i + 3];
+    if (x >= J.X || y >= J.Y || z >= J.Z || w <= VOXEL_FREE || w > 0x7FFFu) {
+      s.err |= VF_JERR_INVALID;
+      continue;
+    }
+    const uint32_t b = J.brick_base + ((x / VF_BX) * J.nby + y / VF_BY) * J.nbz + z / VF_BZ;
+    if (!live[b]) {
+      live[b] = 1;
+      list[atomicAdd(count, 1u)] = b;
+    }
+  }
+}
+
+// seeds into the keys (later seeds win a shared voxel, as grid.set in list
+// order does, FloodFracturer.cpp:101-103) and their bricks onto queue 0
+__global__ void k_seed_keys(const JobDesc* jobs, JobState* st, int njobs, uint32_t* epoch,
+                            uint32_t* queue0, uint32_t* qcount) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= njobs) return;
+  const JobDesc& J = jobs[j];
+  if (!J.active) return;
+  JobState& s = st[j];
+  if (s.err) return;
+  const uint32_t ns = s.nseeds;
+  for (uint32_t i = 0; i < ns; ++i) {
+    const uint32_t x = J.seeds[4 * i], y = J.seeds[4 * i + 1], z = J.seeds[4 * i + 2];
+    J.keys[vf_kidx(J, x, y, z)] = ~i;
+    const uint32_t b = J.brick_base + ((x / VF_BX) * J.nby + y / VF_BY) * J.nbz + z / VF_BZ;
+    if (atomicMax(&epoch[b], 1u) < 1u) queue0[atomicAdd(qcount, 1u)] = b;
+  }
+}
+
+// keys -> labels (undoMask fused: & 0xFF unless prefixes must survive)
+__global__ void __launch_bounds__(256) k_finalize(const JobDesc* jobs, const JobState* st,
+                                                  const uint32_t* list, const uint32_t* count,
+                                                  const uint32_t* brick_job, int pass2) {
+  const uint32_t n = *count;
+  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+    const uint32_t b = list[it];
+    const uint32_t j = brick_job[b];
+    const JobDesc& J = jobs[j];
+    if (!J.active) continue;
+    const JobState& s = st[j];
+    if (pass2 && !s.has_prefix) continue;  // keys of every prefix job are final here
+    const bool keep_prefix = !pass2 && s.has_prefix;
+    const uint32_t lb = b - J.brick_base;
+    const uint32_t bz = lb % J.nbz, by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
+    const uint32_t x = bx * VF_BX + threadIdx.x / VF_BY, y = by * VF_BY + threadIdx.x % VF_BY;
+    const uint32_t z0 = bz * VF_BZ;
+    if (x >= J.X || y >= J.Y) continue;
+    const uint4* kk = reinterpret_cast<const uint4*>(J.keys + vf_kidx(J, x, y, z0));
+    uint32_t* g = reinterpret_cast<uint32_t*>(J.grid + vf_gidx(J, x, y, z0));
+    const uint32_t nq = min((uint32_t)VF_BZ, J.Zk - z0) / 4;
+    for (uint32_t q = 0; q < nq; ++q) {
+      const uint4 k4 = __ldcg(kk + q);
+      const uint32_t ks[4] = {k4.x, k4.y, k4.z, k4.w};
+      uint32_t lab[4];
+#pragma unroll
+      for (int h = 0; h < 4; ++h) {
+        const uint32_t key = ks[h];
+        uint32_t v;
+        if (key >= VF_KEY_MIN_REACHED) {
+          const uint32_t slot = (~key) & 0xFFFu;
+          v = pass2 ? s.rank_value[slot] : J.seeds[4 * slot + 3];
+          if (!keep_prefix) v &= 0xFFu;
+        } else {
+          v = key;  // 0 EMPTY, 1 FREE
+        }
+        lab[h] = v;
+      }
+      g[2 * q] = lab[0] | (lab[1] << 16);
+      g[2 * q + 1] = lab[2] | (lab[3] << 16);
+    }
+  }
+}
+
+// ---- sub-seed prefix competition: component-wise minimum prefix -----------
+__global__ void __launch_bounds__(256) k_competition(const JobDesc* jobs, JobState* st,
+                                                     const uint32_t* list, const uint32_t* count,
+                                                     const uint32_t* brick_job) {
+  const uint32_t n = *count;
+  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+    const uint32_t b = list[it];
+    const uint32_t j = brick_job[b];
+    const JobDesc& J = jobs[j];
+    if (!J.active || !st[j].has_prefix) continue;
+    const uint32_t lb = b - J.brick_base;
+    const uint32_t bz = lb % J.nbz, by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
+    const int x = bx * VF_BX + threadIdx.x / VF_BY, y = by * VF_BY + threadIdx.x % VF_BY;
+    const int z0 = bz * VF_BZ;
+    if (x >= (int)J.X || y >= (int)J.Y) continue;
+    const bool six = J.distance == 1;
+    bool any = false;
+    for (int z = z0; z < min(z0 + VF_BZ, (int)J.Z); ++z) {
+      volatile uint16_t* gv = J.grid + vf_gidx(J, x, y, z);
+      const uint32_t g = *gv;
+      if (g <= VOXEL_FREE) continue;
+      const uint32_t f = g & 0xFFu;
+      uint32_t p = g >> 8;
+      for (int dx = -1; dx <= 1; ++dx)
+        for (int dy = -1; dy <= 1; ++dy)
+          for (int dz = -1; dz <= 1; ++dz) {
+            const int nz = (dx != 0) + (dy != 0) + (dz != 0);
+            if (nz == 0 || (six && nz != 1)) continue;
+            const int ux = x + dx, uy = y + dy, uz = z + dz;
+            if (ux < 0 || uy < 0 || uz < 0 || ux >= (int)J.X || uy >= (int)J.Y || uz >= (int)J.Z) continue;
+            const uint32_t u = *(volatile uint16_t*)(J.grid + vf_gidx(J, ux, uy, uz));
+            if (u > VOXEL_FREE && (u & 0xFFu) == f && (u >> 8) < p) p = u >> 8;
+          }
+      if (p != (g >> 8)) { *gv = (uint16_t)(f | (p << 8)); any = true; }
+    }
+    if (any) atomicOr(&st[j].changed, 1u);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_minprefix(const JobDesc* jobs, JobState* st,
+                                                   const uint32_t* list, const uint32_t* count,
+                                                   const uint32_t* brick_job) {
+  const uint32_t n = *count;
+  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+    const uint32_t b = list[it];
+    const uint32_t j = brick_job[b];
+    const JobDesc& J = jobs[j];
+    if (!J.active || !st[j].has_prefix) continue;
+    const uint32_t lb = b - J.brick_base;
+    const uint32_t bz = lb % J.nbz, by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
+    const uint32_t x = bx * VF_BX + threadIdx.x / VF_BY, y = by * VF_BY + threadIdx.x % VF_BY;
+    const uint32_t z0 = bz * VF_BZ;
+    if (x >= J.X || y >= J.Y) continue;
+    for (uint32_t z = z0; z < min(z0 + VF_BZ, J.Z); ++z) {
+      const uint32_t g = J.grid[vf_gidx(J, x, y, z)];
+      if (g > VOXEL_FREE) atomicMin(&st[j].minprefix[g & 0xFFu], g >> 8);
+    }
+  }
+}
+
+// per job: surviving values sorted -> re-flood slots (ties to lowest value)
+__global__ void k_ranks(const JobDesc* jobs, JobState* st, int njobs) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= njobs || !jobs[j].active || !st[j].has_prefix) return;
+  JobState& s = st[j];
+  uint32_t nr = 0;
+  for (uint32_t f = 0; f < 256; ++f)
+    if (s.minprefix[f] != 0xFFFFFFFFu) s.rank_value[nr++] = f | (s.minprefix[f] << 8);
+  for (uint32_t a = 1; a < nr; ++a) {  // insertion sort, <= 254 entries
+    const uint32_t v = s.rank_value[a];
+    uint32_t b = a;
+    while (b > 0 && s.rank_value[b - 1] > v) { s.rank_value[b] = s.rank_value[b - 1]; --b; }
+    s.rank_value[b] = v;
+  }
+  for (uint32_t r = 0; r < nr; ++r) s.value_rank[s.rank_value[r] & 0xFFu] = r;
+  s.nranks = nr;
+}
+
+// disjointSetStack: non-minimal prefixes -> FREE; survivors keyed by slot
+__global__ void __launch_bounds__(256) k_disjoint_reset(const JobDesc* jobs, JobState* st,
+                                                        const uint32_t* list, const uint32_t* count,
+                                                        const uint32_t* brick_job) {
+  const uint32_t n = *count;
+  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+    const uint32_t b = list[it];
+    const uint32_t j = brick_job[b];
+    const JobDesc& J = jobs[j];
+    if (!J.active || !st[j].has_prefix) continue;
+    JobState& s = st[j];
+    const uint32_t lb = b - J.brick_base;
+    const uint32_t bz = lb % J.nbz, by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
+    const uint32_t x = bx * VF_BX + threadIdx.x / VF_BY, y = by * VF_BY + threadIdx.x % VF_BY;
+    const uint32_t z0 = bz * VF_BZ;
+    uint32_t reset = 0;
+    if (x < J.X && y < J.Y) {
+      for (uint32_t z = z0; z < min(z0 + VF_BZ, J.Zk); ++z) {
+        uint32_t key = 0;
+        if (z < J.Z) {
+          uint16_t* gp = J.grid + vf_gidx(J, x, y, z);
+          const uint32_t g = *gp;
+          if (g == VOXEL_FREE) key = VF_KEY_UNREACHED;
+          else if (g > VOXEL_FREE) {
+            if ((g >> 8) != s.minprefix[g & 0xFFu]) {
+              *gp = VOXEL_FREE;
+              key = VF_KEY_UNREACHED;
+              ++reset;
+            } else {
+              key = ~s.value_rank[g & 0xFFu];
+            }
+          }
+        }
+        J.keys[vf_kidx(J, x, y, z)] = key;
+      }
+    }
+    if (reset) atomicAdd(&s.disjoint, reset);
+  }
+}
+
+__global__ void k_enqueue_pass2(const JobDesc* jobs, const JobState* st, const uint32_t* list,
+                                const uint32_t* count, const uint32_t* brick_job,
+                                uint32_t* epoch, uint32_t* queue0, uint32_t* qcount) {
+  const uint32_t n = *count;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t b = list[i];
+    const uint32_t j = brick_job[b];
+    if (!jobs[j].active || !st[j].has_prefix || !st[j].disjoint) continue;
+    if (atomicMax(&epoch[b], 1u) < 1u) queue0[atomicAdd(qcount, 1u)] = b;
+  }
+}
+
+}  // namespace
+
+namespace vfk {
+
+static inline int brick_grid(uint32_t max_count) {
+  uint32_t g = max_count ? max_count : 1;
+  return (int)(g > (1u << 20) ? (1u << 20) : g);
+}
+
+void flood_init_keys(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
+                     const uint32_t* count, uint32_t max_count, const uint32_t* brick_job,
+                     const uint8_t*) {
+  if (max_count) k_init_keys<<<brick_grid(max_count), 256, 0, st>>>(dj, list, count, brick_job);
+}
+
+void flood_seed_bricks(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs, uint8_t* live,
+                       uint32_t* list, uint32_t* count) {
+  if (njobs > 0) k_seed_bricks<<<(njobs + 127) / 128, 128, 0, st>>>(dj, ds, njobs, live, list, count);
+}
+
+void flood_seed(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs,
+                const FloodScratch& fs, const uint8_t*) {
+  cudaMemsetAsync(fs.epoch, 0, sizeof(uint32_t) * fs.total_bricks, st);
+  cudaMemsetAsync(fs.qcount, 0, sizeof(uint32_t) * 3, st);
+  cudaMemsetAsync(fs.qhead, 0, sizeof(uint32_t) * 3, st);
+  cudaMemsetAsync(fs.barrier, 0, sizeof(uint32_t) * 2, st);
+  if (njobs > 0)
+    k_seed_keys<<<(njobs + 127) / 128, 128, 0, st>>>(dj, ds, njobs, fs.epoch, fs.queue[0], fs.qcount);
+}
+
+static int relax_blocks(int num_sms) {
+  static int per_sm = -1;
+  if (per_sm < 0) {
+    cudaFuncSetAttribute(k_relax, cudaFuncAttributeMaxDynamicSharedMemorySize, TILE_BYTES);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_relax, 256, TILE_BYTES) != cudaSuccess)
+      per_sm = 1;
+    if (per_sm < 1) per_sm = 1;
+  }
+  return per_sm * num_sms;
+}
+
+cudaError_t flood_relax(cudaStream_t st, const JobDesc* dj, JobState* ds,
+                        const uint32_t* brick_job, const uint8_t* live,
+                        const FloodScratch& fs, int num_sms, int* blocks_used) {
+  FloodArgs a;
+  a.jobs = dj;
+  a.st = ds;
+  a.brick_job = brick_job;
+  a.live = live;
+  a.queue[0] = fs.queue[0];
+  a.queue[1] = fs.queue[1];
+  a.queue[2] = fs.queue[2];
+  a.qcount = fs.qcount;
+  a.qhead = fs.qhead;
+  a.epoch = fs.epoch;
+  a.bar = fs.barrier;
+  a.err = fs.err;
+  a.stats = fs.stats;
+  a.max_passes = fs.max_passes;
+  const int blocks = relax_blocks(num_sms);
+  if (blocks_used) *blocks_used = blocks;
+  void* args[] = {&a};
+  return cudaLaunchCooperativeKernel((const void*)k_relax, dim3(blocks), dim3(256), args,
+                                     TILE_BYTES, st);
+}
+
+void flood_finalize(cudaStream_t st, const JobDesc* dj, const JobState* ds, const uint32_t* list,
+                    const uint32_t* count, uint32_t max_count, const uint32_t* brick_job,
+                    int pass2) {
+  if (max_count) k_finalize<<<brick_grid(max_count), 256, 0, st>>>(dj, ds, list, count, brick_job, pass2);
+}
+
+void flood_competition(cudaStream_t st, const JobDesc* dj, JobState* ds, const uint32_t* list,
+                       const uint32_t* count, uint32_t max_count, const uint32_t* brick_job) {
+  if (max_count) k_competition<<<brick_grid(max_count), 256, 0, st>>>(dj, ds, list, count, brick_job);
+}
+
+void flood_disjoint(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs,
+                    const uint32_t* list, const uint32_t* count, uint32_t max_count,
+                    const uint32_t* brick_job, const FloodScratch& fs, const uint8_t*) {
+  if (!max_count) return;
+  k_minprefix<<<brick_grid(max_count), 256, 0, st>>>(dj, ds, list, count, brick_job);
+  k_ranks<<<(njobs + 127) / 128, 128, 0, st>>>(dj, ds, njobs);
+  k_disjoint_reset<<<brick_grid(max_count), 256, 0, st>>>(dj, ds, list, count, brick_job);
+  cudaMemsetAsync(fs.epoch, 0, sizeof(uint32_t) * fs.total_bricks, st);
+  cudaMemsetAsync(fs.qcount, 0, sizeof(uint32_t) * 3, st);
+  cudaMemsetAsync(fs.qhead, 0, sizeof(uint32_t) * 3, st);
+  cudaMemsetAsync(fs.barrier, 0, sizeof(uint32_t) * 2, st);
+  k_enqueue_pass2<<<brick_grid((max_count + 255) / 256), 256, 0, st>>>(
+      dj, ds, list, count, brick_job, fs.epoch, fs.queue[0], fs.qcount);
+}
+
+}  // namespace vfk

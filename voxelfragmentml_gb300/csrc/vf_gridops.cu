@@ -1,0 +1,666 @@
+// vf_gridops.cu -- seeding, naive Voronoi, perturbation, boundary detection,
+// erosion, isolated-voxel removal and per-fragment counts on sm_103a.
+//
+// Brick kernels: one CTA (256 threads) per live brick, one thread per (x,y)
+// row of VF_BZ = 32 voxels.  The brick plus an xy halo of H voxels and a z
+// window [z0-8, z0+40) is staged in shared memory with 16-byte loads (rows
+// are 16-byte aligned because Zp % 8 == 0), results are written back as
+// 16-byte stores of whole rows (padding z >= Z written as 0).  Halo voxels
+// outside the grid read as EMPTY; voxels of bricks that are not live are
+// EMPTY in memory (both grid buffers start as the voxelizer output).
+//
+// The CTAs of a launch loop over the live-brick list (its length is read on
+// the device, so launches need no host synchronisation).
+#include "vf_kernels.h"
+
+#include <cfloat>
+
+namespace {
+
+constexpr int ZW = VF_BZ + 16;  // z window of a staged tile (u16)
+
+template <int H>
+struct Tile {
+  static constexpr int NX = VF_BX + 2 * H, NY = VF_BY + 2 * H;
+  static constexpr int ROWS = NX * NY;
+  static constexpr int BYTES = ROWS * ZW * 2;
+};
+
+__device__ __forceinline__ void brick_coords(const JobDesc& J, uint32_t b, uint32_t& x0,
+                                             uint32_t& y0, uint32_t& z0) {
+  const uint32_t lb = b - J.brick_base;
+  const uint32_t bz = lb % J.nbz, by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
+  x0 = bx * VF_BX;
+  y0 = by * VF_BY;
+  z0 = bz * VF_BZ;
+}
+
+// stage src rows [x0-H, x0+16+H) x [y0-H, y0+16+H) x [z0-8, z0+40) into tile
+template <int H>
+__device__ __forceinline__ void load_tile(const JobDesc& J, const uint16_t* src, uint32_t x0,
+                                          uint32_t y0, uint32_t z0, uint16_t* tile) {
+  using T = Tile<H>;
+  uint4* t4 = reinterpret_cast<uint4*>(tile);
+  constexpr int PER_ROW = ZW / 8;
+  for (int q = threadIdx.x; q < T::ROWS * PER_ROW; q += blockDim.x) {
+    const int row = q / PER_ROW, part = q % PER_ROW;
+    const int x = (int)x0 - H + row / T::NY, y = (int)y0 - H + row % T::NY;
+    const int z = (int)z0 - 8 + part * 8;
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (x >= 0 && y >= 0 && z >= 0 && x < (int)J.X && y < (int)J.Y && z < (int)J.Zp)
+      v = __ldg(reinterpret_cast<const uint4*>(src + vf_gidx(J, x, y, z)));
+    t4[q] = v;
+  }
+}
+template <int H>
+__device__ __forceinline__ uint16_t tval(const uint16_t* tile, int lx, int ly, int lz) {
+  // lx, ly in [-H, 16+H), lz in [-8, 40) relative to the brick origin
+  return tile[((lx + H) * Tile<H>::NY + (ly + H)) * ZW + (lz + 8)];
+}
+
+__device__ __forceinline__ void store_row(const JobDesc& J, uint16_t* dst, uint32_t x, uint32_t y,
+                                          uint32_t z0, const uint16_t* v /*32*/) {
+  const uint32_t nz = min((uint32_t)VF_BZ, J.Zp - z0);
+  uint4* d = reinterpret_cast<uint4*>(dst + vf_gidx(J, x, y, z0));
+  for (uint32_t q = 0; q < nz / 8; ++q) {
+    uint4 w;
+    w.x = (uint32_t)v[8 * q + 0] | ((uint32_t)v[8 * q + 1] << 16);
+    w.y = (uint32_t)v[8 * q + 2] | ((uint32_t)v[8 * q + 3] << 16);
+    w.z = (uint32_t)v[8 * q + 4] | ((uint32_t)v[8 * q + 5] << 16);
+    w.w = (uint32_t)v[8 * q + 6] | ((uint32_t)v[8 * q + 7] << 16);
+    d[q] = w;
+  }
+}
+
+// ===========================================================================
+// Seeding: Seeder::uniform (Seeder.cpp:154-208) + mergeSeeds (:115-152).
+// One 1024-thread block per job.  Attempts are evaluated 1024 at a time in
+// parallel; warp 0 then accepts them in attempt order (duplicates skipped),
+// which is exactly the sequential rejection loop of the reference.
+__device__ __forceinline__ bool occupied_at(const JobDesc& J, int x, int y, int z) {
+  return J.grid[vf_gidx(J, x, y, z)] != VOXEL_EMPTY;
+}
+__device__ bool is_boundary(const JobDesc& J, int x, int y, int z) {
+  // RegularGrid::isBoundary(x,y,z,1) (RegularGrid.cpp:543-559)
+  const int x0 = vf_clampi(x - 1, 0, J.X - 1), x1 = vf_clampi(x + 1, 0, J.X - 1);
+  const int y0 = vf_clampi(y - 1, 0, J.Y - 1), y1 = vf_clampi(y + 1, 0, J.Y - 1);
+  const int z0 = vf_clampi(z - 1, 0, J.Z - 1), z1 = vf_clampi(z + 1, 0, J.Z - 1);
+  for (int a = x0; a <= x1; ++a)
+    for (int b = y0; b <= y1; ++b)
+      for (int c = z0; c <= z1; ++c)
+        if (J.grid[vf_gidx(J, a, b, c)] == VOXEL_EMPTY) return true;
+  return false;
+}
+
+struct SeedSmem {
+  unsigned long long acc[4096];
+  unsigned long long cand[1024];
+  uint16_t near_[4096];
+  uint32_t idf[256];
+  uint32_t cnt;
+  uint32_t fail;
+};
+
+// returns false on SeederSearchError; out receives n xyzw entries
+__device__ bool uniform_block(const JobDesc& J, SeedSmem& S, uint32_t n, uint64_t seed,
+                              int location, uint32_t* out) {
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  if (t == 0) { S.cnt = 0; S.fail = 0; }
+  __syncthreads();
+  const float fx = (float)(J.X - 1), fy = (float)(J.Y - 1), fz = (float)(J.Z - 1);
+  for (uint32_t base = 0;; base += 1024) {
+    if (S.cnt >= n || S.fail) break;
+    if (base >= VF_MAX_TRIES) { if (t == 0) S.fail = 1; __syncthreads(); break; }
+    const uint32_t a = base + t;
+    unsigned long long key = ~0ull;
+    if (a < VF_MAX_TRIES) {
+      const int x = (int)__fmul_rn(fx, vf_u01(vf_hash(seed, VF_STREAM_SEEDS, 3ull * a + 0)));
+      const int y = (int)__fmul_rn(fy, vf_u01(vf_hash(seed, VF_STREAM_SEEDS, 3ull * a + 1)));
+      const int z = (int)__fmul_rn(fz, vf_u01(vf_hash(seed, VF_STREAM_SEEDS, 3ull * a + 2)));
+      bool ok = occupied_at(J, x, y, z);
+      if (ok && location != 2) ok = ((location == 1) == is_boundary(J, x, y, z));
+      if (ok) key = ((unsigned long long)x << 24) | ((unsigned long long)y << 12) | (unsigned long long)z;
+    }
+    S.cand[t] = key;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t cnt = S.cnt;
+      for (int i = 0; i < 1024 && cnt < n; ++i) {
+        const unsigned long long k = S.cand[i];
+        if (k == ~0ull) continue;
+        bool dup = false;
+        for (uint32_t m = lane; m < cnt; m += 32) dup |= (S.acc[m] == k);
+        dup = __any_sync(0xFFFFFFFFu, dup);
+        if (!dup) {
+          if (lane == 0) S.acc[cnt] = k;
+          ++cnt;
+        }
+        __syncwarp();
+      }
+      if (lane == 0) S.cnt = cnt;
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  if (S.fail || S.cnt < n) return false;
+  // sort lexicographically (std::set<uvec3>), bitonic over the next power of 2
+  uint32_t P = 1;
+  while (P < n) P <<= 1;
+  for (uint32_t i = n + t; i < P; i += blockDim.x) S.acc[i] = ~0ull;
+  __syncthreads();
+  for (uint32_t k = 2; k <= P; k <<= 1)
+    for (uint32_t jx = k >> 1; jx > 0; jx >>= 1) {
+      for (uint32_t i = t; i < P; i += blockDim.x) {
+        const uint32_t l = i ^ jx;
+        if (l > i) {
+          const unsigned long long a = S.acc[i], b = S.acc[l];
+          const bool up = (i & k) == 0;
+          if ((a > b) == up) { S.acc[i] = b; S.acc[l] = a; }
+        }
+      }
+      __syncthreads();
+    }
+  for (uint32_t i = t; i < n; i += blockDim.x) {
+    const unsigned long long k = S.acc[i];
+    out[4 * i] = (uint32_t)(k >> 24);
+    out[4 * i + 1] = (uint32_t)((k >> 12) & 0xFFF);
+    out[4 * i + 2] = (uint32_t)(k & 0xFFF);
+    out[4 * i + 3] = VOXEL_FREE + 1 + i;
+  }
+  __syncthreads();
+  return true;
+}
+
+__device__ __forceinline__ float seed_dist(int dfunc, const uint32_t* s, const uint32_t* f) {
+  const float dx = __fsub_rn((float)s[0], (float)f[0]), dy = __fsub_rn((float)s[1], (float)f[1]),
+              dz = __fsub_rn((float)s[2], (float)f[2]);
+  if (dfunc == 0)
+    return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+  if (dfunc == 1) return __fadd_rn(__fadd_rn(fabsf(dx), fabsf(dy)), fabsf(dz));
+  return fmaxf(fabsf(dx), fmaxf(fabsf(dy), fabsf(dz)));
+}
+
+__global__ void __launch_bounds__(1024) k_seeds(const JobDesc* jobs, JobState* st) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SeedSmem& S = *reinterpret_cast<SeedSmem*>(smem_raw);
+  const JobDesc& J = jobs[blockIdx.x];
+  JobState& js = st[blockIdx.x];
+  const int t = threadIdx.x;
+  if (!J.active) return;
+  if (J.seeds_given) {
+    if (t == 0) {
+      js.nseeds = J.seeds_given;
+      uint32_t hp = 0;
+      for (uint32_t i = 0; i < J.seeds_given; ++i) hp |= J.seeds[4 * i + 3] > 0xFFu;
+      js.has_prefix = hp;
+    }
+    return;
+  }
+  const uint32_t nm = (uint32_t)J.num_seeds, ne = (uint32_t)J.num_extra;
+  if (J.X < 2 || J.Y < 2 || J.Z < 2 || nm > 254 || 2 * nm + ne > J.seeds_cap) {
+    if (t == 0) { js.err |= VF_JERR_INVALID; js.nseeds = 0; }
+    return;
+  }
+  if (!uniform_block(J, S, nm, J.seed, J.seed_location, J.seeds)) {
+    if (t == 0) { js.err |= VF_JERR_SEED_SEARCH; js.nseeds = 0; }
+    return;
+  }
+  uint32_t total = nm;
+  if (ne > 0 && nm > 0) {
+    // extraSeeds = uniform(BOTH) after a copy of the main seeds, merged
+    // (CADScene.cpp:647-655); seed value seed + golden ratio
+    uint32_t* list = J.seeds + 4 * (size_t)nm;
+    for (uint32_t i = t; i < 4 * nm; i += blockDim.x) list[i] = J.seeds[i];
+    __syncthreads();
+    if (!uniform_block(J, S, ne, J.seed + 0x9E3779B97F4A7C15ull, 2, list + 4 * (size_t)nm)) {
+      if (t == 0) { js.err |= VF_JERR_SEED_SEARCH; js.nseeds = 0; }
+      return;
+    }
+    const uint32_t nl = nm + ne;
+    for (uint32_t k = t; k < nl; k += blockDim.x) {
+      float best = FLT_MAX;
+      int nearest = 0;
+      for (uint32_t i = 0; i < nm; ++i) {
+        const float d = seed_dist(J.merge_distance, list + 4 * k, J.seeds + 4 * i);
+        if (d < best) { best = d; nearest = (int)i; }
+      }
+      S.near_[k] = (uint16_t)nearest;
+    }
+    for (uint32_t i = t; i < 256; i += blockDim.x) S.idf[i] = 0;
+    __syncthreads();
+    if (t == 0) {
+      for (uint32_t k = 0; k < nl; ++k) {
+        const uint32_t w = J.seeds[4 * S.near_[k] + 3];
+        const uint32_t pre = ++S.idf[w & 0xFFu];
+        if (pre > 127) js.err |= VF_JERR_RANGE;
+        list[4 * k + 3] = w | (pre << 8);
+      }
+    }
+    total = 2 * nm + ne;
+  }
+  __syncthreads();
+  if (t == 0) {
+    js.nseeds = total;
+    uint32_t hp = 0;
+    for (uint32_t i = 0; i < total; ++i) hp |= J.seeds[4 * i + 3] > 0xFFu;
+    js.has_prefix = hp;
+  }
+}
+
+// ===========================================================================
+// NaiveFracturer::buildCPU (NaiveFracturer.cpp:26-68): every occupied voxel
+// takes the label of the nearest seed; strict '<' keeps the lowest index.
+__global__ void __launch_bounds__(256) k_naive(const JobDesc* jobs, const JobState* st,
+                                               const uint32_t* list, const uint32_t* count,
+                                               const uint32_t* brick_job) {
+  __shared__ uint4 sd[512];
+  const uint32_t n = *count;
+  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+    const uint32_t b = list[it];
+    const uint32_t j = brick_job[b];
+    const JobDesc& J = jobs[j];
+    if (!J.active) continue;
+    const uint32_t ns = st[j].nseeds;
+    uint32_t x0, y0, z0;
+    brick_coords(J, b, x0, y0, z0);
+    const uint32_t x = x0 + threadIdx.x / VF_BY, y = y0 + threadIdx.x % VF_BY;
+    const bool row_ok = x < J.X && y < J.Y;
+    uint16_t v[VF_BZ];
+    float best[VF_BZ];
+    if (row_ok) {
+      const uint4* src = reinterpret_cast<const uint4*>(J.grid + vf_gidx(J, x, y, z0));
+      const uint32_t nz = min((uint32_t)VF_BZ, J.Zp - z0);
+#pragma unroll
+      for (int q = 0; q < VF_BZ / 8; ++q) {
+        uint4 w = (q * 8 < (int)nz) ? src[q] : make_uint4(0, 0, 0, 0);
+        v[8 * q + 0] = w.x & 0xFFFF; v[8 * q + 1] = w.x >> 16;
+        v[8 * q + 2] = w.y & 0xFFFF; v[8 * q + 3] = w.y >> 16;
+        v[8 * q + 4] = w.z & 0xFFFF; v[8 * q + 5] = w.z >> 16;
+        v[8 * q + 6] = w.w & 0xFFFF; v[8 * q + 7] = w.w >> 16;
+      }
+    }
+#pragma unroll
+    for (int z = 0; z < VF_BZ; ++z) best[z] = FLT_MAX;
+    for (uint32_t c0 = 0; c0 < ns; c0 += 512) {
+      __syncthreads();
+      for (uint32_t i = threadIdx.x; i < 512 && c0 + i < ns; i += blockDim.x)
+        sd[i] = reinterpret_cast<const uint4*>(J.seeds)[c0 + i];
+      __syncthreads();
+      if (!row_ok) continue;
+      const uint32_t cn = min(512u, ns - c0);
+      for (uint32_t s = 0; s < cn; ++s) {
+        const uint4 sp = sd[s];
+        const int dx = (int)x - (int)sp.x, dy = (int)y - (int)sp.y;
+#pragma unroll
+        for (int z = 0; z < VF_BZ; ++z) {
+          const int dz = (int)(z0 + z) - (int)sp.z;
+          float d;
+          if (J.distance == 0) {
+            const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
+            d = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy)), __fmul_rn(fz, fz)));
+          } else if (J.distance == 1) {
+            d = (float)(abs(dx) + abs(dy) + abs(dz));
+          } else {
+            d = (float)max(abs(dx), max(abs(dy), abs(dz)));
+          }
+          if (v[z] != VOXEL_EMPTY && d < best[z]) { best[z] = d; v[z] = (uint16_t)sp.w; }
+        }
+      }
+    }
+    if (row_ok) {
+      // padding voxels stay 0 (they are EMPTY and never labelled)
+      store_row(J, J.grid, x, y, z0, v);
+    }
+  }
+}
+
+// ===========================================================================
+// Boundary perturbation (no reference counterpart).  Lattice values are
+// precomputed per job; per voxel the 3-channel trilinear noise gives the
+// offset of the voxel whose label is taken.  Reads src, writes dst.
+__global__ void k_lattice(const JobDesc* jobs) {
+  const JobDesc& J = jobs[blockIdx.y];
+  if (!J.active) return;
+  const uint32_t n = J.lat_nx * J.lat_ny * J.lat_nz * 3;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t c = i % 3, p = i / 3;
+    const uint32_t iz = p % J.lat_nz, iy = (p / J.lat_nz) % J.lat_ny, ix = p / (J.lat_nz * J.lat_ny);
+    const uint64_t ctr = (((uint64_t)ix << 40) | ((uint64_t)iy << 20) | iz) * 4u + c;
+    J.lattice[i] = __fsub_rn(__fmul_rn(vf_u01(vf_hash(J.seed, VF_STREAM_NOISE, ctr)), 2.0f), 1.0f);
+  }
+}
+
+__device__ __forceinline__ float lerp_(float a, float b, float t) {
+  return __fadd_rn(a, __fmul_rn(t, __fsub_rn(b, a)));
+}
+
+__device__ __forceinline__ uint16_t perturb_voxel(const JobDesc& J, const uint16_t* src, uint32_t x,
+                                                  uint32_t y, uint32_t z, uint16_t g) {
+  const uint32_t P = J.noise_period;
+  const float fp = (float)P;
+  const uint32_t i0 = x / P, i1 = y / P, i2 = z / P;
+  const float t0 = __fdiv_rn((float)(x % P), fp), t1 = __fdiv_rn((float)(y % P), fp),
+              t2 = __fdiv_rn((float)(z % P), fp);
+  const uint32_t sy = J.lat_nz * 3, sx = J.lat_ny * sy;
+  const float* L = J.lattice + (size_t)i0 * sx + (size_t)i1 * sy + (size_t)i2 * 3;
+  int o[3];
+#pragma unroll
+  for (int ch = 0; ch < 3; ++ch) {
+    const float c000 = L[ch], c001 = L[3 + ch];
+    const float c010 = L[sy + ch], c011 = L[sy + 3 + ch];
+    const float c100 = L[sx + ch], c101 = L[sx + 3 + ch];
+    const float c110 = L[sx + sy + ch], c111 = L[sx + sy + 3 + ch];
+    const float c00 = lerp_(c000, c001, t2), c01 = lerp_(c010, c011, t2);
+    const float c10 = lerp_(c100, c101, t2), c11 = lerp_(c110, c111, t2);
+    const float c0 = lerp_(c00, c01, t1), c1 = lerp_(c10, c11, t1);
+    const float nz = lerp_(c0, c1, t0);
+    o[ch] = (int)floorf(__fadd_rn(__fmul_rn(J.noise_amplitude, nz), 0.5f));
+  }
+  const long ux = (long)x + o[0], uy = (long)y + o[1], uz = (long)z + o[2];
+  if (ux < 0 || uy < 0 || uz < 0 || ux >= (long)J.X || uy >= (long)J.Y || uz >= (long)J.Z) return g;
+  const uint16_t u = src[vf_gidx(J, (uint32_t)ux, (uint32_t)uy, (uint32_t)uz)];
+  return u > VOXEL_FREE ? u : g;
+}
+
+__global__ void __launch_bounds__(256) k_perturb(const JobDesc* jobs, const uint32_t* list,
+                                                 const uint32_t* count, const uint32_t* brick_job) {
+  const uint32_t n = *count;
+  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+    const uint32_t b = list[it];
+    const JobDesc& J = jobs[brick_job[b]];
+    if (!J.active) continue;
+    uint32_t x0, y0, z0;
+    brick_coords(J, b, x0, y0, z0);
+    const uint32_t x = x0 + threadIdx.x / VF_BY, y = y0 + threadIdx.x % VF_BY;
+    if (x >= J.X || y >= J.Y) continue;
+    const uint16_t* src = J.grid;
+    uint16_t v[VF_BZ];
+    const uint4* s4 = reinterpret_cast<const uint4*>(src + vf_gidx(J, x, y, z0));
+    const uint32_t nz = min((uint32_t)VF_BZ, J.Zp - z0);
+#pragma unroll
+    for (int q = 0; q < VF_BZ / 8; ++q) {
+      uint4 w = (q * 8 < (int)nz) ? s4[q] : make_uint4(0, 0, 0, 0);
+      v[8 * q + 0] = w.x & 0xFFFF; v[8 * q + 1] = w.x >> 16;
+      v[8 * q + 2] = w.y & 0xFFFF; v[8 * q + 3] = w.y >> 16;
+      v[8 * q + 4] = w.z & 0xFFFF; v[8 * q + 5] = w.z >> 16;
+      v[8 * q + 6] = w.w & 0xFFFF; v[8 * q + 7] = w.w >> 16;
+    }
+#pragma unroll 4
+    for (int z = 0; z < VF_BZ; ++z)
+      if (v[z] > VOXEL_FREE) v[z] = perturb_voxel(J, src, x, y, z0 + z, v[z]);
+    store_row(J, J.grid2, x, y, z0, v);
+  }
+}
+
+// ===========================================================================
+// detectBoundaries-comp.glsl:18-43 (in place; neighbour reads clear bit 15,
+// so concurrent updates of neighbours cannot change the outcome).
+template <int H>
+__global__ void __launch_bounds__(256) k_detect(const JobDesc* jobs, const uint32_t* list,
+                                                const uint32_t* count, const uint32_t* brick_job) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint16_t* tile = reinterpret_cast<uint16_t*>(smem_raw);
+  const uint32_t n = *count;
+  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+    const uint32_t b = list[it];
+    const JobDesc& J = jobs[brick_job[b]];
+    if (!J.active) continue;  // uniform across the CTA
+    uint32_t x0, y0, z0;
+    brick_coords(J, b, x0, y0, z0);
+    __syncthreads();
+    load_tile<H>(J, J.grid, x0, y0, z0, tile);
+    __syncthreads();
+    const int lx = threadIdx.x / VF_BY, ly = threadIdx.x % VF_BY;
+    const uint32_t x = x0 + lx, y = y0 + ly;
+    if (x >= J.X || y >= J.Y) continue;
+    const int bs = J.boundary_size;
+    uint16_t v[VF_BZ];
+    bool any = false;
+    for (int z = 0; z < VF_BZ; ++z) {
+      const uint16_t g = tval<H>(tile, lx, ly, z);
+      v[z] = g;
+      const int gz = (int)z0 + z;
+      if (g <= VOXEL_FREE || gz >= (int)J.Z) continue;
+      const int xa = max((int)x - bs, 0) - (int)x0, xb = min((int)x + bs, (int)J.X - 1) - (int)x0;
+      const int ya = max((int)y - bs, 0) - (int)y0, yb = min((int)y + bs, (int)J.Y - 1) - (int)y0;
+      const int za = max(gz - bs, 0) - (int)z0, zb = min(gz + bs, (int)J.Z - 1) - (int)z0;
+      bool bd = false;
+      for (int a = xa; a <= xb && !bd; ++a)
+        for (int c = ya; c <= yb && !bd; ++c)
+          for (int d = za; d <= zb && !bd; ++d) {
+            const uint16_t u = tval<H>(tile, a, c, d) & 0x7FFFu;
+            bd = u > VOXEL_FREE && u != g;
+          }
+      if (bd) { v[z] = g | 0x8000u; any = true; }
+    }
+    if (any) store_row(J, J.grid, x, y, z0, v);
+  }
+}
+
+// erodeGrid-comp.glsl:26-59: src -> dst.  Gate bool(unmaskedBit(v,15)) holds
+// for every labelled voxel; full 16-bit equality; globalCount = clamped
+// window size; noise[idx % 1e6] from the counter RNG.
+template <int H>
+__global__ void __launch_bounds__(256) k_erode(const JobDesc* jobs, const uint32_t* list,
+                                               const uint32_t* count, const uint32_t* brick_job) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint16_t* tile = reinterpret_cast<uint16_t*>(smem_raw);
+  float* mask = reinterpret_cast<float*>(smem_raw + Tile<H>::BYTES);
+  const uint32_t n = *count;
+  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+    const uint32_t b = list[it];
+    const JobDesc& J = jobs[brick_job[b]];
+    if (!J.active) continue;
+    uint32_t x0, y0, z0;
+    brick_coords(J, b, x0, y0, z0);
+    const int k = J.ek, m2 = k / 2;
+    __syncthreads();
+    load_tile<H>(J, J.grid, x0, y0, z0, tile);
+    for (int i = threadIdx.x; i < k * k * k; i += blockDim.x) mask[i] = J.emask[i];
+    __syncthreads();
+    const int lx = threadIdx.x / VF_BY, ly = threadIdx.x % VF_BY;
+    const uint32_t x = x0 + lx, y = y0 + ly;
+    if (x >= J.X || y >= J.Y) continue;
+    uint16_t v[VF_BZ];
+    const unsigned long long rowlin = ((unsigned long long)x * J.Y + y) * J.Z;
+    for (int z = 0; z < VF_BZ; ++z) {
+      const uint16_t g = tval<H>(tile, lx, ly, z);
+      v[z] = g;
+      const int gz = (int)z0 + z;
+      if (gz >= (int)J.Z) continue;
+      if (!(g > VOXEL_FREE && (g & 0x7FFFu) != 0)) continue;
+      const uint32_t nidx = (uint32_t)((rowlin + gz) % VF_NOISE_BUFFER);
+      if (!(vf_u01(vf_hash(J.seed, VF_STREAM_ERODE, nidx)) < J.erosion_probability)) continue;
+      const int mnx = (int)x - m2, mny = (int)y - m2, mnz = gz - m2;
+      const int xa = max(mnx, 0), xb = min((int)x + m2, (int)J.X - 1);
+      const int ya = max(mny, 0), yb = min((int)y + m2, (int)J.Y - 1);
+      const int za = max(mnz, 0), zb = min(gz + m2, (int)J.Z - 1);
+      uint32_t cnt = 0, global = 0;
+      for (int a = xa; a <= xb; ++a)
+        for (int c = ya; c <= yb; ++c)
+          for (int d = za; d <= zb; ++d) {
+            const float m = mask[(a - mnx) * k * k + (c - mny) * k + (d - mnz)];
+            const float eq = (float)(tval<H>(tile, a - (int)x0, c - (int)y0, d - (int)z0) == g);
+            cnt += (uint32_t)__fmul_rn(eq, m);
+            ++global;
+          }
+      const float act = __fdiv_rn((float)cnt, (float)global);
+      if (act < J.elimit) v[z] = VOXEL_EMPTY;
+    }
+    store_row(J, J.grid2, x, y, z0, v);
+  }
+}
+
+// removeIsolatedRegionsGrid-comp.glsl:16-39, src -> dst (Jacobi)
+__global__ void __launch_bounds__(256) k_isolated(const JobDesc* jobs, const uint32_t* list,
+                                                  const uint32_t* count, const uint32_t* brick_job) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint16_t* tile = reinterpret_cast<uint16_t*>(smem_raw);
+  const uint32_t n = *count;
+  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+    const uint32_t b = list[it];
+    const JobDesc& J = jobs[brick_job[b]];
+    if (!J.active) continue;
+    uint32_t x0, y0, z0;
+    brick_coords(J, b, x0, y0, z0);
+    __syncthreads();
+    load_tile<1>(J, J.grid, x0, y0, z0, tile);
+    __syncthreads();
+    const int lx = threadIdx.x / VF_BY, ly = threadIdx.x % VF_BY;
+    const uint32_t x = x0 + lx, y = y0 + ly;
+    if (x >= J.X || y >= J.Y) continue;
+    uint16_t v[VF_BZ];
+    const int xa = ((int)x > 0 ? -1 : 0) + lx, xb = ((int)x + 1 < (int)J.X ? 1 : 0) + lx;
+    const int ya = ((int)y > 0 ? -1 : 0) + ly, yb = ((int)y + 1 < (int)J.Y ? 1 : 0) + ly;
+    for (int z = 0; z < VF_BZ; ++z) {
+      const uint16_t g = tval<1>(tile, lx, ly, z);
+      v[z] = g;
+      const int gz = (int)z0 + z;
+      if (gz >= (int)J.Z || g == VOXEL_EMPTY) continue;  // EMPTY stays EMPTY
+      const int za = (gz > 0 ? -1 : 0) + z, zb = (gz + 1 < (int)J.Z ? 1 : 0) + z;
+      int c = -1;
+      for (int a = xa; a <= xb; ++a)
+        for (int q = ya; q <= yb; ++q)
+          for (int d = za; d <= zb; ++d) c += tval<1>(tile, a, q, d) == g;
+      if (c < 6) v[z] = VOXEL_EMPTY;
+    }
+    store_row(J, J.grid2, x, y, z0, v);
+  }
+}
+
+// RegularGrid::countValues (RegularGrid.cpp:601-625)
+__global__ void __launch_bounds__(256) k_counts(const JobDesc* jobs, JobState* st,
+                                                const uint32_t* list, const uint32_t* count,
+                                                const uint32_t* brick_job) {
+  __shared__ uint32_t hist[256];
+  __shared__ unsigned long long occ;
+  const uint32_t n = *count;
+  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+    const uint32_t b = list[it];
+    const uint32_t j = brick_job[b];
+    const JobDesc& J = jobs[j];
+    if (!J.active) continue;
+    uint32_t x0, y0, z0;
+    brick_coords(J, b, x0, y0, z0);
+    __syncthreads();
+    hist[threadIdx.x] = 0;
+    if (threadIdx.x == 0) occ = 0;
+    __syncthreads();
+    const uint32_t x = x0 + threadIdx.x / VF_BY, y = y0 + threadIdx.x % VF_BY;
+    uint32_t mine = 0, err = 0;
+    if (x < J.X && y < J.Y) {
+      const uint4* s4 = reinterpret_cast<const uint4*>(J.grid + vf_gidx(J, x, y, z0));
+      const uint32_t nz = min((uint32_t)VF_BZ, J.Zp - z0);
+      for (uint32_t q = 0; q < nz / 8; ++q) {
+        const uint4 w = s4[q];
+        const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int h = 0; h < 8; ++h) {
+          const uint32_t g = (ww[h >> 1] >> (16 * (h & 1))) & 0xFFFFu;
+          if (g > VOXEL_FREE) {
+            const uint32_t val = g & 0x7FFFu;
+            ++mine;
+            if (val < 256) atomicAdd(&hist[val], 1u);
+            else if (val < J.ncounts) atomicAdd(&J.counts[val], 1u);
+            else err = 1;
+          }
+        }
+      }
+    }
+    if (mine) atomicAdd(&occ, (unsigned long long)mine);
+    if (err) atomicOr(&st[j].err, VF_JERR_RANGE);
+    __syncthreads();
+    const uint32_t h = hist[threadIdx.x];
+    if (h) {
+      if (threadIdx.x < J.ncounts) atomicAdd(&J.counts[threadIdx.x], h);
+      else atomicOr(&st[j].err, VF_JERR_RANGE);
+    }
+    if (threadIdx.x == 0 && occ) atomicAdd(&st[j].occupied, occ);
+  }
+}
+
+}  // namespace
+
+namespace vfk {
+
+static inline int brick_grid(uint32_t max_count) {
+  uint32_t g = max_count ? max_count : 1;
+  return (int)(g > (1u << 20) ? (1u << 20) : g);
+}
+
+void sample_seeds(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_seeds, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SeedSmem));
+    attr = true;
+  }
+  if (njobs > 0) k_seeds<<<njobs, 1024, sizeof(SeedSmem), st>>>(dj, ds);
+}
+
+void naive(cudaStream_t st, const JobDesc* dj, const JobState* ds, const uint32_t* list,
+           const uint32_t* count, uint32_t max_count, const uint32_t* brick_job) {
+  if (max_count) k_naive<<<brick_grid(max_count), 256, 0, st>>>(dj, ds, list, count, brick_job);
+}
+
+void lattice(cudaStream_t st, const JobDesc* dj, int njobs) {
+  if (njobs > 0) k_lattice<<<dim3(64, njobs), 256, 0, st>>>(dj);
+}
+void perturb(cudaStream_t st, const JobDesc* dj, const uint32_t* list, const uint32_t* count,
+             uint32_t max_count, const uint32_t* brick_job) {
+  if (max_count) k_perturb<<<brick_grid(max_count), 256, 0, st>>>(dj, list, count, brick_job);
+}
+
+template <int H>
+static void detect_h(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
+                     const uint32_t* count, uint32_t max_count, const uint32_t* brick_job) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_detect<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, Tile<H>::BYTES);
+    attr = true;
+  }
+  k_detect<H><<<brick_grid(max_count), 256, Tile<H>::BYTES, st>>>(dj, list, count, brick_job);
+}
+void detect_boundaries(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
+                       const uint32_t* count, uint32_t max_count, const uint32_t* brick_job) {
+  // boundary sizes 0..3 share the H = 3 tile; 1 (the default) uses H = 1
+  if (!max_count) return;
+  detect_h<1>(st, dj, list, count, max_count, brick_job);
+}
+void detect_boundaries_wide(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
+                            const uint32_t* count, uint32_t max_count, const uint32_t* brick_job) {
+  if (!max_count) return;
+  detect_h<3>(st, dj, list, count, max_count, brick_job);
+}
+
+template <int H>
+static void erode_h(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
+                    const uint32_t* count, uint32_t max_count, const uint32_t* brick_job) {
+  static bool attr = false;
+  const int bytes = Tile<H>::BYTES + 343 * 4;
+  if (!attr) {
+    cudaFuncSetAttribute(k_erode<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    attr = true;
+  }
+  k_erode<H><<<brick_grid(max_count), 256, bytes, st>>>(dj, list, count, brick_job);
+}
+void erode(cudaStream_t st, const JobDesc* dj, const uint32_t* list, const uint32_t* count,
+           uint32_t max_count, const uint32_t* brick_job) {
+  if (!max_count) return;
+  erode_h<3>(st, dj, list, count, max_count, brick_job);
+}
+void remove_isolated(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
+                     const uint32_t* count, uint32_t max_count, const uint32_t* brick_job) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_isolated, cudaFuncAttributeMaxDynamicSharedMemorySize, Tile<1>::BYTES);
+    attr = true;
+  }
+  if (max_count)
+    k_isolated<<<brick_grid(max_count), 256, Tile<1>::BYTES, st>>>(dj, list, count, brick_job);
+}
+void count_values(cudaStream_t st, const JobDesc* dj, JobState* ds, const uint32_t* list,
+                  const uint32_t* count, uint32_t max_count, const uint32_t* brick_job) {
+  if (max_count) k_counts<<<brick_grid(max_count), 256, 0, st>>>(dj, ds, list, count, brick_job);
+}
+
+}  // namespace vfk

@@ -1,0 +1,100 @@
+// vf_kernels.h -- host launchers of the device stages (internal).
+//
+// Every launcher takes a device array of JobDesc (one table per stage, see
+// vf_runtime.cu) plus the per-job JobState array, and enqueues on `st`.
+// Brick-parallel stages take the list of live bricks and brick_job map.
+#pragma once
+#include "vf_common.cuh"
+
+namespace vfk {
+
+// ---- voxelizer (Tetravoxelizer + tri-box SAT) ----
+void centroid_and_slices(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs);
+void tetra_prep(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs,
+                uint32_t total_faces);
+void parity_raster(cudaStream_t st, const JobDesc* dj, int njobs, uint32_t total_faces);
+void shell_sat(cudaStream_t st, const JobDesc* dj, int njobs, uint32_t total_faces);
+// writes 0/1 labels (grid, and grid2 when dual) for every brick of every
+// job and sets live[b]
+void combine(cudaStream_t st, const JobDesc* dj, const uint32_t* brick_job,
+             uint32_t total_bricks, uint8_t* live, int dual);
+void mark_live(cudaStream_t st, const JobDesc* dj, const uint32_t* brick_job,
+               uint32_t total_bricks, uint8_t* live);
+void compact_live(cudaStream_t st, const uint8_t* live, uint32_t total_bricks,
+                  uint32_t* list, uint32_t* count);
+
+// ---- seeds ----
+void sample_seeds(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs);
+
+// ---- fracturers ----
+void naive(cudaStream_t st, const JobDesc* dj, const JobState* ds, const uint32_t* list,
+           const uint32_t* count, uint32_t max_count, const uint32_t* brick_job);
+
+// ---- grid passes (brick kernels, live bricks only) ----
+void lattice(cudaStream_t st, const JobDesc* dj, int njobs);
+void perturb(cudaStream_t st, const JobDesc* dj, const uint32_t* list, const uint32_t* count,
+             uint32_t max_count, const uint32_t* brick_job);
+void detect_boundaries(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
+                       const uint32_t* count, uint32_t max_count, const uint32_t* brick_job);
+// boundary sizes 2..3
+void detect_boundaries_wide(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
+                            const uint32_t* count, uint32_t max_count, const uint32_t* brick_job);
+void erode(cudaStream_t st, const JobDesc* dj, const uint32_t* list, const uint32_t* count,
+           uint32_t max_count, const uint32_t* brick_job);
+void remove_isolated(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
+                     const uint32_t* count, uint32_t max_count, const uint32_t* brick_job);
+void count_values(cudaStream_t st, const JobDesc* dj, JobState* ds, const uint32_t* list,
+                  const uint32_t* count, uint32_t max_count, const uint32_t* brick_job);
+
+// ---- flood (vf_flood.cu) ----
+struct FloodScratch {
+  uint32_t* queue[3];    // brick ids, capacity total_bricks each (rotating)
+  uint32_t* qcount;      // [3]
+  uint32_t* qhead;       // [3]
+  uint32_t* epoch;       // [total_bricks]
+  uint32_t* barrier;     // [2] count, generation
+  uint32_t* err;         // [1] global error word
+  uint32_t* stats;       // [4] brick visits, passes, overflow, timeout
+  uint32_t max_passes;
+  uint32_t total_bricks;
+};
+void flood_init_keys(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
+                     const uint32_t* count, uint32_t max_count, const uint32_t* brick_job,
+                     const uint8_t* live);
+void flood_seed_bricks(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs, uint8_t* live,
+                       uint32_t* list, uint32_t* count);
+void flood_seed(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs,
+                const FloodScratch& fs, const uint8_t* live);
+cudaError_t flood_relax(cudaStream_t st, const JobDesc* dj, JobState* ds,
+                        const uint32_t* brick_job, const uint8_t* live,
+                        const FloodScratch& fs, int num_sms, int* blocks_used);
+void flood_finalize(cudaStream_t st, const JobDesc* dj, const JobState* ds,
+                    const uint32_t* list, const uint32_t* count, uint32_t max_count,
+                    const uint32_t* brick_job, int pass2);
+// sub-seed prefix competition and the disjoint cleanup
+void flood_competition(cudaStream_t st, const JobDesc* dj, JobState* ds, const uint32_t* list,
+                       const uint32_t* count, uint32_t max_count, const uint32_t* brick_job);
+void flood_disjoint(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs,
+                    const uint32_t* list, const uint32_t* count, uint32_t max_count,
+                    const uint32_t* brick_job, const FloodScratch& fs, const uint8_t* live);
+
+// ---- plain (reference-shaped) per-voxel kernels for one job ----
+void plain_init_keys(cudaStream_t st, const JobDesc* dj, const JobDesc& hj);
+void plain_seed(cudaStream_t st, const JobDesc* dj, JobState* ds, uint32_t* frontier,
+                uint32_t* fcount);
+void plain_wave(cudaStream_t st, const JobDesc* dj, JobState* ds, const JobDesc& hj,
+                const uint32_t* cur, uint32_t ncur, uint32_t* next, uint32_t* ncount);
+void plain_finalize(cudaStream_t st, const JobDesc* dj, const JobState* ds, const JobDesc& hj,
+                    int pass2);
+void plain_undo_mask(cudaStream_t st, const JobDesc* dj, const JobDesc& hj);
+void plain_detect(cudaStream_t st, const JobDesc* dj, const JobDesc& hj);
+void plain_erode(cudaStream_t st, const JobDesc* dj, const JobDesc& hj);
+void plain_remove_isolated(cudaStream_t st, const JobDesc* dj, const JobDesc& hj);
+void plain_perturb(cudaStream_t st, const JobDesc* dj, const JobDesc& hj);
+void plain_naive(cudaStream_t st, const JobDesc* dj, const JobState* ds, const JobDesc& hj);
+void plain_counts(cudaStream_t st, const JobDesc* dj, JobState* ds, const JobDesc& hj);
+void plain_competition(cudaStream_t st, const JobDesc* dj, JobState* ds, const JobDesc& hj);
+void plain_disjoint(cudaStream_t st, const JobDesc* dj, JobState* ds, const JobDesc& hj,
+                    uint32_t* frontier, uint32_t* fcount);
+
+}  // namespace vfk

@@ -1,0 +1,108 @@
+// vf_runtime.h -- host runtime of the pipeline (internal).
+//
+// A Batch owns the device memory of a set of jobs (grow-only arenas), the
+// per-stage job tables and a CUDA stream.  enqueue() issues every upload,
+// stage and download of the batch asynchronously; finish() waits and fills
+// the results.  The context owns one Batch for vf_batch_run / vf_plain_run;
+// the server owns one per in-flight micro-batch.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/vf.h"
+#include "vf_kernels.h"
+
+namespace vfr {
+
+void set_error(const std::string& msg);
+vf_status fail(vf_status s, const std::string& msg);
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+
+struct JobPlan {
+  uint32_t X, Y, Z, Zp, Zk, Zw, nbx, nby, nbz, nbricks;
+  float amin[3], amax[3];
+  size_t o_grid, o_keys, o_par, o_tets, o_range, o_ys, o_seeds, o_counts, o_lat, o_verts,
+      o_faces, o_emask;
+  uint32_t ncounts, seeds_cap, lat_nx, lat_ny, lat_nz, ek;
+  float elimit;
+  std::vector<float> emask;
+  int final_cur;
+  bool prefix_possible;
+};
+
+struct Sizes {
+  size_t grid = 0, keys = 0, par = 0, tets = 0, range = 0, ys = 0, seeds = 0, counts = 0,
+         lat = 0, verts = 0, faces = 0, emask = 0;
+  uint32_t bricks = 0, faces_total = 0, max_iters = 0;
+};
+
+struct Ctx;
+
+// stage selection for Batch::enqueue_batched (the grid API runs subsets)
+enum : uint32_t {
+  ST_VOX = 1, ST_SEED = 2, ST_FRACTURE = 4, ST_PERTURB = 8, ST_ERODE = 16, ST_DETECT = 32,
+  ST_COUNT = 64, ST_DOWNLOAD = 128, ST_ALL = 255
+};
+
+struct Batch {
+  Ctx* ctx = nullptr;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  DevBuf grid0, grid1, keys, par, tets, range, ys, seeds, counts, lat, verts, faces, emask;
+  DevBuf tables, state, brick_job, live, list, lcount, q[3], scal, epoch, front[2];
+  void* h_tables = nullptr;  // pinned staging
+  size_t h_tables_cap = 0;
+  JobState* h_state = nullptr;  // pinned
+  size_t h_state_cap = 0;
+  uint32_t* h_scal = nullptr;   // pinned: [0..3] flood stats, [4] err, [8] fcount
+  cudaEvent_t ev_flood0 = nullptr, ev_flood1 = nullptr, ev_done = nullptr;
+  std::vector<JobPlan> plans;
+  std::vector<const vf_job*> jobs;
+  Sizes sz;
+  size_t bytes = 0;
+  uint32_t ntables = 0;
+  uint32_t stages = ST_ALL;
+  // caller-provided seeds per job (vf_fracture): host xyzw, count
+  std::vector<std::pair<const uint32_t*, uint32_t>> given;
+  // per-launch bookkeeping
+  uint64_t launches = 0;
+  bool flood_timed = false;
+  int relax_blocks = 0;
+
+  vf_status init(Ctx* c, bool own);
+  void release();
+  vf_status plan(const vf_job* const* js, uint32_t n);
+  vf_status enqueue_batched();
+  vf_status enqueue_plain_and_wait(vf_job_result* res, bool skip_vox);
+  vf_status finish(vf_job_result* res);
+  size_t table_off(uint32_t t) const;
+  const JobDesc* dtable(uint32_t t) const;
+};
+
+struct Ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  size_t budget = 0;
+  size_t in_use = 0;
+  cudaEvent_t ev[16] = {};
+  Batch batch;
+  // stats of the last batch
+  uint64_t last_launches = 0;
+  float last_flood_ms = 0.f;
+  uint64_t last_flood_visits = 0;
+  uint64_t last_flood_passes = 0;
+  vf_status alloc(DevBuf& b, size_t bytes);
+  void free_buf(DevBuf& b);
+};
+
+size_t job_footprint(const vf_job& j);
+
+}  // namespace vfr
