@@ -1,0 +1,387 @@
+#!/usr/bin/env python3
+"""Benchmark of the voxelize -> seed -> flood -> perturb -> boundaries ->
+count pipeline on one GB300.
+
+Workload (one "step"): the mixed-256 batch -- 256 seeded synthetic vessels
+with uneven grids (each axis log-uniform in [64, 384]), 5k-200k triangles,
+2-32 fragments, metric and noise amplitude drawn per job (about 1.4 G
+voxels, 2.8 GB of uint16 label grids).
+
+Printed JSON line (rank 0):
+  value     fragmented voxels/s of the batched path with the inputs already
+            resident in HBM (vf_batch_prepare once, vf_batch_execute per
+            step), CUDA events on the library's stream around K steps;
+  e2e       the same metric through vf_batch_run with pinned host buffers:
+            mesh upload, all stages, label-grid + count download per step;
+  plain     the reference-shaped per-job path (vf_plain_run) on a subset;
+  serving   Poisson arrivals through vf_server (continuous batching):
+            p50/p99 latency submit -> labels on host, sustained voxels/s;
+  roofline  the flood relaxation kernel against the measured HBM peak;
+  cpu_baseline the CPU oracle on a bounded sample of the same workload.
+
+`--impl reference` times the reference algorithm's CPU restatement (the
+reference itself is Windows/OpenGL-only and cannot run here) on a bounded
+sample per step, with all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "fragmented voxels/s batched+served vs plain on 1 GB300; p50/p99 job latency"
+WORKLOAD = ("mixed-256: 256 synthetic vessels, grid axes log-uniform in [64,384], "
+            "5k-200k triangles, 2-32 fragments, per-job metric and noise amplitude 0-3 "
+            "(period 16), flood + detectBoundaries(1)")
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def _oracle_params(job, O):
+    from voxelfragmentml_gb300 import workloads as W
+    import voxelfragmentml_gb300 as V  # enum values only
+    kw = W.params_for(job, V)
+    p = O.Params()
+    base = dict(algorithm=1, distance=2, num_seeds=8, num_extra_seeds=0, merge_distance=0,
+                seed_location=2, seed=80, noise_amplitude=0.0, noise_period=16, erode=0,
+                erosion_type=1, erosion_size=3, erosion_iterations=3, erosion_probability=0.5,
+                erosion_threshold=0.5, boundary_size=1)
+    base.update(kw)
+    for k, v in base.items():
+        setattr(p, k, v)
+    return p
+
+
+def cpu_sample(jobs, stride=16):
+    return [j for j in jobs if j["index"] % stride == 0]
+
+
+def run_cpu(jobs, meshes=None):
+    """Oracle (CPU restatement of the reference algorithm) over `jobs`;
+    returns (voxels, seconds)."""
+    import oracle as O
+    from voxelfragmentml_gb300 import vessel as Vs, workloads as W
+    O.build()
+    vox, secs = 0, 0.0
+    for j in jobs:
+        v, f = meshes[j["index"]] if meshes else W.mesh_for(j)
+        mn, mx = Vs.mesh_aabb(v)
+        dims = j["dims"] or Vs.grid_dims(mn, mx, j["max_dim"])
+        p = _oracle_params(j, O)
+        t = time.perf_counter()
+        O.run_job(v, f, dims, mn, mx, p)
+        secs += time.perf_counter() - t
+        vox += int(np.prod(dims))
+    return vox, secs
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from voxelfragmentml_gb300 import workloads as W
+    jobs = W.mixed(256)
+    sample = cpu_sample(jobs, args.cpu_stride)
+    meshes = {j["index"]: W.mesh_for(j) for j in sample}
+    for _ in range(args.warmup):
+        run_cpu(sample[:1], meshes)
+    tot_v, tot_s = 0, 0.0
+    for _ in range(args.steps):
+        v, s = run_cpu(sample, meshes)
+        tot_v += v
+        tot_s += s
+    value = tot_v / tot_s
+    cores = os.cpu_count()
+    desc = (f"CPU oracle (restatement of the reference's flood/seed/voxelize/erode code; "
+            f"the reference is Windows+OpenGL only) on every {args.cpu_stride}th job of "
+            f"mixed-256 ({len(sample)} jobs, {tot_v // args.steps} voxels) per step")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "voxels/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * tot_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u16", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": desc},
+            "cpu_baseline": {"value": value, "unit": "voxels/s", "cores": cores, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": value, "unit": "voxels/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _traffic():
+    """Per-launch DRAM bytes of the flood kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "roofline_traffic.json")) as fh:
+            return json.load(fh)
+    except Exception:
+        return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--jobs", type=int, default=256)
+    ap.add_argument("--plain-jobs", type=int, default=32)
+    ap.add_argument("--serve-rate", type=float, default=400.0)
+    ap.add_argument("--serve-seconds", type=float, default=3.0)
+    ap.add_argument("--cpu-stride", type=int, default=16)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        # replicas: every rank runs the whole workload on its own GPU; no collective on
+        # the data path (jobs are independent)
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    from voxelfragmentml_gb300 import build as B
+    B.build()
+    import voxelfragmentml_gb300 as V
+    from voxelfragmentml_gb300 import workloads as W
+
+    ctx = V.Context(local)
+    jobs = W.mixed(args.jobs)
+    specs = [W.to_spec(j, V, want_labels=True, ncounts=256, pinned=True) for j in jobs]
+    voxels = sum(int(np.prod(s.dims)) for s in specs)
+    h2d = sum(s.verts.nbytes + s.faces.nbytes for s in specs)
+    d2h = sum(s.labels.nbytes + s.counts.nbytes for s in specs)
+
+    # ---- value: inputs resident in HBM ------------------------------------
+    rb = V.ResidentBatch(specs, ctx)
+    for _ in range(args.warmup):
+        res = rb.execute(download=False)
+    bad = [r.status for r in res if r.status]
+    if bad:
+        raise SystemExit(f"batch failed: {bad[:4]} {V.lib().vf_last_error()}")
+    L = V.lib()
+    clocks = Clocks()
+    clocks.start()
+    if world > 1:
+        dist.barrier()
+    ctx.synchronize()
+    L.vf_ctx_event_record(ctx.h, 0)
+    launches, flood_ms, flood_bytes, visits = 0, 0.0, 0, 0
+    stage_tot = {}
+    for _ in range(args.steps):
+        rb.execute(download=False)
+        st = ctx.last_stats()
+        launches += st["launches"]
+        flood_ms += st["flood_ms"]
+        flood_bytes += st["flood_bytes"]
+        visits += st["flood_visits"]
+        for k, v in ctx.stage_ms().items():
+            stage_tot[k] = stage_tot.get(k, 0.0) + v
+    L.vf_ctx_event_record(ctx.h, 1)
+    ctx.synchronize()
+    import ctypes as C
+    msv = C.c_float()
+    L.vf_ctx_event_elapsed(ctx.h, 0, 1, C.byref(msv))
+    dev_ms = msv.value
+    if world > 1:
+        import torch
+        t = torch.tensor([dev_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_ms = float(t.item())
+    ms_per_step = dev_ms / args.steps
+    value = voxels * args.steps * world / (dev_ms / 1000.0)
+
+    # ---- e2e: host buffers, copies inside the timed region ----------------
+    for _ in range(1):
+        V.batch_run(specs, ctx)
+    ctx.synchronize()
+    L.vf_ctx_event_record(ctx.h, 2)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        res = V.batch_run(specs, ctx)
+    L.vf_ctx_event_record(ctx.h, 3)
+    ctx.synchronize()
+    wall_e2e = time.perf_counter() - t0
+    L.vf_ctx_event_elapsed(ctx.h, 2, 3, C.byref(msv))
+    e2e_ms = max(msv.value, 1e-6)
+    e2e_value = voxels * args.steps * world / (e2e_ms / 1000.0)
+    clk = clocks.stop()
+    assert all(r.status == 0 for r in res)
+
+    # ---- plain per-job path (reference-shaped) on a subset ---------------
+    plain = None
+    if args.plain_jobs > 0:
+        sub = specs[:args.plain_jobs]
+        sub_vox = sum(int(np.prod(s.dims)) for s in sub)
+        V.plain_run(sub[:2], ctx)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        pr = V.plain_run(sub, ctx)
+        ctx.synchronize()
+        pt = time.perf_counter() - t0
+        waves = [r.flood_passes for r in pr]
+        plain = {"value": sub_vox / pt, "unit": "voxels/s", "jobs": len(sub),
+                 "ms_per_job": 1000.0 * pt / len(sub), "mean_bfs_waves": float(np.mean(waves)),
+                 "batched_over_plain": e2e_value / (sub_vox / pt),
+                 "resident_batched_over_plain": value / (sub_vox / pt),
+                 "timing": "wall clock, synchronised; includes mesh upload and label download"}
+
+    # ---- serving: Poisson arrivals, continuous batching -----------------
+    serving = None
+    if not args.no_serve and args.serve_seconds > 0:
+        serving = serve(V, ctx, jobs, args.serve_rate, args.serve_seconds)
+
+    # ---- CPU baseline (oracle) on a bounded sample -----------------------
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        sample = cpu_sample(jobs, args.cpu_stride)
+        cv, cs = run_cpu(sample)
+        cpu = {"value": cv / cs, "unit": "voxels/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"CPU oracle on every {args.cpu_stride}th job of mixed-256 "
+                         f"({len(sample)} jobs, {cv} voxels, {cs:.1f} s)"}
+
+    peak, peak_kind = _peaks()
+    flood_launch_ms = flood_ms / args.steps
+    flood_launch_bytes = flood_bytes / args.steps
+    achieved = (flood_launch_bytes / 1e9) / (flood_launch_ms / 1000.0) if flood_launch_ms else 0.0
+    traffic = _traffic()
+    roof = {"kernel": "k_relax (flood brick relaxation, one cooperative launch per step)",
+            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_kind": f"{peak_kind} copy bandwidth",
+            "algorithmic_bytes_per_launch": flood_launch_bytes,
+            "bytes_rule": "4 B (u16 label read + write) per voxel of every brick visit",
+            "brick_visits_per_launch": visits / args.steps,
+            "launch_ms": flood_launch_ms,
+            "traffic": (traffic or {}).get("bytes_per_launch_scaled")}
+    line = {"metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "jobs": len(specs), "voxels_per_step": voxels,
+                       "l2": "inputs larger than L2 (label grids 2.8 GB per step)",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "path": "batched (one persistent brick-queue kernel per stage)"},
+            "e2e": {"value": e2e_value, "unit": "voxels/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms / args.steps,
+                    "wall_ms_per_step": 1000.0 * wall_e2e / args.steps},
+            "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+            "gpu_launches": launches, "plain": plain, "serving": serving,
+            "stages_ms_per_step": {k: v / args.steps for k, v in stage_tot.items()}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def serve(V, ctx, jobs, rate, seconds, pool=64, copies=4):
+    """Poisson arrivals of mixed-256 jobs at `rate` jobs/s for `seconds`."""
+    from voxelfragmentml_gb300 import workloads as W
+    base = [W.to_spec(j, V, want_labels=False, ncounts=256, pinned=True) for j in jobs[:pool]]
+    outs = {}
+    for k in range(copies):
+        for i, s in enumerate(base):
+            outs[(i, k)] = V.pinned_array(s.dims, np.uint16)
+    srv = V.Server(ctx, max_inflight=3, max_batch=32)
+    rng = np.random.default_rng(7)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * seconds * 2) + 16))
+    arrivals = arrivals[arrivals < seconds]
+    results = []
+    t0 = time.perf_counter()
+    vox = 0
+    for n, at in enumerate(arrivals):
+        now = time.perf_counter() - t0
+        if at > now:
+            time.sleep(at - now)
+        i = n % pool
+        s = base[i]
+        s.labels = outs[(i, (n // pool) % copies)]
+        s.tag = n
+        srv.submit(s)
+        vox += int(np.prod(s.dims))
+        results += srv.poll(256, 0)
+    deadline = time.perf_counter() + 120
+    while len(results) < len(arrivals) and time.perf_counter() < deadline:
+        results += srv.poll(256, 50)
+    span = time.perf_counter() - t0
+    srv.close()
+    lat = sorted(r.done_ms - r.submit_ms for r in results)
+    ok = sum(1 for r in results if r.status == 0)
+    return {"rate_jobs_per_s": rate, "seconds": seconds, "submitted": int(len(arrivals)),
+            "completed_ok": ok, "p50_ms": float(np.percentile(lat, 50)) if lat else None,
+            "p99_ms": float(np.percentile(lat, 99)) if lat else None,
+            "sustained_voxels_per_s": vox / span,
+            "note": "latency = submit to labels on host; pool of 64 distinct jobs cycled"}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -219,6 +219,12 @@ typedef struct vf_job_result {
  * kernels, labels and counts copied back to the jobs' host buffers. */
 vf_status vf_batch_run(vf_ctx* ctx, const vf_job* jobs, uint32_t njobs,
                        vf_job_result* results);
+/* Resident mode: plan the jobs and upload their inputs once; then every
+ * vf_batch_execute runs all stages on the HBM-resident inputs (download != 0
+ * also copies labels and counts back).  The job structs and their host
+ * buffers must stay valid until the next prepare or run. */
+vf_status vf_batch_prepare(vf_ctx* ctx, const vf_job* jobs, uint32_t njobs);
+vf_status vf_batch_execute(vf_ctx* ctx, int download, vf_job_result* results);
 /* Plain path: one job at a time, stage by stage, flood as one launch plus a
  * host read per BFS wave (the reference's execution shape). */
 vf_status vf_plain_run(vf_ctx* ctx, const vf_job* jobs, uint32_t njobs,
@@ -247,6 +253,11 @@ vf_status vf_ctx_event_elapsed(vf_ctx* ctx, int slot_a, int slot_b, float* ms);
 vf_status vf_ctx_last_stats(vf_ctx* ctx, uint64_t* kernel_launches,
                             float* flood_ms, uint64_t* flood_bytes,
                             uint64_t* flood_brick_visits);
+
+/* device ms of the stages of the last batched run: [0] input upload,
+ * [1] voxelize, [2] seeds, [3] fracture, [4] perturb, [5] erode/boundaries,
+ * [6] counts, [7] download (n <= 8 entries written) */
+vf_status vf_ctx_stage_ms(vf_ctx* ctx, float* ms, uint32_t n);
 
 #ifdef __cplusplus
 }

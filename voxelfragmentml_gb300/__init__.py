@@ -34,6 +34,8 @@ EUCLIDEAN, MANHATTAN, CHEBYSHEV = 0, 1, 2
 SQUARE, ELLIPSE, CROSS = 0, 1, 2
 INNER, OUTER, BOTH = 0, 1, 2
 MAX_SEEDS = 4095
+STAGES = ("upload", "voxelize", "seeds", "fracture", "perturb", "erode_boundaries", "counts",
+          "download")
 
 
 class VFError(RuntimeError):
@@ -118,6 +120,9 @@ EXPORTS = {
     "vf_job_footprint": (C.c_size_t, [C.c_void_p]),
     "vf_batch_run": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     "vf_plain_run": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "vf_batch_prepare": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "vf_batch_execute": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "vf_ctx_stage_ms": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_server_create": (C.c_int, [C.c_void_p, C.c_size_t, C.c_uint32, C.c_uint32, C.c_void_p]),
     "vf_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "vf_server_poll": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int]),
@@ -185,6 +190,12 @@ class Context:
     @property
     def bytes_in_use(self) -> int:
         return lib().vf_ctx_bytes_in_use(self.h)
+
+    def stage_ms(self):
+        """Device ms per stage of the last batched run (see STAGES)."""
+        a = (C.c_float * 8)()
+        _check(lib().vf_ctx_stage_ms(self.h, a, 8))
+        return dict(zip(STAGES, list(a)))
 
     def last_stats(self):
         la, vis, by = C.c_uint64(), C.c_uint64(), C.c_uint64()
@@ -398,6 +409,49 @@ def _run(fn, specs, ctx):
 def batch_run(specs, ctx: Context | None = None):
     """Batched path: every stage once over all jobs (vf_batch_run)."""
     return _run(lib().vf_batch_run, specs, ctx)
+
+
+class ResidentBatch:
+    """vf_batch_prepare / vf_batch_execute: inputs uploaded once, then
+    every execute() runs all stages on the HBM-resident inputs."""
+
+    def __init__(self, specs, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.specs = list(specs)
+        self._jobs = (Job * len(self.specs))(*[s.job() for s in self.specs])
+        _check(lib().vf_batch_prepare(self.ctx.h, self._jobs, len(self.specs)))
+
+    def execute(self, download: bool = False):
+        res = (JobResult * len(self.specs))()
+        st = lib().vf_batch_execute(self.ctx.h, 1 if download else 0, res)
+        if st != OK and all(r.status == OK for r in res):
+            _check(st)
+        return list(res)
+
+
+def pinned_array(shape, dtype):
+    """A numpy array in page-locked host memory (vf_host_alloc); freed when
+    the array is garbage collected."""
+    dt = np.dtype(dtype)
+    count = int(np.prod(shape))
+    n = max(count * dt.itemsize, 1)
+    p = lib().vf_host_alloc(n)
+    if not p:
+        raise VFError(ERR_OOM, "pinned host allocation failed")
+    buf = (C.c_ubyte * n).from_address(p)
+    buf._owner = _PinnedOwner(p)  # lives as long as the buffer
+    return np.frombuffer(buf, dtype=dt, count=count).reshape(shape)
+
+
+class _PinnedOwner:
+    def __init__(self, p):
+        self.p = p
+
+    def __del__(self):
+        try:
+            lib().vf_host_free(self.p)
+        except Exception:
+            pass
 
 
 def plain_run(specs, ctx: Context | None = None):

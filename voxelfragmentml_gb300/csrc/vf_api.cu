@@ -492,6 +492,7 @@ vf_status vf_batch_run(vf_ctx* ctx, const vf_job* jobs, uint32_t njobs, vf_job_r
   if (njobs == 0) return VF_OK;
   cudaSetDevice(ctx->c.device);
   vfr::Batch& B = ctx->c.batch;
+  ctx->c.resident = false;
   std::vector<const vf_job*> ptrs(njobs);
   for (uint32_t i = 0; i < njobs; ++i) ptrs[i] = jobs + i;
   B.stages = vfr::ST_ALL;
@@ -503,10 +504,45 @@ vf_status vf_batch_run(vf_ctx* ctx, const vf_job* jobs, uint32_t njobs, vf_job_r
   return B.finish(results);
 }
 
+vf_status vf_batch_prepare(vf_ctx* ctx, const vf_job* jobs, uint32_t njobs) {
+  if (!ctx || (njobs && !jobs)) return fail(VF_ERR_INVALID, "NULL argument");
+  cudaSetDevice(ctx->c.device);
+  vfr::Batch& B = ctx->c.batch;
+  ctx->c.resident = false;
+  std::vector<const vf_job*> ptrs(njobs);
+  for (uint32_t i = 0; i < njobs; ++i) ptrs[i] = jobs + i;
+  B.stages = vfr::ST_ALL;
+  B.given.clear();
+  vf_status s = B.plan(ptrs.data(), njobs);
+  if (s) return s;
+  s = B.upload_inputs();
+  if (s) return s;
+  VF_CK(cudaStreamSynchronize(B.stream));
+  ctx->c.resident = true;
+  return VF_OK;
+}
+
+vf_status vf_batch_execute(vf_ctx* ctx, int download, vf_job_result* results) {
+  if (!ctx) return fail(VF_ERR_INVALID, "ctx is NULL");
+  if (!ctx->c.resident) return fail(VF_ERR_INVALID, "no prepared batch (call vf_batch_prepare)");
+  cudaSetDevice(ctx->c.device);
+  vfr::Batch& B = ctx->c.batch;
+  vf_status s = B.enqueue_batched(false, download != 0);
+  if (s) return s;
+  return B.finish(results);
+}
+
+vf_status vf_ctx_stage_ms(vf_ctx* ctx, float* ms, uint32_t n) {
+  if (!ctx || (n && !ms)) return fail(VF_ERR_INVALID, "NULL argument");
+  for (uint32_t i = 0; i < n && i < 8; ++i) ms[i] = ctx->c.last_stage_ms[i];
+  return VF_OK;
+}
+
 vf_status vf_plain_run(vf_ctx* ctx, const vf_job* jobs, uint32_t njobs, vf_job_result* results) {
   if (!ctx || (njobs && !jobs)) return fail(VF_ERR_INVALID, "NULL argument");
   cudaSetDevice(ctx->c.device);
   vfr::Batch& B = ctx->c.batch;
+  ctx->c.resident = false;
   vf_status first = VF_OK;
   uint64_t launches = 0;
   for (uint32_t i = 0; i < njobs; ++i) {

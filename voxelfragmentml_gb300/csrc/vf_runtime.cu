@@ -73,6 +73,7 @@ vf_status Batch::init(Ctx* c, bool own) {
   VF_CK(cudaEventCreate(&ev_flood0));
   VF_CK(cudaEventCreate(&ev_flood1));
   VF_CK(cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming));
+  for (int i = 0; i < NSTAGE_EV; ++i) VF_CK(cudaEventCreate(&ev_stage[i]));
   VF_CK(cudaMallocHost(&h_scal, 64 * sizeof(uint32_t)));
   return VF_OK;
 }
@@ -92,6 +93,8 @@ void Batch::release() {
   if (ev_flood0) cudaEventDestroy(ev_flood0);
   if (ev_flood1) cudaEventDestroy(ev_flood1);
   if (ev_done) cudaEventDestroy(ev_done);
+  for (int i = 0; i < NSTAGE_EV; ++i)
+    if (ev_stage[i]) cudaEventDestroy(ev_stage[i]);
   ev_flood0 = ev_flood1 = ev_done = nullptr;
   if (own_stream && stream) cudaStreamDestroy(stream);
   stream = nullptr;
@@ -402,7 +405,8 @@ __global__ void k_brick_job(const JobDesc* jobs, uint32_t* brick_job) {
 }
 }  // namespace
 
-static vf_status upload_common(Batch& B) {
+// inputs: meshes, given seeds, stage tables, erosion masks (host -> device)
+static vf_status upload_inputs_impl(Batch& B) {
   const uint32_t n = (uint32_t)B.jobs.size();
   cudaStream_t st = B.stream;
   for (uint32_t i = 0; i < n && (B.stages & ST_VOX); ++i) {
@@ -424,8 +428,17 @@ static vf_status upload_common(Batch& B) {
   if (B.sz.emask)
     VF_CK(cudaMemcpyAsync(B.emask.p, static_cast<char*>(B.h_tables) + tb, B.sz.emask * 4,
                           cudaMemcpyHostToDevice, st));
+  return VF_OK;
+}
+
+vf_status Batch::upload_inputs() { return upload_inputs_impl(*this); }
+
+// per-run scratch: job states, bit planes, counts, flood words, brick map
+static vf_status reset_scratch(Batch& B) {
+  const uint32_t n = (uint32_t)B.jobs.size();
+  cudaStream_t st = B.stream;
   VF_CK(cudaMemsetAsync(B.state.p, 0, sizeof(JobState) * n, st));
-  VF_CK(cudaMemsetAsync(B.par.p, 0, B.sz.par * 8, st));
+  if (B.stages & ST_VOX) VF_CK(cudaMemsetAsync(B.par.p, 0, B.sz.par * 8, st));
   VF_CK(cudaMemsetAsync(B.counts.p, 0, B.sz.counts * 4, st));
   VF_CK(cudaMemsetAsync(B.scal.p, 0, 4096, st));
   uint32_t maxb = 1;
@@ -434,6 +447,12 @@ static vf_status upload_common(Batch& B) {
       B.dtable(T_VOX), static_cast<uint32_t*>(B.brick_job.p));
   B.launches += 1;
   return VF_OK;
+}
+
+static vf_status upload_common(Batch& B) {
+  vf_status s = upload_inputs_impl(B);
+  if (s) return s;
+  return reset_scratch(B);
 }
 
 static void voxelize_stages(Batch& B) {
@@ -467,12 +486,20 @@ static vfk::FloodScratch flood_scratch(Batch& B) {
   return fs;
 }
 
-vf_status Batch::enqueue_batched() {
+vf_status Batch::enqueue_batched(bool do_upload, bool do_download) {
   const uint32_t n = (uint32_t)jobs.size();
   cudaStream_t st = stream;
   launches = 0;
   flood_timed = false;
-  vf_status s = upload_common(*this);
+  for (int i = 0; i < NSTAGE_EV; ++i) stage_rec[i] = false;
+  auto mark = [&](int i) {
+    if (cudaEventRecord(ev_stage[i], st) == cudaSuccess) stage_rec[i] = true;
+  };
+  mark(0);
+  vf_status s = do_upload ? upload_inputs_impl(*this) : VF_OK;
+  if (s) return s;
+  mark(1);
+  s = reset_scratch(*this);
   if (s) return s;
   JobState* ds = static_cast<JobState*>(state.p);
   const uint32_t* bj = static_cast<uint32_t*>(brick_job.p);
@@ -488,10 +515,12 @@ vf_status Batch::enqueue_batched() {
     vfk::compact_live(st, lv, sz.bricks, lst, lc);
     launches += 2;
   }
+  mark(2);
   if (stages & (ST_SEED | ST_FRACTURE)) {
     vfk::sample_seeds(st, dtable(T_SEED), ds, n);
     launches += 1;
   }
+  mark(3);
   bool any_flood = false, any_naive = false, any_pert = false, any_erode = false,
        any_det1 = false, any_det3 = false, any_prefix = false;
   for (uint32_t i = 0; i < n; ++i) {
@@ -543,11 +572,13 @@ vf_status Batch::enqueue_batched() {
     }
   }
   if (any_naive) { vfk::naive(st, dtable(T_NAIVE), ds, lst, lc, maxc, bj); launches += 1; }
+  mark(4);
   if (any_pert) {
     vfk::lattice(st, dtable(T_PERT), n);
     vfk::perturb(st, dtable(T_PERT), lst, lc, maxc, bj);
     launches += 2;
   }
+  mark(5);
   for (uint32_t it = 0; it < erode_iters; ++it) {
     vfk::detect_boundaries(st, dtable(t_edet(it)), lst, lc, maxc, bj);
     vfk::erode(st, dtable(t_ero(it)), lst, lc, maxc, bj);
@@ -556,13 +587,15 @@ vf_status Batch::enqueue_batched() {
   if (any_erode) { vfk::remove_isolated(st, dtable(T_ISO), lst, lc, maxc, bj); launches += 1; }
   if (any_det1) { vfk::detect_boundaries(st, dtable(T_DET1), lst, lc, maxc, bj); launches += 1; }
   if (any_det3) { vfk::detect_boundaries_wide(st, dtable(T_DET3), lst, lc, maxc, bj); launches += 1; }
+  mark(6);
   if (stages & ST_COUNT) {
     vfk::count_values(st, dtable(T_CNT), ds, lst, lc, maxc, bj);
     launches += 1;
   }
+  mark(7);
   VF_CK(cudaGetLastError());
   // downloads
-  for (uint32_t i = 0; i < n && (stages & ST_DOWNLOAD); ++i) {
+  for (uint32_t i = 0; i < n && (stages & ST_DOWNLOAD) && do_download; ++i) {
     const vf_job& j = *jobs[i];
     const JobPlan& p = plans[i];
     const uint16_t* src = static_cast<uint16_t*>(p.final_cur ? grid1.p : grid0.p) + p.o_grid;
@@ -575,6 +608,7 @@ vf_status Batch::enqueue_batched() {
   }
   VF_CK(cudaMemcpyAsync(h_state, ds, sizeof(JobState) * n, cudaMemcpyDeviceToHost, st));
   VF_CK(cudaMemcpyAsync(h_scal, scal.p, 64 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  mark(8);
   VF_CK(cudaEventRecord(ev_done, st));
   return VF_OK;
 }
@@ -625,6 +659,14 @@ vf_status Batch::finish(vf_job_result* res) {
     ctx->last_flood_passes = 0;
   }
   ctx->last_launches = launches;
+  for (int i = 0; i < 8; ++i) {
+    float ms = 0.f;
+    if (stage_rec[i] && stage_rec[i + 1] &&
+        cudaEventElapsedTime(&ms, ev_stage[i], ev_stage[i + 1]) == cudaSuccess)
+      ctx->last_stage_ms[i] = ms;
+    else
+      ctx->last_stage_ms[i] = 0.f;
+  }
   return first;
 }
 
@@ -634,6 +676,7 @@ vf_status Batch::enqueue_plain_and_wait(vf_job_result* res, bool skip_vox) {
   cudaStream_t st = stream;
   launches = 0;
   flood_timed = false;
+  for (int i = 0; i < NSTAGE_EV; ++i) stage_rec[i] = false;
   const vf_job& j = *jobs[0];
   const JobPlan& p = plans[0];
   const uint64_t N = (uint64_t)p.X * p.Y * p.Z;
@@ -660,8 +703,12 @@ vf_status Batch::enqueue_plain_and_wait(vf_job_result* res, bool skip_vox) {
     launches += 2;
     for (int pass = 0; pass < 2; ++pass) {
       VF_CK(cudaMemcpyAsync(h_scal + 8, cnt, 4, cudaMemcpyDeviceToHost, st));
+      VF_CK(cudaMemcpyAsync(h_state, ds, sizeof(JobState), cudaMemcpyDeviceToHost, st));
       VF_CK(cudaStreamSynchronize(st));
       uint32_t ncur = h_scal[8];
+      // while (numDisjointVoxels != 0) (FloodFracturer.cpp:135): no
+      // re-flood when the cleanup reset nothing
+      if (pass == 1 && h_state[0].disjoint == 0) ncur = 0;
       while (ncur > 0) {  // FloodFracturer.cpp:143-158
         VF_CK(cudaMemsetAsync(cnt, 0, 4, st));
         vfk::plain_wave(st, tf, ds, hj, f0, ncur, f1, cnt);

@@ -63,6 +63,11 @@ struct Batch {
   size_t h_state_cap = 0;
   uint32_t* h_scal = nullptr;   // pinned: [0..3] flood stats, [4] err, [8] fcount
   cudaEvent_t ev_flood0 = nullptr, ev_flood1 = nullptr, ev_done = nullptr;
+  // stage boundaries: 0 start, 1 inputs uploaded, 2 voxelized, 3 seeded,
+  // 4 fractured, 5 perturbed, 6 eroded/boundaries, 7 counted, 8 downloaded
+  static constexpr int NSTAGE_EV = 9;
+  cudaEvent_t ev_stage[NSTAGE_EV] = {};
+  bool stage_rec[NSTAGE_EV] = {};
   std::vector<JobPlan> plans;
   std::vector<const vf_job*> jobs;
   Sizes sz;
@@ -79,7 +84,8 @@ struct Batch {
   vf_status init(Ctx* c, bool own);
   void release();
   vf_status plan(const vf_job* const* js, uint32_t n);
-  vf_status enqueue_batched();
+  vf_status enqueue_batched(bool upload_inputs = true, bool download = true);
+  vf_status upload_inputs();
   vf_status enqueue_plain_and_wait(vf_job_result* res, bool skip_vox);
   vf_status finish(vf_job_result* res);
   size_t table_off(uint32_t t) const;
@@ -97,6 +103,8 @@ struct Ctx {
   // stats of the last batch
   uint64_t last_launches = 0;
   float last_flood_ms = 0.f;
+  float last_stage_ms[8] = {};
+  bool resident = false;  // batch inputs uploaded by vf_batch_prepare
   uint64_t last_flood_visits = 0;
   uint64_t last_flood_passes = 0;
   vf_status alloc(DevBuf& b, size_t bytes);
