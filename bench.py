@@ -234,7 +234,7 @@ def main():
         dist.barrier()
     ctx.synchronize()
     L.vf_ctx_event_record(ctx.h, 0)
-    launches, flood_ms, flood_bytes, visits = 0, 0.0, 0, 0
+    launches, flood_ms, flood_bytes, visits, passes, sweeps, maxit = 0, 0.0, 0, 0, 0, 0, 0
     stage_tot = {}
     for _ in range(args.steps):
         rb.execute(download=False)
@@ -243,6 +243,9 @@ def main():
         flood_ms += st["flood_ms"]
         flood_bytes += st["flood_bytes"]
         visits += st["flood_visits"]
+        passes += st["flood_passes"]
+        sweeps += st["flood_sweeps"]
+        maxit += st["flood_maxit_hits"]
         for k, v in ctx.stage_ms().items():
             stage_tot[k] = stage_tot.get(k, 0.0) + v
     L.vf_ctx_event_record(ctx.h, 1)
@@ -319,6 +322,9 @@ def main():
             "algorithmic_bytes_per_launch": flood_launch_bytes,
             "bytes_rule": "4 B (u16 label read + write) per voxel of every brick visit",
             "brick_visits_per_launch": visits / args.steps,
+            "passes_per_launch": passes / args.steps,
+            "sweeps_per_visit": sweeps / max(visits, 1),
+            "visits_at_sweep_cap": maxit / args.steps,
             "launch_ms": flood_launch_ms,
             "traffic": (traffic or {}).get("bytes_per_launch_scaled")}
     line = {"metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world,

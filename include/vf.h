@@ -255,9 +255,14 @@ vf_status vf_ctx_last_stats(vf_ctx* ctx, uint64_t* kernel_launches,
                             uint64_t* flood_brick_visits);
 
 /* device ms of the stages of the last batched run: [0] input upload,
- * [1] voxelize, [2] seeds, [3] fracture, [4] perturb, [5] erode/boundaries,
- * [6] counts, [7] download (n <= 8 entries written) */
+ * [1] tetrahedra, [2] parity raster, [3] shell SAT, [4] combine + live
+ * bricks, [5] seeds, [6] fracture, [7] perturb, [8] erode/boundaries,
+ * [9] counts, [10] download (n <= 11 entries written) */
 vf_status vf_ctx_stage_ms(vf_ctx* ctx, float* ms, uint32_t n);
+/* flood relaxation of the last batched run: passes (grid-wide rounds),
+ * brick sweeps summed over all visits, visits that hit the sweep cap */
+vf_status vf_ctx_flood_stats(vf_ctx* ctx, uint64_t* passes, uint64_t* sweeps,
+                             uint64_t* maxit_hits);
 
 #ifdef __cplusplus
 }

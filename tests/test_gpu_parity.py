@@ -38,7 +38,8 @@ def _oracle(oracle_lib):
 
 # (angular, profile, mesh seed, max_dim): includes Z % 8 == 4 and dims that
 # are not multiples of the 16x16x32 brick
-VOX_CASES = [(32, 24, 1, 32), (48, 36, 2, 60), (64, 48, 3, 76), (96, 72, 4, 100), (40, 30, 5, 44)]
+VOX_CASES = [(32, 24, 1, 32), (48, 36, 2, 60), (64, 48, 3, 76), (96, 72, 4, 100), (40, 30, 5, 44),
+             (12, 9, 6, 128), (24, 18, 7, 200), (200, 150, 8, 64)]  # coarse/fine meshes
 
 
 def _mesh(A, P, ms, md):

@@ -34,8 +34,8 @@ EUCLIDEAN, MANHATTAN, CHEBYSHEV = 0, 1, 2
 SQUARE, ELLIPSE, CROSS = 0, 1, 2
 INNER, OUTER, BOTH = 0, 1, 2
 MAX_SEEDS = 4095
-STAGES = ("upload", "voxelize", "seeds", "fracture", "perturb", "erode_boundaries", "counts",
-          "download")
+STAGES = ("upload", "tetrahedra", "parity", "shell", "combine", "seeds", "fracture", "perturb",
+          "erode_boundaries", "counts", "download")
 
 
 class VFError(RuntimeError):
@@ -123,6 +123,7 @@ EXPORTS = {
     "vf_batch_prepare": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_batch_execute": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "vf_ctx_stage_ms": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "vf_ctx_flood_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "vf_server_create": (C.c_int, [C.c_void_p, C.c_size_t, C.c_uint32, C.c_uint32, C.c_void_p]),
     "vf_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "vf_server_poll": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int]),
@@ -193,16 +194,19 @@ class Context:
 
     def stage_ms(self):
         """Device ms per stage of the last batched run (see STAGES)."""
-        a = (C.c_float * 8)()
-        _check(lib().vf_ctx_stage_ms(self.h, a, 8))
+        a = (C.c_float * 11)()
+        _check(lib().vf_ctx_stage_ms(self.h, a, 11))
         return dict(zip(STAGES, list(a)))
 
     def last_stats(self):
         la, vis, by = C.c_uint64(), C.c_uint64(), C.c_uint64()
         ms = C.c_float()
         _check(lib().vf_ctx_last_stats(self.h, C.byref(la), C.byref(ms), C.byref(by), C.byref(vis)))
+        pa, sw, mh = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        _check(lib().vf_ctx_flood_stats(self.h, C.byref(pa), C.byref(sw), C.byref(mh)))
         return {"launches": la.value, "flood_ms": ms.value, "flood_bytes": by.value,
-                "flood_visits": vis.value}
+                "flood_visits": vis.value, "flood_passes": pa.value, "flood_sweeps": sw.value,
+                "flood_maxit_hits": mh.value}
 
 
 _default_ctx = None

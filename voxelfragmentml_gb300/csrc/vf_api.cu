@@ -532,9 +532,17 @@ vf_status vf_batch_execute(vf_ctx* ctx, int download, vf_job_result* results) {
   return B.finish(results);
 }
 
+vf_status vf_ctx_flood_stats(vf_ctx* ctx, uint64_t* passes, uint64_t* sweeps, uint64_t* maxit_hits) {
+  if (!ctx) return fail(VF_ERR_INVALID, "ctx is NULL");
+  if (passes) *passes = ctx->c.last_flood_passes;
+  if (sweeps) *sweeps = ctx->c.last_flood_sweeps;
+  if (maxit_hits) *maxit_hits = ctx->c.last_flood_maxit;
+  return VF_OK;
+}
+
 vf_status vf_ctx_stage_ms(vf_ctx* ctx, float* ms, uint32_t n) {
   if (!ctx || (n && !ms)) return fail(VF_ERR_INVALID, "NULL argument");
-  for (uint32_t i = 0; i < n && i < 8; ++i) ms[i] = ctx->c.last_stage_ms[i];
+  for (uint32_t i = 0; i < n && i < 11; ++i) ms[i] = ctx->c.last_stage_ms[i];
   return VF_OK;
 }
 

@@ -13,7 +13,9 @@
 //   key(v) <- max(key(v), max_{u in N(v)} key(u) - 4096)
 //
 // Bricks of 16x16x32 voxels are relaxed to local convergence in shared
-// memory (many BFS waves per visit), and a brick whose face voxels changed
+// memory (many BFS waves per visit: each sweep recomputes only the rows next
+// to a change and runs forward/backward along the 32-voxel z rows), and a
+// brick whose face voxels changed
 // puts its neighbours on the next pass's queue (deduplicated by a pass
 // epoch, appended with warp ballot/popc).  All passes of all jobs of a batch
 // run in ONE cooperative persistent kernel; passes are separated by a
@@ -112,7 +114,7 @@ __device__ __forceinline__ void enqueue(const FloodArgs& a, uint32_t b, uint32_t
 template <int CONN>
 __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, uint32_t b,
                             uint32_t pass, uint32_t* tile, uint32_t* live27, uint32_t* dirs,
-                            int* reenq) {
+                            int* reenq, uint8_t* rflag) {
   const uint32_t lb = b - J.brick_base;
   const int bz = lb % J.nbz, by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
   const int x0 = bx * VF_BX, y0 = by * VF_BY, z0 = bz * VF_BZ;
@@ -152,65 +154,102 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     k[4 * q] = w.x; k[4 * q + 1] = w.y; k[4 * q + 2] = w.z; k[4 * q + 3] = w.w;
   }
   uint32_t changed = 0, overflow = 0;
-  int it = 0;
+  // rflag[b][row]: the row changed in the previous sweep.  Every interior row
+  // runs in sweep 0 (new halo data); later only rows next to a change run.
+  for (int q = t; q < KROWS; q += blockDim.x) {
+    const int lx = q / KNY, ly = q % KNY;
+    const bool interior = lx >= 1 && lx <= VF_BX && ly >= 1 && ly <= VF_BY;
+    rflag[q] = interior ? 1 : 0;
+    rflag[KROWS + q] = 0;
+  }
+  __syncthreads();
+  const int own = (tx + 1) * KNY + (ty + 1);
+  int it = 0, cur = 0;
   for (; it < MAXIT; ++it) {
-    uint32_t c[VF_BZ + 2];
-#pragma unroll
-    for (int j = 0; j < VF_BZ + 2; ++j) c[j] = 0;
+    const uint8_t* pf = rflag + cur * KROWS;
+    bool active;
     if (CONN == 26) {
+      active = false;
 #pragma unroll
-      for (int r = 0; r < 9; ++r) {
-        const uint32_t* rp = tile + ((tx + r / 3) * KNY + (ty + r % 3)) * KP;
-        c[0] = max(c[0], rp[3]);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const uint4 w = *reinterpret_cast<const uint4*>(rp + 4 + 4 * q);
-          c[1 + 4 * q] = max(c[1 + 4 * q], w.x);
-          c[2 + 4 * q] = max(c[2 + 4 * q], w.y);
-          c[3 + 4 * q] = max(c[3 + 4 * q], w.z);
-          c[4 + 4 * q] = max(c[4 + 4 * q], w.w);
-        }
-        c[VF_BZ + 1] = max(c[VF_BZ + 1], rp[4 + VF_BZ]);
-      }
+      for (int r = 0; r < 9; ++r) active |= pf[(tx + r / 3) * KNY + (ty + r % 3)] != 0;
     } else {
-      const int rs[4][2] = {{0, 1}, {2, 1}, {1, 0}, {1, 2}};
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        const uint32_t* rp = tile + ((tx + rs[r][0]) * KNY + (ty + rs[r][1])) * KP;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const uint4 w = *reinterpret_cast<const uint4*>(rp + 4 + 4 * q);
-          c[1 + 4 * q] = max(c[1 + 4 * q], w.x);
-          c[2 + 4 * q] = max(c[2 + 4 * q], w.y);
-          c[3 + 4 * q] = max(c[3 + 4 * q], w.z);
-          c[4 + 4 * q] = max(c[4 + 4 * q], w.w);
-        }
-      }
+      active = pf[own] | pf[own - KNY] | pf[own + KNY] | pf[own - 1] | pf[own + 1];
     }
-    const uint32_t zlo = own_row[3], zhi = own_row[4 + VF_BZ];
     uint32_t chg = 0;
+    if (active) {
+      uint32_t c[VF_BZ + 2];
 #pragma unroll
-    for (int z = 0; z < VF_BZ; ++z) {
-      uint32_t m;
+      for (int jz = 0; jz < VF_BZ + 2; ++jz) c[jz] = 0;
       if (CONN == 26) {
-        m = max(c[z], max(c[z + 1], c[z + 2]));
-      } else {
-        const uint32_t lo = z == 0 ? zlo : k[z - 1];
-        const uint32_t hi = z == VF_BZ - 1 ? zhi : k[z + 1];
-        m = max(c[z + 1], max(lo, hi));
-      }
-      const uint32_t cand = m >= 2u * VF_KEY_STEP ? m - VF_KEY_STEP : 0u;
-      const uint32_t kk = k[z];
-      if (kk == VF_KEY_UNREACHED && m >= VF_KEY_MIN_REACHED && m < 2u * VF_KEY_STEP) overflow = 1;
-      const uint32_t nk = kk ? max(kk, cand) : 0u;
-      if (nk != kk) { k[z] = nk; chg |= 1u << z; }
-    }
-    if (chg) {
 #pragma unroll
-      for (int z = 0; z < VF_BZ; ++z)
-        if (chg & (1u << z)) own_row[4 + z] = k[z];
+        for (int r = 0; r < 9; ++r) {
+          const uint32_t* rp = tile + ((tx + r / 3) * KNY + (ty + r % 3)) * KP;
+          c[0] = max(c[0], rp[3]);
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const uint4 w = *reinterpret_cast<const uint4*>(rp + 4 + 4 * q);
+            c[1 + 4 * q] = max(c[1 + 4 * q], w.x);
+            c[2 + 4 * q] = max(c[2 + 4 * q], w.y);
+            c[3 + 4 * q] = max(c[3 + 4 * q], w.z);
+            c[4 + 4 * q] = max(c[4 + 4 * q], w.w);
+          }
+          c[VF_BZ + 1] = max(c[VF_BZ + 1], rp[4 + VF_BZ]);
+        }
+      } else {
+        const int rs[4][2] = {{0, 1}, {2, 1}, {1, 0}, {1, 2}};
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const uint32_t* rp = tile + ((tx + rs[r][0]) * KNY + (ty + rs[r][1])) * KP;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const uint4 w = *reinterpret_cast<const uint4*>(rp + 4 + 4 * q);
+            c[1 + 4 * q] = max(c[1 + 4 * q], w.x);
+            c[2 + 4 * q] = max(c[2 + 4 * q], w.y);
+            c[3 + 4 * q] = max(c[3 + 4 * q], w.z);
+            c[4 + 4 * q] = max(c[4 + 4 * q], w.w);
+          }
+        }
+        c[0] = own_row[3];              // z - 1 halo of the own row
+        c[VF_BZ + 1] = own_row[4 + VF_BZ];
+      }
+      // cross-row candidates (26: the 3x3x3 block; 6: the 4 side rows)
+#pragma unroll
+      for (int z = 0; z < VF_BZ; ++z) {
+        const uint32_t m = CONN == 26 ? max(c[z], max(c[z + 1], c[z + 2])) : c[z + 1];
+        const uint32_t kk = k[z];
+        if (kk == VF_KEY_UNREACHED && m >= VF_KEY_MIN_REACHED && m < 2u * VF_KEY_STEP) overflow = 1;
+        const uint32_t nk = kk ? max(kk, m >= 2u * VF_KEY_STEP ? m - VF_KEY_STEP : 0u) : 0u;
+        if (nk != kk) { k[z] = nk; chg |= 1u << z; }
+      }
+      // in-row sweeps along z, from the z halo: a front along z crosses the
+      // whole row in one sweep
+      uint32_t prev = c[0];
+#pragma unroll
+      for (int z = 0; z < VF_BZ; ++z) {
+        const uint32_t kk = k[z];
+        if (kk == VF_KEY_UNREACHED && prev >= VF_KEY_MIN_REACHED && prev < 2u * VF_KEY_STEP) overflow = 1;
+        const uint32_t nk = kk ? max(kk, prev >= 2u * VF_KEY_STEP ? prev - VF_KEY_STEP : 0u) : 0u;
+        if (nk != kk) { k[z] = nk; chg |= 1u << z; }
+        prev = nk;
+      }
+      prev = c[VF_BZ + 1];
+#pragma unroll
+      for (int z = VF_BZ - 1; z >= 0; --z) {
+        const uint32_t kk = k[z];
+        if (kk == VF_KEY_UNREACHED && prev >= VF_KEY_MIN_REACHED && prev < 2u * VF_KEY_STEP) overflow = 1;
+        const uint32_t nk = kk ? max(kk, prev >= 2u * VF_KEY_STEP ? prev - VF_KEY_STEP : 0u) : 0u;
+        if (nk != kk) { k[z] = nk; chg |= 1u << z; }
+        prev = nk;
+      }
+      if (chg) {
+#pragma unroll
+        for (int z = 0; z < VF_BZ; ++z)
+          if (chg & (1u << z)) own_row[4 + z] = k[z];
+      }
     }
+    rflag[(cur ^ 1) * KROWS + own] = chg != 0;
     changed |= chg;
+    cur ^= 1;
     if (!__syncthreads_or(chg != 0)) break;
   }
   const int x = x0 + tx, y = y0 + ty;
@@ -249,7 +288,11 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     dm &= ~(1u << 13);  // self
     if (dm) atomicOr(dirs, dm);
   }
-  if (t == 0 && it == MAXIT) *reenq = 1;
+  if (t == 0) {
+    if (it == MAXIT) *reenq = 1;
+    atomicAdd(a.stats + 4, (uint32_t)it + 1u);  // sweeps (statistics)
+    if (it == MAXIT) atomicAdd(a.stats + 5, 1u);
+  }
   __syncthreads();
   if (t < 32) {
     const uint32_t dm = *dirs;
@@ -271,6 +314,7 @@ __global__ void __launch_bounds__(256, 2) k_relax(FloodArgs a) {
   __shared__ uint32_t dirs;
   __shared__ int reenq;
   __shared__ uint32_t item;
+  __shared__ uint8_t rflag[2 * KROWS];
   for (uint32_t p = 0; p < a.max_passes; ++p) {
     const uint32_t cur = p % 3u;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -288,8 +332,8 @@ __global__ void __launch_bounds__(256, 2) k_relax(FloodArgs a) {
       const uint32_t b = a.queue[cur][i];
       const uint32_t jid = a.brick_job[b];
       const JobDesc& J = a.jobs[jid];
-      if (J.distance == 1) relax_brick<6>(a, J, jid, b, p, tile, live27, &dirs, &reenq);
-      else relax_brick<26>(a, J, jid, b, p, tile, live27, &dirs, &reenq);
+      if (J.distance == 1) relax_brick<6>(a, J, jid, b, p, tile, live27, &dirs, &reenq, rflag);
+      else relax_brick<26>(a, J, jid, b, p, tile, live27, &dirs, &reenq, rflag);
       if (threadIdx.x == 0) atomicMax(&a.st[jid].passes, p + 1);
       ++visits;
     }

@@ -9,11 +9,22 @@
 namespace vfk {
 
 // ---- voxelizer (Tetravoxelizer + tri-box SAT) ----
+// flattened (tetrahedron, slice) work list: per-face pair counts and their
+// exclusive prefix sums over the faces of all jobs
+struct FaceScratch {
+  uint32_t* pcnt;                // [total_faces]
+  unsigned long long* pbase;     // [total_faces]
+  unsigned long long* psums;     // [ceil(total_faces / 1024)]
+  unsigned long long* ptotal;    // [1]
+};
 void centroid_and_slices(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs);
 void tetra_prep(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs,
-                uint32_t total_faces);
-void parity_raster(cudaStream_t st, const JobDesc* dj, int njobs, uint32_t total_faces);
-void shell_sat(cudaStream_t st, const JobDesc* dj, int njobs, uint32_t total_faces);
+                uint32_t total_faces, const FaceScratch& fs);
+void parity_raster(cudaStream_t st, const JobDesc* dj, int njobs, uint32_t total_faces,
+                   const FaceScratch& fs, int num_sms);
+// reuses the face scratch after the parity raster (counts, scan, runs)
+void shell_sat(cudaStream_t st, const JobDesc* dj, int njobs, uint32_t total_faces,
+               const FaceScratch& fs, int num_sms);
 // writes 0/1 labels (grid, and grid2 when dual) for every brick of every
 // job and sets live[b]
 void combine(cudaStream_t st, const JobDesc* dj, const uint32_t* brick_job,

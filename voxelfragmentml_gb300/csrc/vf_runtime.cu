@@ -12,6 +12,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <functional>
 
 #include "vf_runtime.h"
 
@@ -82,7 +83,8 @@ void Batch::release() {
   if (!ctx) return;
   for (DevBuf* b : {&grid0, &grid1, &keys, &par, &tets, &range, &ys, &seeds, &counts, &lat,
                     &verts, &faces, &emask, &tables, &state, &brick_job, &live, &list, &lcount,
-                    &q[0], &q[1], &q[2], &scal, &epoch, &front[0], &front[1]})
+                    &q[0], &q[1], &q[2], &scal, &epoch, &front[0], &front[1], &pcnt, &pbase,
+                    &psums})
     ctx->free_buf(*b);
   if (h_tables) cudaFreeHost(h_tables);
   if (h_state) cudaFreeHost(h_state);
@@ -296,6 +298,10 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
   for (int i = 0; i < 3; ++i) ALLOC(q[i], nb * 4);
   ALLOC(epoch, nb * 4);
   ALLOC(scal, 4096);
+  const size_t nf = std::max<uint32_t>(sz.faces_total, 1);
+  ALLOC(pcnt, nf * 4);
+  ALLOC(pbase, nf * 8);
+  ALLOC(psums, ((nf + 1023) / 1024 + 1) * 8);
 #undef ALLOC
   const size_t tbytes = sizeof(JobDesc) * ntables * std::max<size_t>(n, 1) + sz.emask * 4 + 256;
   if (tbytes > h_tables_cap) {
@@ -455,20 +461,28 @@ static vf_status upload_common(Batch& B) {
   return reset_scratch(B);
 }
 
-static void voxelize_stages(Batch& B) {
+static void voxelize_stages(Batch& B, const std::function<void(int)>& mark) {
   const uint32_t n = (uint32_t)B.jobs.size();
   cudaStream_t st = B.stream;
   const JobDesc* tv = B.dtable(T_VOX);
   JobState* ds = static_cast<JobState*>(B.state.p);
+  vfk::FaceScratch fsc;
+  fsc.pcnt = static_cast<uint32_t*>(B.pcnt.p);
+  fsc.pbase = static_cast<unsigned long long*>(B.pbase.p);
+  fsc.psums = static_cast<unsigned long long*>(B.psums.p);
+  fsc.ptotal = static_cast<unsigned long long*>(B.scal.p) + 256;  // bytes 2048..2055
   vfk::centroid_and_slices(st, tv, ds, n);
-  vfk::tetra_prep(st, tv, ds, n, B.sz.faces_total);
-  vfk::parity_raster(st, tv, n, B.sz.faces_total);
-  vfk::shell_sat(st, tv, n, B.sz.faces_total);
+  vfk::tetra_prep(st, tv, ds, n, B.sz.faces_total, fsc);
+  mark(2);
+  vfk::parity_raster(st, tv, n, B.sz.faces_total, fsc, B.ctx->num_sms);
+  mark(3);
+  vfk::shell_sat(st, tv, n, B.sz.faces_total, fsc, B.ctx->num_sms);
+  mark(4);
   vfk::combine(st, tv, static_cast<uint32_t*>(B.brick_job.p), B.sz.bricks,
                static_cast<uint8_t*>(B.live.p), 1);
   vfk::compact_live(st, static_cast<uint8_t*>(B.live.p), B.sz.bricks,
                     static_cast<uint32_t*>(B.list.p), static_cast<uint32_t*>(B.lcount.p));
-  B.launches += 7;
+  B.launches += 14;
 }
 
 static vfk::FloodScratch flood_scratch(Batch& B) {
@@ -479,7 +493,7 @@ static vfk::FloodScratch flood_scratch(Batch& B) {
   fs.qhead = sc + 4;     // [3]
   fs.barrier = sc + 8;   // [2]
   fs.err = sc + 12;      // [1]
-  fs.stats = sc + 16;    // [4]
+  fs.stats = sc + 16;    // [8]: visits, passes, -, timeouts, sweeps, MAXIT hits
   fs.epoch = static_cast<uint32_t*>(B.epoch.p);
   fs.max_passes = 1u << 20;
   fs.total_bricks = B.sz.bricks;
@@ -492,7 +506,7 @@ vf_status Batch::enqueue_batched(bool do_upload, bool do_download) {
   launches = 0;
   flood_timed = false;
   for (int i = 0; i < NSTAGE_EV; ++i) stage_rec[i] = false;
-  auto mark = [&](int i) {
+  std::function<void(int)> mark = [&](int i) {
     if (cudaEventRecord(ev_stage[i], st) == cudaSuccess) stage_rec[i] = true;
   };
   mark(0);
@@ -508,19 +522,19 @@ vf_status Batch::enqueue_batched(bool do_upload, bool do_download) {
   uint8_t* lv = static_cast<uint8_t*>(live.p);
   const uint32_t maxc = sz.bricks;
   if (stages & ST_VOX) {
-    voxelize_stages(*this);
+    voxelize_stages(*this, mark);
   } else {
     // live bricks of an existing grid
     vfk::mark_live(st, dtable(T_VOX), bj, sz.bricks, lv);
     vfk::compact_live(st, lv, sz.bricks, lst, lc);
     launches += 2;
   }
-  mark(2);
+  mark(5);
   if (stages & (ST_SEED | ST_FRACTURE)) {
     vfk::sample_seeds(st, dtable(T_SEED), ds, n);
     launches += 1;
   }
-  mark(3);
+  mark(6);
   bool any_flood = false, any_naive = false, any_pert = false, any_erode = false,
        any_det1 = false, any_det3 = false, any_prefix = false;
   for (uint32_t i = 0; i < n; ++i) {
@@ -572,13 +586,13 @@ vf_status Batch::enqueue_batched(bool do_upload, bool do_download) {
     }
   }
   if (any_naive) { vfk::naive(st, dtable(T_NAIVE), ds, lst, lc, maxc, bj); launches += 1; }
-  mark(4);
+  mark(7);
   if (any_pert) {
     vfk::lattice(st, dtable(T_PERT), n);
     vfk::perturb(st, dtable(T_PERT), lst, lc, maxc, bj);
     launches += 2;
   }
-  mark(5);
+  mark(8);
   for (uint32_t it = 0; it < erode_iters; ++it) {
     vfk::detect_boundaries(st, dtable(t_edet(it)), lst, lc, maxc, bj);
     vfk::erode(st, dtable(t_ero(it)), lst, lc, maxc, bj);
@@ -587,12 +601,12 @@ vf_status Batch::enqueue_batched(bool do_upload, bool do_download) {
   if (any_erode) { vfk::remove_isolated(st, dtable(T_ISO), lst, lc, maxc, bj); launches += 1; }
   if (any_det1) { vfk::detect_boundaries(st, dtable(T_DET1), lst, lc, maxc, bj); launches += 1; }
   if (any_det3) { vfk::detect_boundaries_wide(st, dtable(T_DET3), lst, lc, maxc, bj); launches += 1; }
-  mark(6);
+  mark(9);
   if (stages & ST_COUNT) {
     vfk::count_values(st, dtable(T_CNT), ds, lst, lc, maxc, bj);
     launches += 1;
   }
-  mark(7);
+  mark(10);
   VF_CK(cudaGetLastError());
   // downloads
   for (uint32_t i = 0; i < n && (stages & ST_DOWNLOAD) && do_download; ++i) {
@@ -608,7 +622,7 @@ vf_status Batch::enqueue_batched(bool do_upload, bool do_download) {
   }
   VF_CK(cudaMemcpyAsync(h_state, ds, sizeof(JobState) * n, cudaMemcpyDeviceToHost, st));
   VF_CK(cudaMemcpyAsync(h_scal, scal.p, 64 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-  mark(8);
+  mark(11);
   VF_CK(cudaEventRecord(ev_done, st));
   return VF_OK;
 }
@@ -653,13 +667,15 @@ vf_status Batch::finish(vf_job_result* res) {
     if (cudaEventElapsedTime(&ms, ev_flood0, ev_flood1) == cudaSuccess) ctx->last_flood_ms = ms;
     ctx->last_flood_visits = h_scal[16];
     ctx->last_flood_passes = h_scal[17];
+    ctx->last_flood_sweeps = h_scal[20];
+    ctx->last_flood_maxit = h_scal[21];
   } else {
     ctx->last_flood_ms = 0.f;
     ctx->last_flood_visits = 0;
     ctx->last_flood_passes = 0;
   }
   ctx->last_launches = launches;
-  for (int i = 0; i < 8; ++i) {
+  for (int i = 0; i < NSTAGE_EV - 1; ++i) {
     float ms = 0.f;
     if (stage_rec[i] && stage_rec[i + 1] &&
         cudaEventElapsedTime(&ms, ev_stage[i], ev_stage[i + 1]) == cudaSuccess)
@@ -683,7 +699,8 @@ vf_status Batch::enqueue_plain_and_wait(vf_job_result* res, bool skip_vox) {
   if (N >= (1ull << 32)) return fail(VF_ERR_RANGE, "plain path needs X*Y*Z < 2^32");
   vf_status s = upload_common(*this);
   if (s) return s;
-  if (!skip_vox) voxelize_stages(*this);
+  std::function<void(int)> nomark = [](int) {};
+  if (!skip_vox) voxelize_stages(*this, nomark);
   JobState* ds = static_cast<JobState*>(state.p);
   vfk::sample_seeds(st, dtable(T_SEED), ds, 1);
   launches += 1;

@@ -57,15 +57,18 @@ struct Batch {
   bool own_stream = false;
   DevBuf grid0, grid1, keys, par, tets, range, ys, seeds, counts, lat, verts, faces, emask;
   DevBuf tables, state, brick_job, live, list, lcount, q[3], scal, epoch, front[2];
+  DevBuf pcnt, pbase, psums;  // flattened (tetrahedron, slice) work list
   void* h_tables = nullptr;  // pinned staging
   size_t h_tables_cap = 0;
   JobState* h_state = nullptr;  // pinned
   size_t h_state_cap = 0;
   uint32_t* h_scal = nullptr;   // pinned: [0..3] flood stats, [4] err, [8] fcount
   cudaEvent_t ev_flood0 = nullptr, ev_flood1 = nullptr, ev_done = nullptr;
-  // stage boundaries: 0 start, 1 inputs uploaded, 2 voxelized, 3 seeded,
-  // 4 fractured, 5 perturbed, 6 eroded/boundaries, 7 counted, 8 downloaded
-  static constexpr int NSTAGE_EV = 9;
+  // stage boundaries: 0 start, 1 inputs uploaded, 2 tetrahedra built,
+  // 3 parity rasterised, 4 shell tested, 5 voxelized (combine + live list),
+  // 6 seeded, 7 fractured, 8 perturbed, 9 eroded/boundaries, 10 counted,
+  // 11 downloaded
+  static constexpr int NSTAGE_EV = 12;
   cudaEvent_t ev_stage[NSTAGE_EV] = {};
   bool stage_rec[NSTAGE_EV] = {};
   std::vector<JobPlan> plans;
@@ -103,10 +106,12 @@ struct Ctx {
   // stats of the last batch
   uint64_t last_launches = 0;
   float last_flood_ms = 0.f;
-  float last_stage_ms[8] = {};
+  float last_stage_ms[11] = {};
   bool resident = false;  // batch inputs uploaded by vf_batch_prepare
   uint64_t last_flood_visits = 0;
   uint64_t last_flood_passes = 0;
+  uint64_t last_flood_sweeps = 0;
+  uint64_t last_flood_maxit = 0;
   vf_status alloc(DevBuf& b, size_t bytes);
   void free_buf(DevBuf& b);
 };

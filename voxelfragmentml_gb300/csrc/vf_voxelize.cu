@@ -9,10 +9,13 @@
 //                         lane sums of the vertices + the slice planes
 //   tetra_prep          : one thread per face -> tetrahedron (face + centroid)
 //                         in NDC, vertices sorted by y, slice range
-//   parity_raster       : one warp per tetrahedron, lanes over its slices;
-//                         cross-section triangles rasterised with exact
-//                         integer edge functions, XOR into bit planes
-//   shell_sat           : one warp per triangle, lanes over candidate voxels
+//   parity_raster       : (tetrahedron, slice) pairs flattened by a prefix
+//                         sum over the faces; each thread rasterises a run
+//                         of 64 pairs (cross-section triangles, exact integer
+//                         edge functions, XOR into bit planes)
+//   shell_sat           : per-face work items (columns of the triangle's
+//                         footprint) flattened by a prefix sum; each thread
+//                         tests a run of 16 items with the exact SAT
 //   combine             : one CTA per brick; bit planes -> uint16 0/1 rows,
 //                         brick liveness
 // All float arithmetic uses the _rn intrinsics (and the file is compiled
@@ -85,7 +88,8 @@ __device__ __forceinline__ uint32_t upper_bound_f(const float* a, uint32_t n, fl
   return lo;
 }
 
-__global__ void k_tetra(const JobDesc* jobs, JobState* st, int njobs, uint32_t total) {
+__global__ void k_tetra(const JobDesc* jobs, JobState* st, int njobs, uint32_t total,
+                        uint32_t* pcnt) {
   for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total;
        g += gridDim.x * blockDim.x) {
     const int j = job_of_face(jobs, njobs, g);
@@ -95,6 +99,7 @@ __global__ void k_tetra(const JobDesc* jobs, JobState* st, int njobs, uint32_t t
     if (fi[0] >= J.nverts || fi[1] >= J.nverts || fi[2] >= J.nverts) {
       atomicOr(&st[j].err, VF_JERR_INVALID);  // bad face: never dereferenced
       J.tet_range[f] = 0xFFFFu;
+      pcnt[g] = 0;
       continue;
     }
     float ctr[3], dim[3];
@@ -118,6 +123,7 @@ __global__ void k_tetra(const JobDesc* jobs, JobState* st, int njobs, uint32_t t
     uint32_t s0 = upper_bound_f(J.ys, J.Y, v[0].y);
     uint32_t s1e = upper_bound_f(J.ys, J.Y, v[3].y);
     J.tet_range[f] = (s1e > s0) ? (s0 | ((s1e - 1) << 16)) : 0xFFFFu;  // s0=0xFFFF,s1=0: none
+    pcnt[g] = s1e > s0 ? s1e - s0 : 0u;  // (tetrahedron, slice) pairs of this face
   }
 }
 
@@ -142,81 +148,238 @@ __device__ __forceinline__ int owns_edge(int ax, int az, int bx, int bz) {
   int dz = bz - az, dx = bx - ax;
   return (dz < 0) || (dz == 0 && dx > 0);
 }
-__device__ __forceinline__ long long fdiv_floor(long long a, long long b) {
-  long long q = a / b;
-  if ((a % b != 0) && ((a < 0) != (b < 0))) --q;
-  return q;
+
+// Narrow [lo, hi] (k' in [0, nk]) to the k' with q + k' * sk > 0.
+__device__ __forceinline__ void span_bound(long long q, long long sk, int nk, int& lo, int& hi) {
+  if (sk == 0) {
+    if (q <= 0) { lo = 1; hi = 0; }
+    return;
+  }
+  if (sk > 0) {  // increasing in k': smallest k' with a positive value
+    int k = 0;
+    if (q <= 0) {
+      const float est = __fdividef((float)(-q), (float)sk) + 1.0f;
+      k = (int)fminf(fmaxf(floorf(est), 0.0f), (float)(nk + 1));
+    }
+    while (k <= nk && q + (long long)k * sk <= 0) ++k;
+    while (k > 0 && q + (long long)(k - 1) * sk > 0) --k;
+    lo = max(lo, k);
+  } else {       // decreasing in k': largest k' with a positive value
+    if (q <= 0) { lo = 1; hi = 0; return; }
+    const float est = __fdividef((float)q, (float)(-sk));
+    int k = (int)fminf(fmaxf(floorf(est), -1.0f), (float)nk);
+    while (k >= 0 && q + (long long)k * sk <= 0) --k;
+    while (k < nk && q + (long long)(k + 1) * sk > 0) ++k;
+    hi = min(hi, k);
+  }
 }
 
+// Rasterise one cross-section triangle (NDC x,z) into the bit planes of
+// `slice` with XOR.  Same rule as the oracle: vertices snapped to 1/256 pixel,
+// pixel centres tested with exact integer edge functions, a sample exactly
+// on an edge belongs to the triangle for which it is a top-left edge.  With
+// integer E, "E > 0 || (E == 0 && owns)" is "E + owns > 0".
 __device__ void raster_xor(const JobDesc& J, uint32_t slice, float ax, float az, float bx,
                            float bz, float cx, float cz) {
   const float hw = __fmul_rn(0.5f, (float)J.X), hh = __fmul_rn(0.5f, (float)J.Z);
   int x0 = to_fixed(ax, hw), z0 = to_fixed(az, hh);
   int x1 = to_fixed(bx, hw), z1 = to_fixed(bz, hh);
   int x2 = to_fixed(cx, hw), z2 = to_fixed(cz, hh);
-  long long area = edge_fn(x0, z0, x1, z1, x2, z2);
+  const int mnx = min(x0, min(x1, x2)), mxx = max(x0, max(x1, x2));
+  const int mnz = min(z0, min(z1, z2)), mxz = max(z0, max(z1, z2));
+  // pixel centres 256*i + 128 inside [mn, mx] (fixed point)
+  const int ilo = max((mnx + 127) >> 8, 0), ihi = min((mxx - 128) >> 8, (int)J.X - 1);
+  const int klo = max((mnz + 127) >> 8, 0), khi = min((mxz - 128) >> 8, (int)J.Z - 1);
+  if (ilo > ihi || klo > khi) return;
+  const long long area = edge_fn(x0, z0, x1, z1, x2, z2);
   if (area == 0) return;
   if (area < 0) { int tx = x1, tz = z1; x1 = x2; z1 = z2; x2 = tx; z2 = tz; }
-  int mnx = min(x0, min(x1, x2)), mxx = max(x0, max(x1, x2));
-  int mnz = min(z0, min(z1, z2)), mxz = max(z0, max(z1, z2));
-  long long ilo = fdiv_floor((long long)mnx - 128 + 255, 256), ihi = fdiv_floor((long long)mxx - 128, 256);
-  long long klo = fdiv_floor((long long)mnz - 128 + 255, 256), khi = fdiv_floor((long long)mxz - 128, 256);
-  if (ilo < 0) ilo = 0;
-  if (klo < 0) klo = 0;
-  if (ihi > (long long)J.X - 1) ihi = (long long)J.X - 1;
-  if (khi > (long long)J.Z - 1) khi = (long long)J.Z - 1;
-  const int o01 = owns_edge(x0, z0, x1, z1), o12 = owns_edge(x1, z1, x2, z2),
-            o20 = owns_edge(x2, z2, x0, z0);
-  for (long long i = ilo; i <= ihi; ++i) {
-    const long long px = i * 256 + 128;
-    uint32_t* row = J.par + ((size_t)i * J.Y + slice) * J.Zw;
-    uint32_t word = 0xFFFFFFFFu, bits = 0;
-    for (long long k = klo; k <= khi; ++k) {
-      const long long pz = k * 256 + 128;
-      long long e0 = edge_fn(x0, z0, x1, z1, px, pz);
-      long long e1 = edge_fn(x1, z1, x2, z2, px, pz);
-      long long e2 = edge_fn(x2, z2, x0, z0, px, pz);
-      bool in = (e0 > 0 || (e0 == 0 && o01)) && (e1 > 0 || (e1 == 0 && o12)) &&
-                (e2 > 0 || (e2 == 0 && o20));
-      if (!in) continue;
-      uint32_t w = (uint32_t)(k >> 5);
-      if (w != word) {
-        if (bits) atomicXor(row + word, bits);
-        word = w;
-        bits = 0;
+  const long long b0 = owns_edge(x0, z0, x1, z1), b1 = owns_edge(x1, z1, x2, z2),
+                  b2 = owns_edge(x2, z2, x0, z0);
+  const long long px0 = (long long)ilo * 256 + 128, pz0 = (long long)klo * 256 + 128;
+  // edge values (+ tie bias) at the first pixel centre; steps per k and per i
+  const long long r0 = edge_fn(x0, z0, x1, z1, px0, pz0) + b0;
+  const long long r1 = edge_fn(x1, z1, x2, z2, px0, pz0) + b1;
+  const long long r2 = edge_fn(x2, z2, x0, z0, px0, pz0) + b2;
+  const long long sk0 = 256LL * (x1 - x0), sk1 = 256LL * (x2 - x1), sk2 = 256LL * (x0 - x2);
+  const long long si0 = -256LL * (z1 - z0), si1 = -256LL * (z2 - z1), si2 = -256LL * (z0 - z2);
+  uint32_t* const col = J.par + (size_t)slice * J.Zw;  // + i * Y * Zw per pixel column
+  const size_t istride = (size_t)J.Y * J.Zw;
+  if (ihi - ilo <= 1 && khi - klo <= 1) {
+    // <= 2x2 candidate pixels (almost every cross-section): no loops
+#pragma unroll
+    for (int di = 0; di < 2; ++di) {
+      if (ilo + di > ihi) break;
+      const long long e0 = r0 + di * si0, e1 = r1 + di * si1, e2 = r2 + di * si2;
+      const bool in0 = (e0 > 0) & (e1 > 0) & (e2 > 0);
+      const bool in1 = (klo + 1 <= khi) & (e0 + sk0 > 0) & (e1 + sk1 > 0) & (e2 + sk2 > 0);
+      uint32_t* row = col + (size_t)(ilo + di) * istride;
+      const uint32_t w0 = (uint32_t)klo >> 5, w1 = (uint32_t)(klo + 1) >> 5;
+      const uint32_t m0 = in0 ? 1u << (klo & 31) : 0u, m1 = in1 ? 1u << ((klo + 1) & 31) : 0u;
+      if (w0 == w1) {
+        if (m0 | m1) atomicXor(row + w0, m0 | m1);
+      } else {
+        if (m0) atomicXor(row + w0, m0);
+        if (m1) atomicXor(row + w1, m1);
       }
-      bits ^= 1u << (k & 31);
     }
-    if (bits) atomicXor(row + word, bits);
+    return;
+  }
+  // span path: for pixel column i the covered k form one interval (the
+  // triangle is convex); each edge bounds it from one side.  The bound is
+  // estimated with a float division and then fixed with exact integer edge
+  // values, so the covered set is exactly the per-pixel test's.
+  const int nk = khi - klo;
+  long long q0 = r0, q1 = r1, q2 = r2;
+  for (int i = ilo; i <= ihi; ++i, q0 += si0, q1 += si1, q2 += si2) {
+    int lo = 0, hi = nk;
+    span_bound(q0, sk0, nk, lo, hi);
+    span_bound(q1, sk1, nk, lo, hi);
+    span_bound(q2, sk2, nk, lo, hi);
+    if (lo > hi) continue;
+    uint32_t* row = col + (size_t)i * istride;
+    const int ka = klo + lo, kb = klo + hi;
+    for (int w = ka >> 5; w <= (kb >> 5); ++w) {
+      const int a = max(ka, w << 5) & 31, b = min(kb, (w << 5) + 31) & 31;
+      const uint32_t m = (b == 31 ? 0xFFFFFFFFu : ((2u << b) - 1u)) & ~((1u << a) - 1u);
+      atomicXor(row + w, m);
+    }
   }
 }
 
-__global__ void k_parity(const JobDesc* jobs, int njobs, uint32_t total) {
+// one (tetrahedron, slice) pair: the 1-2 cross-section triangles
+// (Tetravoxelizer.cpp:59-89; endpoint choice without divergent branches)
+__device__ __forceinline__ void cross_section(const JobDesc& J, const tv& A, const tv& B,
+                                              const tv& Cc, const tv& D, uint32_t s) {
+  const float sl = J.ys[s];
+  float p0x, p0z, v1x, v1z, v2x, v2z;
+  interp(A, D, sl, p0x, p0z);
+  const bool ab = sl <= B.y, ac = sl <= Cc.y;
+  interp(ab ? A : B, ab ? B : D, sl, v1x, v1z);
+  interp(ac ? A : Cc, ac ? Cc : D, sl, v2x, v2z);
+  raster_xor(J, s, p0x, p0z, v1x, v1z, v2x, v2z);
+  if (B.y < sl && sl <= Cc.y) {
+    float bx, bz;
+    interp(B, Cc, sl, bx, bz);
+    raster_xor(J, s, bx, bz, v2x, v2z, v1x, v1z);
+  }
+}
+
+// ---- exclusive scan of the per-face pair counts (1024 faces per block) -----
+__device__ __forceinline__ unsigned long long warp_incl_scan(unsigned long long v) {
   const int lane = threadIdx.x & 31;
-  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < total; g += warps) {
-    const int j = job_of_face(jobs, njobs, g);
-    const JobDesc& J = jobs[j];
-    const uint32_t f = g - J.face_base;
-    const uint32_t rg = J.tet_range[f];
-    const uint32_t s0 = rg & 0xFFFFu, s1 = rg >> 16;
-    if (s0 > s1) continue;
-    const float4* o = J.tets + 3 * (size_t)f;
-    float4 q0 = o[0], q1 = o[1], q2 = o[2];
-    tv A = {q0.x, q0.y, q0.z}, B = {q0.w, q1.x, q1.y}, Cc = {q1.z, q1.w, q2.x},
-       D = {q2.y, q2.z, q2.w};
-    for (uint32_t s = s0 + lane; s <= s1; s += 32) {
-      const float sl = J.ys[s];
-      float p0x, p0z, v1x, v1z, v2x, v2z;
-      interp(A, D, sl, p0x, p0z);
-      if (sl <= B.y) interp(A, B, sl, v1x, v1z); else interp(B, D, sl, v1x, v1z);
-      if (sl <= Cc.y) interp(A, Cc, sl, v2x, v2z); else interp(Cc, D, sl, v2x, v2z);
-      raster_xor(J, s, p0x, p0z, v1x, v1z, v2x, v2z);
-      if (B.y < sl && sl <= Cc.y) {
-        float bx, bz;
-        interp(B, Cc, sl, bx, bz);
-        raster_xor(J, s, bx, bz, v2x, v2z, v1x, v1z);
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long t = __shfl_up_sync(0xFFFFFFFFu, v, o);
+    if (lane >= o) v += t;
+  }
+  return v;
+}
+// block-wide exclusive scan of one value per thread (blockDim 1024)
+__device__ unsigned long long block_excl_scan(unsigned long long v, unsigned long long* total) {
+  __shared__ unsigned long long ws[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const unsigned long long inc = warp_incl_scan(v);
+  if (lane == 31) ws[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    const unsigned long long x = ws[lane];
+    ws[lane] = warp_incl_scan(x) - x;
+  }
+  __syncthreads();
+  const unsigned long long r = ws[w] + inc - v;
+  if (total && threadIdx.x == blockDim.x - 1) *total = r + v;
+  __syncthreads();
+  return r;
+}
+__global__ void __launch_bounds__(1024) k_scan_local(const uint32_t* in, unsigned long long* out,
+                                                     unsigned long long* sums, uint32_t n) {
+  const uint32_t i = blockIdx.x * 1024u + threadIdx.x;
+  const unsigned long long v = i < n ? in[i] : 0ull;
+  __shared__ unsigned long long tot;
+  const unsigned long long r = block_excl_scan(v, &tot);
+  if (i < n) out[i] = r;
+  if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+__global__ void __launch_bounds__(1024) k_scan_sums(unsigned long long* sums, uint32_t nb,
+                                                    unsigned long long* grand) {
+  // one block: each thread owns a contiguous chunk of block sums
+  const uint32_t per = (nb + 1023) / 1024;
+  const uint32_t b0 = threadIdx.x * per, b1 = min(b0 + per, nb);
+  unsigned long long acc = 0;
+  for (uint32_t b = b0; b < b1; ++b) acc += sums[b];
+  __shared__ unsigned long long tot;
+  unsigned long long base = block_excl_scan(acc, &tot);
+  for (uint32_t b = b0; b < b1; ++b) {
+    const unsigned long long t = sums[b];
+    sums[b] = base;
+    base += t;
+  }
+  if (threadIdx.x == 0) *grand = tot;
+}
+__global__ void k_scan_add(unsigned long long* out, const unsigned long long* sums, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] += sums[i / 1024u];
+}
+
+// Warp-interleaved runs over a flattened work list (faces in batch order,
+// items of a face contiguous): a warp owns WARP_RUN consecutive items and
+// lane l takes items base + l, base + l + 32, ...  Neighbouring lanes work on
+// neighbouring items of the same face, so control flow stays coherent and no
+// lane idles when a face has few items.  One binary search per warp run; each
+// lane then steps its face cursor forward.
+constexpr uint32_t WARP_RUN = 32 * 16;
+
+__device__ __forceinline__ uint32_t face_of_item(const unsigned long long* base, uint32_t nfaces,
+                                                 unsigned long long p) {
+  uint32_t lo = 0, hi = nfaces - 1;  // last face whose first item is <= p
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) >> 1;
+    if (base[mid] <= p) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(256, 4) k_parity_flat(const JobDesc* jobs, int njobs,
+                                                     const uint32_t* pcnt,
+                                                     const unsigned long long* pbase,
+                                                     const unsigned long long* ptotal,
+                                                     uint32_t total_faces) {
+  const unsigned long long total = *ptotal;
+  const int lane = threadIdx.x & 31;
+  const unsigned long long nwruns = (total + WARP_RUN - 1) / WARP_RUN;
+  const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+  for (unsigned long long wr = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
+       wr < nwruns; wr += nwarps) {
+    const unsigned long long base = wr * WARP_RUN;
+    const unsigned long long end = min(base + WARP_RUN, total);
+    uint32_t g = 0;
+    if (lane == 0) g = face_of_item(pbase, total_faces, base);
+    g = __shfl_sync(0xFFFFFFFFu, g, 0);
+    uint32_t cached = 0xFFFFFFFFu;
+    tv A, B, Cc, D;
+    const JobDesc* J = nullptr;
+    uint32_t s0 = 0;
+    unsigned long long fb = 0, fe = 0;
+    for (unsigned long long p = base + lane; p < end; p += 32) {
+      // advance the face cursor (faces with no item have pbase equal to the next)
+      while (p >= pbase[g] + pcnt[g]) ++g;
+      if (g != cached) {
+        cached = g;
+        J = &jobs[job_of_face(jobs, njobs, g)];
+        const uint32_t f = g - J->face_base;
+        const float4* o = J->tets + 3 * (size_t)f;
+        const float4 q0 = o[0], q1 = o[1], q2 = o[2];
+        A = {q0.x, q0.y, q0.z};
+        B = {q0.w, q1.x, q1.y};
+        Cc = {q1.z, q1.w, q2.x};
+        D = {q2.y, q2.z, q2.w};
+        s0 = J->tet_range[f] & 0xFFFFu;
+        fb = pbase[g];
+        fe = fb + pcnt[g];
       }
+      (void)fe;
+      cross_section(*J, A, B, Cc, D, s0 + (uint32_t)(p - fb));
     }
   }
 }
@@ -311,43 +474,156 @@ __device__ __forceinline__ int float_cell(float f, int n) {
   return vf_clampi((int)floorf(f), -2, n + 1);
 }
 
-__global__ void k_shell(const JobDesc* jobs, int njobs, uint32_t total) {
+// the exact test of one voxel (reference operation order) and the mark
+__device__ __forceinline__ void test_cell(const JobDesc& J, const float* cs, const tv& p0,
+                                          const tv& p1, const tv& p2, int i, int jj, int k) {
+  tv bmin = {ADD(J.amin[0], MUL(cs[0], (float)i)), ADD(J.amin[1], MUL(cs[1], (float)jj)),
+             ADD(J.amin[2], MUL(cs[2], (float)k))};
+  tv bmax = {ADD(bmin.x, cs[0]), ADD(bmin.y, cs[1]), ADD(bmin.z, cs[2])};
+  tv ce = {__fdiv_rn(ADD(bmax.x, bmin.x), 2.0f), __fdiv_rn(ADD(bmax.y, bmin.y), 2.0f),
+           __fdiv_rn(ADD(bmax.z, bmin.z), 2.0f)};
+  tv r = {SUB(bmax.x, ce.x), SUB(bmax.y, ce.y), SUB(bmax.z, ce.z)};
+  if (tri_box(p0, p1, p2, ce, r))
+    atomicOr(J.shell + ((size_t)i * J.Y + jj) * J.Zw + (k >> 5), 1u << (k & 31));
+}
+
+// Per-face setup of the shell test.  Candidates: the triangle's cell bbox
+// grown by one cell.  Pruning: two of the SAT's own separating axes are
+// evaluated early with a margin of a quarter cell -- (1) the triangle's
+// projection on the plane orthogonal to its dominant normal axis c against
+// each column's square (the edge x c axes and the a, b box axes), (2) the
+// plane slab along c (the plane-box test).  A dropped box is separated by at
+// least 0.25 cell along a SAT axis, far beyond float rounding, so the exact
+// SAT would reject it too: the marked set equals testing the full bbox.
+// Work items: columns (a, b) when pruning, else every bbox cell.
+struct ShellSetup {
+  float cs[3], q0[3], nr[3], Pa[3], Pb[3];
+  float ha, hb, w;
+  tv p0, p1, p2;
+  int lo[3], n[3];
+  int c, ax, bx;
+  bool prune;
+  uint32_t items;
+};
+
+__device__ bool shell_setup(const JobDesc& J, uint32_t f, ShellSetup& S) {
+  const uint32_t dims[3] = {J.X, J.Y, J.Z};
+  for (int a = 0; a < 3; ++a) S.cs[a] = __fdiv_rn(SUB(J.amax[a], J.amin[a]), (float)dims[a]);
+  const uint32_t* fi = J.faces + 3 * (size_t)f;
+  if (fi[0] >= J.nverts || fi[1] >= J.nverts || fi[2] >= J.nverts) return false;
+  const float* q0 = J.verts + 3 * (size_t)fi[0];
+  const float* q1 = J.verts + 3 * (size_t)fi[1];
+  const float* q2 = J.verts + 3 * (size_t)fi[2];
+  for (int a = 0; a < 3; ++a) {
+    float mn, mx;
+    mm3(q0[a], q1[a], q2[a], mn, mx);
+    S.lo[a] = vf_clampi(float_cell(__fdiv_rn(SUB(mn, J.amin[a]), S.cs[a]), dims[a]) - 1, 0, dims[a] - 1);
+    const int hi = vf_clampi(float_cell(__fdiv_rn(SUB(mx, J.amin[a]), S.cs[a]), dims[a]) + 1, 0, dims[a] - 1);
+    S.n[a] = hi - S.lo[a] + 1;
+    S.q0[a] = q0[a];
+  }
+  S.p0 = {q0[0], q0[1], q0[2]};
+  S.p1 = {q1[0], q1[1], q1[2]};
+  S.p2 = {q2[0], q2[1], q2[2]};
+  const float e1[3] = {q1[0] - q0[0], q1[1] - q0[1], q1[2] - q0[2]};
+  const float e2[3] = {q2[0] - q0[0], q2[1] - q0[1], q2[2] - q0[2]};
+  S.nr[0] = e1[1] * e2[2] - e1[2] * e2[1];
+  S.nr[1] = e1[2] * e2[0] - e1[0] * e2[2];
+  S.nr[2] = e1[0] * e2[1] - e1[1] * e2[0];
+  int c = 0;
+  if (fabsf(S.nr[1]) > fabsf(S.nr[c])) c = 1;
+  if (fabsf(S.nr[2]) > fabsf(S.nr[c])) c = 2;
+  S.c = c;
+  S.ax = (c + 1) % 3;
+  S.bx = (c + 2) % 3;
+  const float e1n = fabsf(e1[0]) + fabsf(e1[1]) + fabsf(e1[2]);
+  const float e2n = fabsf(e2[0]) + fabsf(e2[1]) + fabsf(e2[2]);
+  S.prune = fabsf(S.nr[c]) > 1e-3f * e1n * e2n && fabsf(S.nr[c]) > 0.0f;
+  if (!S.prune) {
+    S.items = (uint32_t)(S.n[0] * S.n[1] * S.n[2]);
+    return true;
+  }
+  // projected triangle (relative to q0), counter-clockwise
+  float P1a = e1[S.ax], P1b = e1[S.bx], P2a = e2[S.ax], P2b = e2[S.bx];
+  if (S.nr[c] < 0.0f) { float t = P1a; P1a = P2a; P2a = t; t = P1b; P1b = P2b; P2b = t; }
+  S.Pa[0] = 0.0f; S.Pa[1] = P1a; S.Pa[2] = P2a;
+  S.Pb[0] = 0.0f; S.Pb[1] = P1b; S.Pb[2] = P2b;
+  S.ha = 0.75f * S.cs[S.ax];  // half cell + quarter-cell margin
+  S.hb = 0.75f * S.cs[S.bx];
+  const float hc = 0.75f * S.cs[c];
+  S.w = hc + fabsf(S.nr[S.ax]) / fabsf(S.nr[c]) * S.ha + fabsf(S.nr[S.bx]) / fabsf(S.nr[c]) * S.hb;
+  S.items = (uint32_t)(S.n[S.ax] * S.n[S.bx]);
+  return true;
+}
+
+__device__ void shell_item(const JobDesc& J, const ShellSetup& S, uint32_t q) {
+  if (!S.prune) {
+    const int k = S.lo[2] + (int)(q % S.n[2]);
+    const int jj = S.lo[1] + (int)((q / S.n[2]) % S.n[1]);
+    const int i = S.lo[0] + (int)(q / (S.n[2] * S.n[1]));
+    test_cell(J, S.cs, S.p0, S.p1, S.p2, i, jj, k);
+    return;
+  }
+  const int ax = S.ax, bx = S.bx, c = S.c;
+  const int ia = S.lo[ax] + (int)(q / S.n[bx]), ib = S.lo[bx] + (int)(q % S.n[bx]);
+  const float ca = (J.amin[ax] + S.cs[ax] * ((float)ia + 0.5f)) - S.q0[ax];
+  const float cb = (J.amin[bx] + S.cs[bx] * ((float)ib + 0.5f)) - S.q0[bx];
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    const int f2 = (e + 1) % 3;
+    const float dx = S.Pa[f2] - S.Pa[e], dy = S.Pb[f2] - S.Pb[e];
+    const float E = dx * (cb - S.Pb[e]) - dy * (ca - S.Pa[e]);
+    if (E + fabsf(dx) * S.hb + fabsf(dy) * S.ha < 0.0f) return;
+  }
+  const float tc = S.q0[c] - (S.nr[ax] * ca + S.nr[bx] * cb) / S.nr[c];
+  const int klo = max(S.lo[c], (int)floorf((tc - S.w - J.amin[c]) / S.cs[c] - 0.5f));
+  const int khi = min(S.lo[c] + S.n[c] - 1, (int)ceilf((tc + S.w - J.amin[c]) / S.cs[c] - 0.5f));
+  for (int k = klo; k <= khi; ++k) {
+    int idx[3];
+    idx[ax] = ia;
+    idx[bx] = ib;
+    idx[c] = k;
+    test_cell(J, S.cs, S.p0, S.p1, S.p2, idx[0], idx[1], idx[2]);
+  }
+}
+
+__global__ void k_shell_count(const JobDesc* jobs, int njobs, uint32_t total, uint32_t* scnt) {
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+    const JobDesc& J = jobs[job_of_face(jobs, njobs, g)];
+    ShellSetup S;
+    scnt[g] = shell_setup(J, g - J.face_base, S) ? S.items : 0u;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_shell_flat(const JobDesc* jobs, int njobs,
+                                                    const uint32_t* scnt,
+                                                    const unsigned long long* sbase,
+                                                    const unsigned long long* stotal,
+                                                    uint32_t total_faces) {
+  const unsigned long long total = *stotal;
   const int lane = threadIdx.x & 31;
-  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < total; g += warps) {
-    const int j = job_of_face(jobs, njobs, g);
-    const JobDesc& J = jobs[j];
-    const uint32_t f = g - J.face_base;
-    const uint32_t dims[3] = {J.X, J.Y, J.Z};
-    float cs[3];
-    for (int a = 0; a < 3; ++a) cs[a] = __fdiv_rn(SUB(J.amax[a], J.amin[a]), (float)dims[a]);
-    const uint32_t* fi = J.faces + 3 * (size_t)f;
-    if (fi[0] >= J.nverts || fi[1] >= J.nverts || fi[2] >= J.nverts) continue;  // flagged by k_tetra
-    const float* q0 = J.verts + 3 * (size_t)fi[0];
-    const float* q1 = J.verts + 3 * (size_t)fi[1];
-    const float* q2 = J.verts + 3 * (size_t)fi[2];
-    int lo[3], n[3];
-    for (int a = 0; a < 3; ++a) {
-      float mn, mx;
-      mm3(q0[a], q1[a], q2[a], mn, mx);
-      lo[a] = vf_clampi(float_cell(__fdiv_rn(SUB(mn, J.amin[a]), cs[a]), dims[a]) - 1, 0, dims[a] - 1);
-      int hi = vf_clampi(float_cell(__fdiv_rn(SUB(mx, J.amin[a]), cs[a]), dims[a]) + 1, 0, dims[a] - 1);
-      n[a] = hi - lo[a] + 1;
-    }
-    const tv p0 = {q0[0], q0[1], q0[2]}, p1 = {q1[0], q1[1], q1[2]}, p2 = {q2[0], q2[1], q2[2]};
-    const int cnt = n[0] * n[1] * n[2];
-    for (int c = lane; c < cnt; c += 32) {
-      const int k = lo[2] + c % n[2];
-      const int jj = lo[1] + (c / n[2]) % n[1];
-      const int i = lo[0] + c / (n[2] * n[1]);
-      tv bmin = {ADD(J.amin[0], MUL(cs[0], (float)i)), ADD(J.amin[1], MUL(cs[1], (float)jj)),
-                 ADD(J.amin[2], MUL(cs[2], (float)k))};
-      tv bmax = {ADD(bmin.x, cs[0]), ADD(bmin.y, cs[1]), ADD(bmin.z, cs[2])};
-      tv ce = {__fdiv_rn(ADD(bmax.x, bmin.x), 2.0f), __fdiv_rn(ADD(bmax.y, bmin.y), 2.0f),
-               __fdiv_rn(ADD(bmax.z, bmin.z), 2.0f)};
-      tv r = {SUB(bmax.x, ce.x), SUB(bmax.y, ce.y), SUB(bmax.z, ce.z)};
-      if (tri_box(p0, p1, p2, ce, r))
-        atomicOr(J.shell + ((size_t)i * J.Y + jj) * J.Zw + (k >> 5), 1u << (k & 31));
+  const unsigned long long nwruns = (total + WARP_RUN - 1) / WARP_RUN;
+  const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+  for (unsigned long long wr = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
+       wr < nwruns; wr += nwarps) {
+    const unsigned long long base = wr * WARP_RUN;
+    const unsigned long long end = min(base + WARP_RUN, total);
+    uint32_t g = 0;
+    if (lane == 0) g = face_of_item(sbase, total_faces, base);
+    g = __shfl_sync(0xFFFFFFFFu, g, 0);
+    uint32_t cached = 0xFFFFFFFFu;
+    ShellSetup S;
+    const JobDesc* J = nullptr;
+    unsigned long long fb = 0;
+    for (unsigned long long p = base + lane; p < end; p += 32) {
+      while (p >= sbase[g] + scnt[g]) ++g;
+      if (g != cached) {
+        cached = g;
+        J = &jobs[job_of_face(jobs, njobs, g)];
+        shell_setup(*J, g - J->face_base, S);
+        fb = sbase[g];
+      }
+      shell_item(*J, S, (uint32_t)(p - fb));
     }
   }
 }
@@ -441,14 +717,28 @@ void centroid_and_slices(cudaStream_t st, const JobDesc* dj, JobState* ds, int n
   if (njobs > 0) k_centroid<<<njobs, 1024, 0, st>>>(dj, ds);
 }
 void tetra_prep(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs,
-                uint32_t total_faces) {
-  if (total_faces) k_tetra<<<grid_for(total_faces, 256, 65535), 256, 0, st>>>(dj, ds, njobs, total_faces);
+                uint32_t total_faces, const FaceScratch& fs) {
+  if (total_faces)
+    k_tetra<<<grid_for(total_faces, 256, 65535), 256, 0, st>>>(dj, ds, njobs, total_faces, fs.pcnt);
 }
-void parity_raster(cudaStream_t st, const JobDesc* dj, int njobs, uint32_t total_faces) {
-  if (total_faces) k_parity<<<grid_for(total_faces, 8, 1 << 20), 256, 0, st>>>(dj, njobs, total_faces);
+void parity_raster(cudaStream_t st, const JobDesc* dj, int njobs, uint32_t total_faces,
+                   const FaceScratch& fs, int num_sms) {
+  if (!total_faces) return;
+  const uint32_t nb = (total_faces + 1023) / 1024;
+  k_scan_local<<<nb, 1024, 0, st>>>(fs.pcnt, fs.pbase, fs.psums, total_faces);
+  k_scan_sums<<<1, 1024, 0, st>>>(fs.psums, nb, fs.ptotal);
+  k_scan_add<<<(total_faces + 255) / 256, 256, 0, st>>>(fs.pbase, fs.psums, total_faces);
+  k_parity_flat<<<num_sms * 16, 256, 0, st>>>(dj, njobs, fs.pcnt, fs.pbase, fs.ptotal, total_faces);
 }
-void shell_sat(cudaStream_t st, const JobDesc* dj, int njobs, uint32_t total_faces) {
-  if (total_faces) k_shell<<<grid_for(total_faces, 8, 1 << 20), 256, 0, st>>>(dj, njobs, total_faces);
+void shell_sat(cudaStream_t st, const JobDesc* dj, int njobs, uint32_t total_faces,
+               const FaceScratch& fs, int num_sms) {
+  if (!total_faces) return;
+  const uint32_t nb = (total_faces + 1023) / 1024;
+  k_shell_count<<<grid_for(total_faces, 256, 65535), 256, 0, st>>>(dj, njobs, total_faces, fs.pcnt);
+  k_scan_local<<<nb, 1024, 0, st>>>(fs.pcnt, fs.pbase, fs.psums, total_faces);
+  k_scan_sums<<<1, 1024, 0, st>>>(fs.psums, nb, fs.ptotal);
+  k_scan_add<<<(total_faces + 255) / 256, 256, 0, st>>>(fs.pbase, fs.psums, total_faces);
+  k_shell_flat<<<num_sms * 16, 256, 0, st>>>(dj, njobs, fs.pcnt, fs.pbase, fs.ptotal, total_faces);
 }
 void combine(cudaStream_t st, const JobDesc* dj, const uint32_t* brick_job,
              uint32_t total_bricks, uint8_t* live, int dual) {
