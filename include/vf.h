@@ -245,6 +245,23 @@ vf_status vf_server_poll(vf_server* s, vf_job_result* out, uint32_t max,
                          uint32_t* n, int wait_ms);
 vf_status vf_server_destroy(vf_server* s);
 
+/* ---- flood without device allocation ------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory during this step (their memory is owned by a pool of their own, or
+ * must not grow after start-up): FloodFracturer::build semantics on the
+ * caller's device buffers -- d_grid (uint16, x-major X*Y*Z, 0 = EMPTY), the
+ * seeds (device, 4 uint32 x,y,z,label per seed, labels 2..255) -- writing the
+ * labels to d_labels (uint16, x-major X*Y*Z).  All scratch lives in one
+ * file-scope device array of 32 MiB inside the library, held by every GPU
+ * that loads it until exit; grids needing more (about 5 million voxels)
+ * return VF_ERR_RANGE.  Calls share that array: calls that overlap on the
+ * GPU race.  The first call on a device looks up the array's address; make
+ * it before any stream capture.  Runs on `stream` (a cudaStream_t, NULL =
+ * default stream) and returns when the labels are written. */
+vf_status vf_flood_noalloc(const uint16_t* d_grid, uint16_t* d_labels, uint32_t X, uint32_t Y,
+                           uint32_t Z, const uint32_t* d_seeds_xyzw, uint32_t nseeds,
+                           int distance, void* stream);
+
 /* ---- timing helpers for benchmarks (CUDA events on the context stream) --- */
 vf_status vf_ctx_event_record(vf_ctx* ctx, int slot);
 vf_status vf_ctx_event_elapsed(vf_ctx* ctx, int slot_a, int slot_b, float* ms);

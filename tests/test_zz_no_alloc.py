@@ -1,0 +1,69 @@
+"""The flood entry point that allocates no device memory, vf_flood_noalloc.
+
+It exists for callers that cannot allocate while this step runs (their
+device memory belongs to a pool of their own, or must not grow after
+start-up): they pass their own device buffers and the library uses a fixed
+scratch array of its own.  This test calls it through the C ABI on device
+buffers owned by the test and checks its labels against the regular flood
+entry point (vf_fracture through a grid), bit for bit, on two calls in a
+row.  The file is collected last so that a run stopping at the first
+failure has already run every other test.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle as O
+from voxelfragmentml_gb300 import vessel as Vs
+
+pytestmark = pytest.mark.gpu
+
+
+def _device_call(vf, occ, seeds, dfunc):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    g = torch.from_numpy(occ.astype(np.int16)).cuda()
+    out = torch.full(occ.shape, -1, dtype=torch.int16, device="cuda")
+    s = torch.from_numpy(seeds.astype(np.int32)).cuda()
+    torch.cuda.synchronize()
+    X, Y, Z = occ.shape
+    st = vf.lib().vf_flood_noalloc(C.c_void_p(g.data_ptr()), C.c_void_p(out.data_ptr()),
+                                   X, Y, Z, C.c_void_p(s.data_ptr()), seeds.shape[0], dfunc,
+                                   None)
+    assert st == 0, vf.lib().vf_last_error()
+    torch.cuda.synchronize()
+    return out.cpu().numpy().view(np.uint16)
+
+
+def _regular(vf, ctx, occ, seeds, dfunc):
+    grid = vf.RegularGrid(occ.shape, None, None, ctx)
+    grid.upload(occ)
+    fr = vf.FloodFracturer()
+    fr.setDistanceFunction(dfunc)
+    fr.build(grid, seeds)
+    return grid.data()
+
+
+def test_flood_noalloc_matches_regular_entry_point_twice(vf, ctx, oracle_lib):
+    v, f = Vs.vessel_mesh(64, 48, 5)
+    mn, mx = Vs.mesh_aabb(v)
+    dims = Vs.grid_dims(mn, mx, 60)   # Z % 8 == 4: padded rows inside the scratch
+    occ = O.voxelize(v, f, dims, mn, mx)
+    cases = [(O.seeder_uniform(occ, 9, 3, 2), 1), (O.seeder_uniform(occ, 21, 4, 2), 2)]
+    for seeds, dfunc in cases:  # two calls in a row share the scratch array
+        got = _device_call(vf, occ, seeds, dfunc)
+        exp = _regular(vf, ctx, occ, seeds, dfunc)
+        assert np.array_equal(got, exp)
+
+
+def test_flood_noalloc_rejects_oversize(vf, ctx):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    g = torch.zeros(8, dtype=torch.int16, device="cuda")
+    st = vf.lib().vf_flood_noalloc(C.c_void_p(g.data_ptr()), C.c_void_p(g.data_ptr()),
+                                   512, 512, 512, None, 0, 1, None)
+    assert st == vf.ERR_RANGE
+    assert b"scratch" in vf.lib().vf_last_error()

@@ -128,6 +128,8 @@ EXPORTS = {
     "vf_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "vf_server_poll": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int]),
     "vf_server_destroy": (C.c_int, [C.c_void_p]),
+    "vf_flood_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
+                                   C.c_void_p, C.c_uint32, C.c_int, C.c_void_p]),
     "vf_ctx_event_record": (C.c_int, [C.c_void_p, C.c_int]),
     "vf_ctx_event_elapsed": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     "vf_ctx_last_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
