@@ -58,6 +58,44 @@ def test_voxelize(vf, ctx, case):
     assert np.array_equal(got, exp), f"{int((got != exp).sum())} voxels differ"
 
 
+def _soup(seed):
+    """Open, non-manifold and degenerate meshes: random triangle soups (some on
+    a coarse lattice, so vertices share slice planes and pixel centres),
+    faces with a repeated vertex, duplicated faces."""
+    rng = np.random.default_rng(seed)
+    nv = int(rng.integers(3, 60))
+    nf = int(rng.integers(1, 90))
+    v = rng.random((nv, 3)).astype(np.float32)
+    if seed % 3 == 0:
+        v = (np.round(v * 8) / 8).astype(np.float32)
+    f = rng.integers(0, nv, (nf, 3)).astype(np.uint32)
+    if seed % 4 == 1:
+        f = np.concatenate([f, f[: nf // 2]])
+    dims = tuple(int(x) for x in rng.integers(4, 48, 3))
+    return v, f, v.min(0), v.max(0), dims
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_voxelize_open_and_degenerate_meshes(vf, ctx, seed):
+    v, f, mn, mx, dims = _soup(seed)
+    g = vf.RegularGrid(dims, mn, mx, ctx)
+    g.fill(v, f)
+    got = g.data()
+    exp = O.voxelize(v, f, dims, mn, mx)
+    assert np.array_equal(got, exp), f"{int((got != exp).sum())} voxels differ"
+
+
+def test_voxelize_closed_mesh_with_extra_faces(vf, ctx):
+    # a closed vessel plus duplicated faces (even and odd edge multiplicities)
+    v, f = Vs.vessel_mesh(24, 18, 3)
+    mn, mx = Vs.mesh_aabb(v)
+    f2 = np.concatenate([f, f[:50], f[10:13]])
+    dims = Vs.grid_dims(mn, mx, 48)
+    g = vf.RegularGrid(dims, mn, mx, ctx)
+    g.fill(v, f2)
+    assert np.array_equal(g.data(), O.voxelize(v, f2, dims, mn, mx))
+
+
 def test_voxelize_anisotropic_cells(vf, ctx):
     v, f = Vs.vessel_mesh(40, 30, 9)
     mn, mx = Vs.mesh_aabb(v)

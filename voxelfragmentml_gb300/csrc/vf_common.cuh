@@ -59,9 +59,12 @@ struct JobDesc {
   uint32_t nverts, nfaces;
   uint32_t face_base;   // first global face index of this job
   float amin[3], amax[3];
-  float4* tets;         // 3 float4 per face: (Ax,Ay,Az,Bx) (By,Bz,Cx,Cy) (Cz,Dx,Dy,Dz)
-  uint32_t* tet_range;  // s0 | s1 << 16 (s1 < s0: no slice)
+  float4* tets;         // 3 float4 per face: its vertices in NDC sorted by y,
+                        // (P0x,P0y,P0z,P1x) (P1y,P1z,P2x,P2y) (P2z,-,-,-)
+  uint32_t* tet_range;  // first slice plane crossing the face (s0 | s1 << 16)
   float* ys;            // Y slice planes
+  unsigned long long* etab;  // edge parity table: key lo << 32 | hi, bit 63 = odd
+  uint32_t ecap;             // slots (power of two, >= 4 * nfaces)
   // seeds
   uint32_t* seeds;      // xyzw, capacity seeds_cap
   uint32_t seeds_cap;

@@ -9,8 +9,9 @@
 namespace vfk {
 
 // ---- voxelizer (Tetravoxelizer + tri-box SAT) ----
-// flattened (tetrahedron, slice) work list: per-face pair counts and their
-// exclusive prefix sums over the faces of all jobs
+// flattened per-face work list (parity: slice planes crossing the face;
+// shell: candidate columns): per-face counts and their exclusive prefix sums
+// over the faces of all jobs
 struct FaceScratch {
   uint32_t* pcnt;                // [total_faces]
   unsigned long long* pbase;     // [total_faces]
@@ -20,8 +21,8 @@ struct FaceScratch {
 void centroid_and_slices(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs);
 void tetra_prep(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs,
                 uint32_t total_faces, const FaceScratch& fs);
-void parity_raster(cudaStream_t st, const JobDesc* dj, int njobs, uint32_t total_faces,
-                   const FaceScratch& fs, int num_sms);
+void parity_raster(cudaStream_t st, const JobDesc* dj, const JobState* ds, int njobs,
+                   uint32_t total_faces, const FaceScratch& fs, int num_sms);
 // reuses the face scratch after the parity raster (counts, scan, runs)
 void shell_sat(cudaStream_t st, const JobDesc* dj, int njobs, uint32_t total_faces,
                const FaceScratch& fs, int num_sms);

@@ -82,7 +82,7 @@ vf_status Batch::init(Ctx* c, bool own) {
 void Batch::release() {
   if (!ctx) return;
   for (DevBuf* b : {&grid0, &grid1, &keys, &par, &tets, &range, &ys, &seeds, &counts, &lat,
-                    &verts, &faces, &emask, &tables, &state, &brick_job, &live, &list, &lcount,
+                    &verts, &faces, &emask, &etab, &tables, &state, &brick_job, &live, &list, &lcount,
                     &q[0], &q[1], &q[2], &scal, &epoch, &front[0], &front[1], &pcnt, &pbase,
                     &psums})
     ctx->free_buf(*b);
@@ -195,13 +195,21 @@ static vf_status check_params(const vf_params& p, uint32_t& ek) {
   return VF_OK;
 }
 
+// slots of a job's edge parity table: a power of two >= 4 * nfaces (load
+// <= 0.75 for a triangle soup, <= 0.375 for a closed mesh)
+static uint32_t edge_slots(uint32_t nfaces) {
+  uint64_t c = 64;
+  while (c < 4ull * nfaces) c <<= 1;
+  return (uint32_t)std::min<uint64_t>(c, 1ull << 31);
+}
+
 size_t job_footprint(const vf_job& j) {
   uint32_t d[3] = {j.dims[0], j.dims[1], j.dims[2]};
   if (!d[0] && !d[1] && !d[2]) d[0] = d[1] = d[2] = j.max_dim;
   const size_t X = d[0], Y = d[1], Z = d[2];
   const size_t Zp = vf_roundup((uint32_t)Z, 8), Zk = vf_roundup((uint32_t)Z, 4), Zw = (Z + 31) / 32;
   size_t b = X * Y * Zp * 2 * 2 + X * Y * Zw * 4 * 2 + (size_t)j.nfaces * (48 + 4 + 12) +
-             (size_t)j.nverts * 12 + 65536;
+             (size_t)edge_slots(j.nfaces) * 8 + (size_t)j.nverts * 12 + 65536;
   if (j.params.algorithm == VF_FLOOD) b += X * Y * Zk * 4;
   return b;
 }
@@ -218,6 +226,8 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
     if (s) return fail(s, "job " + std::to_string(i) + ": " + last_error());
     if (j.nfaces && (!j.verts || !j.faces || !j.nverts))
       return fail(VF_ERR_INVALID, "job " + std::to_string(i) + ": mesh pointers missing");
+    if (j.nverts >= 0x80000000u || j.nfaces >= 0x20000000u)
+      return fail(VF_ERR_RANGE, "job " + std::to_string(i) + ": at most 2^31 - 1 vertices and 2^29 - 1 faces");
     bool aabb_given = false;
     for (int a = 0; a < 3; ++a) aabb_given |= j.aabb_min[a] != j.aabb_max[a];
     if (aabb_given) {
@@ -259,6 +269,8 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
     p.o_par = sz.par; sz.par += align_up(vox * p.Zw, 64);
     p.o_tets = sz.tets; sz.tets += align_up((size_t)j.nfaces * 3, 16);
     p.o_range = sz.range; sz.range += align_up(j.nfaces, 64);
+    p.ecap = j.nfaces ? edge_slots(j.nfaces) : 0u;
+    p.o_etab = sz.etab; sz.etab += p.ecap;
     p.o_ys = sz.ys; sz.ys += align_up(p.Y, 64);
     p.o_seeds = sz.seeds; sz.seeds += align_up(4 * (size_t)p.seeds_cap, 64);
     p.o_counts = sz.counts; sz.counts += align_up(p.ncounts, 64);
@@ -280,6 +292,7 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
   ALLOC(par, std::max<size_t>(sz.par * 8, 256));  // par + shell
   ALLOC(tets, std::max<size_t>(sz.tets * 16, 256));
   ALLOC(range, std::max<size_t>(sz.range * 4, 256));
+  ALLOC(etab, std::max<size_t>(sz.etab * 8, 256));
   ALLOC(ys, std::max<size_t>(sz.ys * 4, 256));
   ALLOC(seeds, std::max<size_t>(sz.seeds * 4, 256));
   ALLOC(counts, std::max<size_t>(sz.counts * 4, 256));
@@ -339,6 +352,8 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
     for (int a = 0; a < 3; ++a) { d.amin[a] = p.amin[a]; d.amax[a] = p.amax[a]; }
     d.tets = static_cast<float4*>(tets.p) + p.o_tets;
     d.tet_range = static_cast<uint32_t*>(range.p) + p.o_range;
+    d.etab = static_cast<unsigned long long*>(etab.p) + p.o_etab;
+    d.ecap = p.ecap;
     d.ys = static_cast<float*>(ys.p) + p.o_ys;
     d.seeds = static_cast<uint32_t*>(seeds.p) + p.o_seeds;
     d.seeds_cap = p.seeds_cap;
@@ -444,7 +459,10 @@ static vf_status reset_scratch(Batch& B) {
   const uint32_t n = (uint32_t)B.jobs.size();
   cudaStream_t st = B.stream;
   VF_CK(cudaMemsetAsync(B.state.p, 0, sizeof(JobState) * n, st));
-  if (B.stages & ST_VOX) VF_CK(cudaMemsetAsync(B.par.p, 0, B.sz.par * 8, st));
+  if (B.stages & ST_VOX) {
+    VF_CK(cudaMemsetAsync(B.par.p, 0, B.sz.par * 8, st));
+    VF_CK(cudaMemsetAsync(B.etab.p, 0xFF, B.sz.etab * 8, st));  // every slot empty
+  }
   VF_CK(cudaMemsetAsync(B.counts.p, 0, B.sz.counts * 4, st));
   VF_CK(cudaMemsetAsync(B.scal.p, 0, 4096, st));
   uint32_t maxb = 1;
@@ -474,7 +492,7 @@ static void voxelize_stages(Batch& B, const std::function<void(int)>& mark) {
   vfk::centroid_and_slices(st, tv, ds, n);
   vfk::tetra_prep(st, tv, ds, n, B.sz.faces_total, fsc);
   mark(2);
-  vfk::parity_raster(st, tv, n, B.sz.faces_total, fsc, B.ctx->num_sms);
+  vfk::parity_raster(st, tv, ds, n, B.sz.faces_total, fsc, B.ctx->num_sms);
   mark(3);
   vfk::shell_sat(st, tv, n, B.sz.faces_total, fsc, B.ctx->num_sms);
   mark(4);
@@ -482,7 +500,7 @@ static void voxelize_stages(Batch& B, const std::function<void(int)>& mark) {
                static_cast<uint8_t*>(B.live.p), 1);
   vfk::compact_live(st, static_cast<uint8_t*>(B.live.p), B.sz.bricks,
                     static_cast<uint32_t*>(B.list.p), static_cast<uint32_t*>(B.lcount.p));
-  B.launches += 14;
+  B.launches += 16;
 }
 
 static vfk::FloodScratch flood_scratch(Batch& B) {

@@ -29,8 +29,8 @@ struct JobPlan {
   uint32_t X, Y, Z, Zp, Zk, Zw, nbx, nby, nbz, nbricks;
   float amin[3], amax[3];
   size_t o_grid, o_keys, o_par, o_tets, o_range, o_ys, o_seeds, o_counts, o_lat, o_verts,
-      o_faces, o_emask;
-  uint32_t ncounts, seeds_cap, lat_nx, lat_ny, lat_nz, ek;
+      o_faces, o_emask, o_etab;
+  uint32_t ecap, ncounts, seeds_cap, lat_nx, lat_ny, lat_nz, ek;
   float elimit;
   std::vector<float> emask;
   int final_cur;
@@ -39,7 +39,7 @@ struct JobPlan {
 
 struct Sizes {
   size_t grid = 0, keys = 0, par = 0, tets = 0, range = 0, ys = 0, seeds = 0, counts = 0,
-         lat = 0, verts = 0, faces = 0, emask = 0;
+         lat = 0, verts = 0, faces = 0, emask = 0, etab = 0;
   uint32_t bricks = 0, faces_total = 0, max_iters = 0;
 };
 
@@ -56,6 +56,7 @@ struct Batch {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   DevBuf grid0, grid1, keys, par, tets, range, ys, seeds, counts, lat, verts, faces, emask;
+  DevBuf etab;  // mesh edge parity tables (voxelizer)
   DevBuf tables, state, brick_job, live, list, lcount, q[3], scal, epoch, front[2];
   DevBuf pcnt, pbase, psums;  // flattened (tetrahedron, slice) work list
   void* h_tables = nullptr;  // pinned staging

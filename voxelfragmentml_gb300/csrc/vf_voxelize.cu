@@ -7,15 +7,19 @@
 // Stages, all batched over every job of a batch:
 //   centroid_and_slices : one 1024-thread block per job; fixed-order
 //                         lane sums of the vertices + the slice planes
-//   tetra_prep          : one thread per face -> tetrahedron (face + centroid)
-//                         in NDC, vertices sorted by y, slice range
-//   parity_raster       : (tetrahedron, slice) pairs flattened by a prefix
-//                         sum over the faces; each thread rasterises a run
-//                         of 64 pairs (cross-section triangles, exact integer
-//                         edge functions, XOR into bit planes)
+//   tetra_prep          : one thread per face -> its vertices in NDC sorted
+//                         by y, the slice planes crossing it, one use of each
+//                         edge in the job's edge parity table
+//   parity_raster       : the tetra-parity fill computed from edge crossings
+//                         (derivation above k_tetra): (face, slice) segments
+//                         flattened by a prefix sum over the faces and run in
+//                         warp-interleaved runs, the internal faces of edges
+//                         used an odd number of times, then a prefix XOR
+//                         along x turns the per-row crossing markers into the
+//                         parity plane
 //   shell_sat           : per-face work items (columns of the triangle's
-//                         footprint) flattened by a prefix sum; each thread
-//                         tests a run of 16 items with the exact SAT
+//                         footprint) flattened by a prefix sum; warps test
+//                         runs of items with the exact SAT
 //   combine             : one CTA per brick; bit planes -> uint16 0/1 rows,
 //                         brick liveness
 // All float arithmetic uses the _rn intrinsics (and the file is compiled
@@ -88,6 +92,61 @@ __device__ __forceinline__ uint32_t upper_bound_f(const float* a, uint32_t n, fl
   return lo;
 }
 
+// ---- parity by edge crossings ---------------------------------------------
+// The reference rasterises, for every slice plane, the cross-section of every
+// tetrahedron (face + centroid) with XOR at pixel centres (GL rules: 8
+// sub-pixel bits, top-left ownership of samples on edges).  With that rule a
+// sample p is inside a cross-section triangle exactly when the point
+// p + (e, e^2) (e -> 0) is inside the open triangle, and that point lies on
+// no edge and no vertex line.  A ray from it towards -x therefore crosses the
+// triangle's boundary an odd number of times exactly when p is inside; for a
+// zero-area triangle (never rasterised) the crossings are even.  Hence the
+// XOR of all rasterised triangles at p is the parity of the number of
+// cross-section EDGES that the ray crosses, and an edge's crossing depends
+// only on its two snapped end points:
+//   edge (u, v), u.z < v.z (fixed point), crosses at pixel centre
+//   p = (256 i + 128, 256 k + 128)  iff  u.z <= p.z < v.z  and
+//   (v.x - u.x)(p.z - u.z) - (v.z - u.z)(p.x - u.x) <= 0.
+// Each cross-section edge lies on one face of its tetrahedron and its end
+// points are INTERP on two tetrahedron edges (lower-y vertex first).  An
+// internal face (mesh edge + centroid) is shared by every tetrahedron whose
+// mesh face holds that edge, and each computes the same end points, so the
+// copies cancel in pairs: only the mesh faces' own segments and the internal
+// faces of mesh edges used an odd number of times (open or non-manifold
+// meshes) contribute.  Per segment and pixel row the first crossed pixel
+// gets a marker bit; a prefix XOR along x then yields the parity plane.
+// The quad split's diagonal belongs to both of its triangles and cancels.
+
+// slot value of an edge parity table: lo << 32 | hi (lo < hi < 2^31), bit 63
+// toggled once per use of the edge; an empty slot is all ones
+#define VF_EDGE_EMPTY 0xFFFFFFFFFFFFFFFFull
+#define VF_EDGE_ODD 0x8000000000000000ull
+
+__device__ __forceinline__ void edge_use(const JobDesc& J, uint32_t a, uint32_t b) {
+  if (a == b) return;  // a degenerate edge bounds a zero-area face: no crossing
+  const unsigned long long key =
+      a < b ? ((unsigned long long)a << 32 | b) : ((unsigned long long)b << 32 | a);
+  const uint32_t mask = J.ecap - 1;
+  uint32_t h = (uint32_t)vf_mix64(key) & mask;
+  for (uint32_t probe = 0; probe < J.ecap; ++probe) {
+    const unsigned long long old = atomicCAS(J.etab + h, VF_EDGE_EMPTY, key);
+    if (old == VF_EDGE_EMPTY || (old & ~VF_EDGE_ODD) == key) {
+      atomicXor(J.etab + h, VF_EDGE_ODD);
+      return;
+    }
+    h = (h + 1) & mask;
+  }
+}
+
+__device__ __forceinline__ void sort3_y(tv* v) {
+  tv t;
+#define SW(a, b) if (v[a].y > v[b].y) { t = v[a]; v[a] = v[b]; v[b] = t; }
+  SW(0, 1) SW(1, 2) SW(0, 1)
+#undef SW
+}
+
+// per face: NDC vertices sorted by y, the slice planes crossing the face
+// (P0.y < ys[s] <= P2.y), and one use of each of its edges
 __global__ void k_tetra(const JobDesc* jobs, JobState* st, int njobs, uint32_t total,
                         uint32_t* pcnt) {
   for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total;
@@ -95,8 +154,9 @@ __global__ void k_tetra(const JobDesc* jobs, JobState* st, int njobs, uint32_t t
     const int j = job_of_face(jobs, njobs, g);
     const JobDesc& J = jobs[j];
     const uint32_t f = g - J.face_base;
-    const uint32_t* fi = J.faces + 3 * (size_t)f;
-    if (fi[0] >= J.nverts || fi[1] >= J.nverts || fi[2] >= J.nverts) {
+    const uint32_t i0 = J.faces[3 * (size_t)f], i1 = J.faces[3 * (size_t)f + 1],
+                   i2 = J.faces[3 * (size_t)f + 2];
+    if (i0 >= J.nverts || i1 >= J.nverts || i2 >= J.nverts) {
       atomicOr(&st[j].err, VF_JERR_INVALID);  // bad face: never dereferenced
       J.tet_range[f] = 0xFFFFu;
       pcnt[g] = 0;
@@ -107,27 +167,26 @@ __global__ void k_tetra(const JobDesc* jobs, JobState* st, int njobs, uint32_t t
       ctr[a] = __fmul_rn(0.5f, __fadd_rn(J.amin[a], J.amax[a]));
       dim[a] = __fsub_rn(J.amax[a], J.amin[a]);
     }
-    tv v[4];
-    for (int k = 0; k < 3; ++k) v[k] = to_ndc(J.verts + 3 * (size_t)J.faces[3 * (size_t)f + k], ctr, dim);
-    v[3] = to_ndc(st[j].centroid, ctr, dim);
-    // sort4Vec3ByLowerY (Tetravoxelizer.h:75-81)
-    tv t;
-#define SW(a, b) if (v[a].y > v[b].y) { t = v[a]; v[a] = v[b]; v[b] = t; }
-    SW(0, 1) SW(2, 3) SW(0, 2) SW(1, 3) SW(1, 2)
-#undef SW
+    tv v[3];
+    v[0] = to_ndc(J.verts + 3 * (size_t)i0, ctr, dim);
+    v[1] = to_ndc(J.verts + 3 * (size_t)i1, ctr, dim);
+    v[2] = to_ndc(J.verts + 3 * (size_t)i2, ctr, dim);
+    sort3_y(v);
     float4* o = J.tets + 3 * (size_t)f;
     o[0] = make_float4(v[0].x, v[0].y, v[0].z, v[1].x);
     o[1] = make_float4(v[1].y, v[1].z, v[2].x, v[2].y);
-    o[2] = make_float4(v[2].z, v[3].x, v[3].y, v[3].z);
-    // slices with A.y < ys[s] <= D.y
-    uint32_t s0 = upper_bound_f(J.ys, J.Y, v[0].y);
-    uint32_t s1e = upper_bound_f(J.ys, J.Y, v[3].y);
-    J.tet_range[f] = (s1e > s0) ? (s0 | ((s1e - 1) << 16)) : 0xFFFFu;  // s0=0xFFFF,s1=0: none
-    pcnt[g] = s1e > s0 ? s1e - s0 : 0u;  // (tetrahedron, slice) pairs of this face
+    o[2] = make_float4(v[2].z, 0.0f, 0.0f, 0.0f);
+    const uint32_t s0 = upper_bound_f(J.ys, J.Y, v[0].y);
+    const uint32_t s1e = upper_bound_f(J.ys, J.Y, v[2].y);
+    J.tet_range[f] = (s1e > s0) ? (s0 | ((s1e - 1) << 16)) : 0xFFFFu;
+    pcnt[g] = s1e > s0 ? s1e - s0 : 0u;  // (face, slice) items
+    edge_use(J, i0, i1);
+    edge_use(J, i1, i2);
+    edge_use(J, i2, i0);
   }
 }
 
-// ---- exact raster (see the oracle for the rule) ---------------------------
+// ---- exact segment arithmetic (INTERP and the raster rule of the oracle) ---
 __device__ __forceinline__ float interp_c(float a, float b, float t) {
   return __fadd_rn(__fmul_rn(a, __fsub_rn(1.0f, t)), __fmul_rn(b, t));
 }
@@ -140,129 +199,48 @@ __device__ __forceinline__ int32_t to_fixed(float ndc, float half) {
   float w = __fadd_rn(__fmul_rn(ndc, half), half);
   return __float2int_rn(__fmul_rn(w, 256.0f));
 }
-__device__ __forceinline__ long long edge_fn(int ax, int az, int bx, int bz, long long px,
-                                             long long pz) {
-  return (long long)(bx - ax) * (pz - az) - (long long)(bz - az) * (px - ax);
+__device__ __forceinline__ int ceil_div_i(int a, int b) {  // b > 0
+  return a >= 0 ? (a + b - 1) / b : -((-a) / b);
 }
-__device__ __forceinline__ int owns_edge(int ax, int az, int bx, int bz) {
-  int dz = bz - az, dx = bx - ax;
-  return (dz < 0) || (dz == 0 && dx > 0);
+__device__ __forceinline__ long long ceil_div_ll(long long a, long long b) {  // b > 0
+  return a >= 0 ? (a + b - 1) / b : -((-a) / b);
 }
 
-// Narrow [lo, hi] (k' in [0, nk]) to the k' with q + k' * sk > 0.
-__device__ __forceinline__ void span_bound(long long q, long long sk, int nk, int& lo, int& hi) {
-  if (sk == 0) {
-    if (q <= 0) { lo = 1; hi = 0; }
-    return;
-  }
-  if (sk > 0) {  // increasing in k': smallest k' with a positive value
-    int k = 0;
-    if (q <= 0) {
-      const float est = __fdividef((float)(-q), (float)sk) + 1.0f;
-      k = (int)fminf(fmaxf(floorf(est), 0.0f), (float)(nk + 1));
-    }
-    while (k <= nk && q + (long long)k * sk <= 0) ++k;
-    while (k > 0 && q + (long long)(k - 1) * sk > 0) --k;
-    lo = max(lo, k);
-  } else {       // decreasing in k': largest k' with a positive value
-    if (q <= 0) { lo = 1; hi = 0; return; }
-    const float est = __fdividef((float)q, (float)(-sk));
-    int k = (int)fminf(fmaxf(floorf(est), -1.0f), (float)nk);
-    while (k >= 0 && q + (long long)k * sk <= 0) --k;
-    while (k < nk && q + (long long)(k + 1) * sk > 0) ++k;
-    hi = min(hi, k);
-  }
-}
-
-// Rasterise one cross-section triangle (NDC x,z) into the bit planes of
-// `slice` with XOR.  Same rule as the oracle: vertices snapped to 1/256 pixel,
-// pixel centres tested with exact integer edge functions, a sample exactly
-// on an edge belongs to the triangle for which it is a top-left edge.  With
-// integer E, "E > 0 || (E == 0 && owns)" is "E + owns > 0".
-__device__ void raster_xor(const JobDesc& J, uint32_t slice, float ax, float az, float bx,
-                           float bz, float cx, float cz) {
-  const float hw = __fmul_rn(0.5f, (float)J.X), hh = __fmul_rn(0.5f, (float)J.Z);
-  int x0 = to_fixed(ax, hw), z0 = to_fixed(az, hh);
-  int x1 = to_fixed(bx, hw), z1 = to_fixed(bz, hh);
-  int x2 = to_fixed(cx, hw), z2 = to_fixed(cz, hh);
-  const int mnx = min(x0, min(x1, x2)), mxx = max(x0, max(x1, x2));
-  const int mnz = min(z0, min(z1, z2)), mxz = max(z0, max(z1, z2));
-  // pixel centres 256*i + 128 inside [mn, mx] (fixed point)
-  const int ilo = max((mnx + 127) >> 8, 0), ihi = min((mxx - 128) >> 8, (int)J.X - 1);
-  const int klo = max((mnz + 127) >> 8, 0), khi = min((mxz - 128) >> 8, (int)J.Z - 1);
-  if (ilo > ihi || klo > khi) return;
-  const long long area = edge_fn(x0, z0, x1, z1, x2, z2);
-  if (area == 0) return;
-  if (area < 0) { int tx = x1, tz = z1; x1 = x2; z1 = z2; x2 = tx; z2 = tz; }
-  const long long b0 = owns_edge(x0, z0, x1, z1), b1 = owns_edge(x1, z1, x2, z2),
-                  b2 = owns_edge(x2, z2, x0, z0);
-  const long long px0 = (long long)ilo * 256 + 128, pz0 = (long long)klo * 256 + 128;
-  // edge values (+ tie bias) at the first pixel centre; steps per k and per i
-  const long long r0 = edge_fn(x0, z0, x1, z1, px0, pz0) + b0;
-  const long long r1 = edge_fn(x1, z1, x2, z2, px0, pz0) + b1;
-  const long long r2 = edge_fn(x2, z2, x0, z0, px0, pz0) + b2;
-  const long long sk0 = 256LL * (x1 - x0), sk1 = 256LL * (x2 - x1), sk2 = 256LL * (x0 - x2);
-  const long long si0 = -256LL * (z1 - z0), si1 = -256LL * (z2 - z1), si2 = -256LL * (z0 - z2);
-  uint32_t* const col = J.par + (size_t)slice * J.Zw;  // + i * Y * Zw per pixel column
+// markers of one snapped segment in the parity plane of `slice`: per pixel
+// row k it crosses, the first pixel column i whose centre the -x ray from
+// (centre + (e, e^2)) sees the segment from
+__device__ void segment_markers(const JobDesc& J, uint32_t slice, int ax, int az, int bx, int bz) {
+  if (az == bz) return;  // horizontal: the ray at z + e^2 never meets it
+  int ux = ax, uz = az, vx = bx, vz = bz;
+  if (uz > vz) { ux = bx; uz = bz; vx = ax; vz = az; }
+  const int klo = max(ceil_div_i(uz - 128, 256), 0);
+  const int khi = min(ceil_div_i(vz - 128, 256) - 1, (int)J.Z - 1);
+  if (klo > khi) return;
+  const long long dz = vz - uz, dx = vx - ux;
+  const long long den = 256 * dz;
+  uint32_t* const col = J.par + (size_t)slice * J.Zw;
   const size_t istride = (size_t)J.Y * J.Zw;
-  if (ihi - ilo <= 1 && khi - klo <= 1) {
-    // <= 2x2 candidate pixels (almost every cross-section): no loops
-#pragma unroll
-    for (int di = 0; di < 2; ++di) {
-      if (ilo + di > ihi) break;
-      const long long e0 = r0 + di * si0, e1 = r1 + di * si1, e2 = r2 + di * si2;
-      const bool in0 = (e0 > 0) & (e1 > 0) & (e2 > 0);
-      const bool in1 = (klo + 1 <= khi) & (e0 + sk0 > 0) & (e1 + sk1 > 0) & (e2 + sk2 > 0);
-      uint32_t* row = col + (size_t)(ilo + di) * istride;
-      const uint32_t w0 = (uint32_t)klo >> 5, w1 = (uint32_t)(klo + 1) >> 5;
-      const uint32_t m0 = in0 ? 1u << (klo & 31) : 0u, m1 = in1 ? 1u << ((klo + 1) & 31) : 0u;
-      if (w0 == w1) {
-        if (m0 | m1) atomicXor(row + w0, m0 | m1);
-      } else {
-        if (m0) atomicXor(row + w0, m0);
-        if (m1) atomicXor(row + w1, m1);
-      }
-    }
-    return;
-  }
-  // span path: for pixel column i the covered k form one interval (the
-  // triangle is convex); each edge bounds it from one side.  The bound is
-  // estimated with a float division and then fixed with exact integer edge
-  // values, so the covered set is exactly the per-pixel test's.
-  const int nk = khi - klo;
-  long long q0 = r0, q1 = r1, q2 = r2;
-  for (int i = ilo; i <= ihi; ++i, q0 += si0, q1 += si1, q2 += si2) {
-    int lo = 0, hi = nk;
-    span_bound(q0, sk0, nk, lo, hi);
-    span_bound(q1, sk1, nk, lo, hi);
-    span_bound(q2, sk2, nk, lo, hi);
-    if (lo > hi) continue;
-    uint32_t* row = col + (size_t)i * istride;
-    const int ka = klo + lo, kb = klo + hi;
-    for (int w = ka >> 5; w <= (kb >> 5); ++w) {
-      const int a = max(ka, w << 5) & 31, b = min(kb, (w << 5) + 31) & 31;
-      const uint32_t m = (b == 31 ? 0xFFFFFFFFu : ((2u << b) - 1u)) & ~((1u << a) - 1u);
-      atomicXor(row + w, m);
-    }
+  for (int k = klo; k <= khi; ++k) {
+    // pixel centre x >= u.x + dx (pz - u.z) / dz
+    const long long num = dz * ux + dx * ((long long)k * 256 + 128 - uz) - 128 * dz;
+    long long i = ceil_div_ll(num, den);
+    if (i < 0) i = 0;
+    if (i >= (long long)J.X) continue;
+    atomicXor(col + (size_t)i * istride + (k >> 5), 1u << (k & 31));
   }
 }
 
-// one (tetrahedron, slice) pair: the 1-2 cross-section triangles
-// (Tetravoxelizer.cpp:59-89; endpoint choice without divergent branches)
-__device__ __forceinline__ void cross_section(const JobDesc& J, const tv& A, const tv& B,
-                                              const tv& Cc, const tv& D, uint32_t s) {
+// the segment of triangle P (sorted by y, P0.y < sl <= P2.y) in plane sl:
+// INTERP on P0-P2 and on P0-P1 or P1-P2 (Tetravoxelizer.cpp:45-89)
+__device__ __forceinline__ void face_segment(const JobDesc& J, const tv& P0, const tv& P1,
+                                             const tv& P2, uint32_t s) {
   const float sl = J.ys[s];
-  float p0x, p0z, v1x, v1z, v2x, v2z;
-  interp(A, D, sl, p0x, p0z);
-  const bool ab = sl <= B.y, ac = sl <= Cc.y;
-  interp(ab ? A : B, ab ? B : D, sl, v1x, v1z);
-  interp(ac ? A : Cc, ac ? Cc : D, sl, v2x, v2z);
-  raster_xor(J, s, p0x, p0z, v1x, v1z, v2x, v2z);
-  if (B.y < sl && sl <= Cc.y) {
-    float bx, bz;
-    interp(B, Cc, sl, bx, bz);
-    raster_xor(J, s, bx, bz, v2x, v2z, v1x, v1z);
-  }
+  float ax, az, bx, bz;
+  interp(P0, P2, sl, ax, az);
+  const bool lo = sl <= P1.y;
+  interp(lo ? P0 : P1, lo ? P1 : P2, sl, bx, bz);
+  const float hw = __fmul_rn(0.5f, (float)J.X), hh = __fmul_rn(0.5f, (float)J.Z);
+  segment_markers(J, s, to_fixed(ax, hw), to_fixed(az, hh), to_fixed(bx, hw), to_fixed(bz, hh));
 }
 
 // ---- exclusive scan of the per-face pair counts (1024 faces per block) -----
@@ -340,11 +318,11 @@ __device__ __forceinline__ uint32_t face_of_item(const unsigned long long* base,
   return lo;
 }
 
-__global__ void __launch_bounds__(256, 4) k_parity_flat(const JobDesc* jobs, int njobs,
-                                                     const uint32_t* pcnt,
-                                                     const unsigned long long* pbase,
-                                                     const unsigned long long* ptotal,
-                                                     uint32_t total_faces) {
+__global__ void __launch_bounds__(256) k_parity_flat(const JobDesc* jobs, int njobs,
+                                                  const uint32_t* pcnt,
+                                                  const unsigned long long* pbase,
+                                                  const unsigned long long* ptotal,
+                                                  uint32_t total_faces) {
   const unsigned long long total = *ptotal;
   const int lane = threadIdx.x & 31;
   const unsigned long long nwruns = (total + WARP_RUN - 1) / WARP_RUN;
@@ -357,10 +335,10 @@ __global__ void __launch_bounds__(256, 4) k_parity_flat(const JobDesc* jobs, int
     if (lane == 0) g = face_of_item(pbase, total_faces, base);
     g = __shfl_sync(0xFFFFFFFFu, g, 0);
     uint32_t cached = 0xFFFFFFFFu;
-    tv A, B, Cc, D;
+    tv P0, P1, P2;
     const JobDesc* J = nullptr;
     uint32_t s0 = 0;
-    unsigned long long fb = 0, fe = 0;
+    unsigned long long fb = 0;
     for (unsigned long long p = base + lane; p < end; p += 32) {
       // advance the face cursor (faces with no item have pbase equal to the next)
       while (p >= pbase[g] + pcnt[g]) ++g;
@@ -370,16 +348,69 @@ __global__ void __launch_bounds__(256, 4) k_parity_flat(const JobDesc* jobs, int
         const uint32_t f = g - J->face_base;
         const float4* o = J->tets + 3 * (size_t)f;
         const float4 q0 = o[0], q1 = o[1], q2 = o[2];
-        A = {q0.x, q0.y, q0.z};
-        B = {q0.w, q1.x, q1.y};
-        Cc = {q1.z, q1.w, q2.x};
-        D = {q2.y, q2.z, q2.w};
+        P0 = {q0.x, q0.y, q0.z};
+        P1 = {q0.w, q1.x, q1.y};
+        P2 = {q1.z, q1.w, q2.x};
         s0 = J->tet_range[f] & 0xFFFFu;
         fb = pbase[g];
-        fe = fb + pcnt[g];
       }
-      (void)fe;
-      cross_section(*J, A, B, Cc, D, s0 + (uint32_t)(p - fb));
+      face_segment(*J, P0, P1, P2, s0 + (uint32_t)(p - fb));
+    }
+  }
+}
+
+// internal faces (mesh edge + centroid) of the edges used an odd number of
+// times: one warp per table word of 32 slots, lanes over the slice planes
+__global__ void __launch_bounds__(256) k_odd_edges(const JobDesc* jobs, const JobState* st,
+                                                   int njobs) {
+  const int lane = threadIdx.x & 31;
+  for (int j = blockIdx.y; j < njobs; j += gridDim.y) {
+    const JobDesc& J = jobs[j];
+    if (!J.nfaces || !J.ecap) continue;
+    float ctr[3], dim[3];
+    for (int a = 0; a < 3; ++a) {
+      ctr[a] = __fmul_rn(0.5f, __fadd_rn(J.amin[a], J.amax[a]));
+      dim[a] = __fsub_rn(J.amax[a], J.amin[a]);
+    }
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < J.ecap / 32;
+         w += (gridDim.x * blockDim.x) >> 5) {
+      const unsigned long long v = J.etab[w * 32 + lane];
+      unsigned m = __ballot_sync(0xFFFFFFFFu, v != VF_EDGE_EMPTY && (v & VF_EDGE_ODD));
+      while (m) {
+        const int src = __ffs(m) - 1;
+        m &= m - 1;
+        const unsigned long long key = __shfl_sync(0xFFFFFFFFu, v, src) & ~VF_EDGE_ODD;
+        tv p[3];
+        p[0] = to_ndc(J.verts + 3 * (size_t)(uint32_t)(key >> 32), ctr, dim);
+        p[1] = to_ndc(J.verts + 3 * (size_t)(uint32_t)key, ctr, dim);
+        p[2] = to_ndc(st[j].centroid, ctr, dim);
+        sort3_y(p);
+        const uint32_t s0 = upper_bound_f(J.ys, J.Y, p[0].y);
+        const uint32_t s1e = upper_bound_f(J.ys, J.Y, p[2].y);
+        for (uint32_t s = s0 + lane; s < s1e; s += 32) face_segment(J, p[0], p[1], p[2], s);
+      }
+    }
+  }
+}
+
+// markers -> parity: prefix XOR along x of every (y, z-word) column
+__global__ void __launch_bounds__(256) k_prefix_x(const JobDesc* jobs, int njobs) {
+  for (int j = blockIdx.y; j < njobs; j += gridDim.y) {
+    const JobDesc& J = jobs[j];
+    if (!J.nfaces) continue;
+    const uint32_t cols = J.Y * J.Zw;
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x) {
+      uint32_t* p = J.par + c;
+      uint32_t run = 0;
+      uint32_t x = 0;
+      for (; x + 8 <= J.X; x += 8) {
+        uint32_t w[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) w[q] = p[(size_t)(x + q) * cols];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) { run ^= w[q]; p[(size_t)(x + q) * cols] = run; }
+      }
+      for (; x < J.X; ++x) { run ^= p[(size_t)x * cols]; p[(size_t)x * cols] = run; }
     }
   }
 }
@@ -721,14 +752,19 @@ void tetra_prep(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs,
   if (total_faces)
     k_tetra<<<grid_for(total_faces, 256, 65535), 256, 0, st>>>(dj, ds, njobs, total_faces, fs.pcnt);
 }
-void parity_raster(cudaStream_t st, const JobDesc* dj, int njobs, uint32_t total_faces,
-                   const FaceScratch& fs, int num_sms) {
+void parity_raster(cudaStream_t st, const JobDesc* dj, const JobState* ds, int njobs,
+                   uint32_t total_faces, const FaceScratch& fs, int num_sms) {
   if (!total_faces) return;
   const uint32_t nb = (total_faces + 1023) / 1024;
   k_scan_local<<<nb, 1024, 0, st>>>(fs.pcnt, fs.pbase, fs.psums, total_faces);
   k_scan_sums<<<1, 1024, 0, st>>>(fs.psums, nb, fs.ptotal);
   k_scan_add<<<(total_faces + 255) / 256, 256, 0, st>>>(fs.pbase, fs.psums, total_faces);
   k_parity_flat<<<num_sms * 16, 256, 0, st>>>(dj, njobs, fs.pcnt, fs.pbase, fs.ptotal, total_faces);
+  const unsigned gy = (unsigned)(njobs < 65535 ? njobs : 65535);
+  k_odd_edges<<<dim3(num_sms, gy), 256, 0, st>>>(dj, ds, njobs);
+  int px = num_sms * 8 / njobs;
+  px = px < 1 ? 1 : (px > 64 ? 64 : px);
+  k_prefix_x<<<dim3(px, gy), 256, 0, st>>>(dj, njobs);
 }
 void shell_sat(cudaStream_t st, const JobDesc* dj, int njobs, uint32_t total_faces,
                const FaceScratch& fs, int num_sms) {
