@@ -85,6 +85,22 @@ def test_voxelize_open_and_degenerate_meshes(vf, ctx, seed):
     assert np.array_equal(got, exp), f"{int((got != exp).sum())} voxels differ"
 
 
+@pytest.mark.parametrize("scale,offset", [(1.0, (1000.0, -500.0, 2000.0)), (1e-3, (0.0, 0.0, 0.0)),
+                                          (250.0, (-3.0e4, 1.0e4, 7.0)), (1.0, (0.3, 0.1, -0.2))])
+def test_voxelize_offset_and_scaled_meshes(vf, ctx, scale, offset):
+    # large coordinates against small cells: float rounding in the SAT is a
+    # sizeable fraction of a cell, so candidate pruning must not drop a cell
+    v, f = Vs.vessel_mesh(48, 36, 11)
+    v = (v.astype(np.float64) * scale + np.array(offset)).astype(np.float32)
+    mn, mx = Vs.mesh_aabb(v)
+    dims = Vs.grid_dims(mn, mx, 64)
+    g = vf.RegularGrid(dims, mn, mx, ctx)
+    g.fill(v, f)
+    got = g.data()
+    exp = O.voxelize(v, f, dims, mn, mx)
+    assert np.array_equal(got, exp), f"{int((got != exp).sum())} voxels differ"
+
+
 def test_voxelize_closed_mesh_with_extra_faces(vf, ctx):
     # a closed vessel plus duplicated faces (even and odd edge multiplicities)
     v, f = Vs.vessel_mesh(24, 18, 3)

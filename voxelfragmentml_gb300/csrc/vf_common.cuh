@@ -59,6 +59,8 @@ struct JobDesc {
   uint32_t nverts, nfaces;
   uint32_t face_base;   // first global face index of this job
   float amin[3], amax[3];
+  float cs[3];          // cell size (amax - amin) / dims, IEEE division on the host
+  float ics[3];         // 1 / cs (approximate: candidate bounds only)
   float4* tets;         // 3 float4 per face: its vertices in NDC sorted by y,
                         // (P0x,P0y,P0z,P1x) (P1y,P1z,P2x,P2y) (P2z,-,-,-)
   uint32_t* tet_range;  // first slice plane crossing the face (s0 | s1 << 16)

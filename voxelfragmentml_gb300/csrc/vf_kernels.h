@@ -17,6 +17,7 @@ struct FaceScratch {
   unsigned long long* pbase;     // [total_faces]
   unsigned long long* psums;     // [ceil(total_faces / 1024)]
   unsigned long long* ptotal;    // [1]
+  float4* srec;                  // [6 * total_faces] per-face shell setup
 };
 void centroid_and_slices(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs);
 void tetra_prep(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs,

@@ -84,7 +84,7 @@ void Batch::release() {
   for (DevBuf* b : {&grid0, &grid1, &keys, &par, &tets, &range, &ys, &seeds, &counts, &lat,
                     &verts, &faces, &emask, &etab, &tables, &state, &brick_job, &live, &list, &lcount,
                     &q[0], &q[1], &q[2], &scal, &epoch, &front[0], &front[1], &pcnt, &pbase,
-                    &psums})
+                    &psums, &srec})
     ctx->free_buf(*b);
   if (h_tables) cudaFreeHost(h_tables);
   if (h_state) cudaFreeHost(h_state);
@@ -315,6 +315,7 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
   ALLOC(pcnt, nf * 4);
   ALLOC(pbase, nf * 8);
   ALLOC(psums, ((nf + 1023) / 1024 + 1) * 8);
+  ALLOC(srec, nf * 96);
 #undef ALLOC
   const size_t tbytes = sizeof(JobDesc) * ntables * std::max<size_t>(n, 1) + sz.emask * 4 + 256;
   if (tbytes > h_tables_cap) {
@@ -350,6 +351,14 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
     d.faces = static_cast<uint32_t*>(faces.p) + p.o_faces;
     d.nverts = j.nverts; d.nfaces = j.nfaces; d.face_base = face_base;
     for (int a = 0; a < 3; ++a) { d.amin[a] = p.amin[a]; d.amax[a] = p.amax[a]; }
+    {
+      const uint32_t dd[3] = {p.X, p.Y, p.Z};
+      for (int a = 0; a < 3; ++a) {
+        const float size = p.amax[a] - p.amin[a];  // RegularGrid.cpp:426-441
+        d.cs[a] = size / (float)dd[a];
+        d.ics[a] = 1.0f / d.cs[a];
+      }
+    }
     d.tets = static_cast<float4*>(tets.p) + p.o_tets;
     d.tet_range = static_cast<uint32_t*>(range.p) + p.o_range;
     d.etab = static_cast<unsigned long long*>(etab.p) + p.o_etab;
@@ -489,6 +498,7 @@ static void voxelize_stages(Batch& B, const std::function<void(int)>& mark) {
   fsc.pbase = static_cast<unsigned long long*>(B.pbase.p);
   fsc.psums = static_cast<unsigned long long*>(B.psums.p);
   fsc.ptotal = static_cast<unsigned long long*>(B.scal.p) + 256;  // bytes 2048..2055
+  fsc.srec = static_cast<float4*>(B.srec.p);
   vfk::centroid_and_slices(st, tv, ds, n);
   vfk::tetra_prep(st, tv, ds, n, B.sz.faces_total, fsc);
   mark(2);

@@ -58,7 +58,7 @@ struct Batch {
   DevBuf grid0, grid1, keys, par, tets, range, ys, seeds, counts, lat, verts, faces, emask;
   DevBuf etab;  // mesh edge parity tables (voxelizer)
   DevBuf tables, state, brick_job, live, list, lcount, q[3], scal, epoch, front[2];
-  DevBuf pcnt, pbase, psums;  // flattened (tetrahedron, slice) work list
+  DevBuf pcnt, pbase, psums, srec;  // flattened per-face work lists, shell setup
   void* h_tables = nullptr;  // pinned staging
   size_t h_tables_cap = 0;
   JobState* h_state = nullptr;  // pinned

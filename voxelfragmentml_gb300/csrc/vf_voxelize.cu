@@ -511,8 +511,9 @@ __device__ __forceinline__ void test_cell(const JobDesc& J, const float* cs, con
   tv bmin = {ADD(J.amin[0], MUL(cs[0], (float)i)), ADD(J.amin[1], MUL(cs[1], (float)jj)),
              ADD(J.amin[2], MUL(cs[2], (float)k))};
   tv bmax = {ADD(bmin.x, cs[0]), ADD(bmin.y, cs[1]), ADD(bmin.z, cs[2])};
-  tv ce = {__fdiv_rn(ADD(bmax.x, bmin.x), 2.0f), __fdiv_rn(ADD(bmax.y, bmin.y), 2.0f),
-           __fdiv_rn(ADD(bmax.z, bmin.z), 2.0f)};
+  // (max + min) / 2: x * 0.5 and x / 2 are the same correctly rounded value
+  tv ce = {MUL(ADD(bmax.x, bmin.x), 0.5f), MUL(ADD(bmax.y, bmin.y), 0.5f),
+           MUL(ADD(bmax.z, bmin.z), 0.5f)};
   tv r = {SUB(bmax.x, ce.x), SUB(bmax.y, ce.y), SUB(bmax.z, ce.z)};
   if (tri_box(p0, p1, p2, ce, r))
     atomicOr(J.shell + ((size_t)i * J.Y + jj) * J.Zw + (k >> 5), 1u << (k & 31));
@@ -520,117 +521,203 @@ __device__ __forceinline__ void test_cell(const JobDesc& J, const float* cs, con
 
 // Per-face setup of the shell test.  Candidates: the triangle's cell bbox
 // grown by one cell.  Pruning: two of the SAT's own separating axes are
-// evaluated early with a margin of a quarter cell -- (1) the triangle's
-// projection on the plane orthogonal to its dominant normal axis c against
-// each column's square (the edge x c axes and the a, b box axes), (2) the
-// plane slab along c (the plane-box test).  A dropped box is separated by at
-// least 0.25 cell along a SAT axis, far beyond float rounding, so the exact
-// SAT would reject it too: the marked set equals testing the full bbox.
+// evaluated early with a margin -- (1) the triangle's projection on the
+// plane orthogonal to its dominant normal axis c against each column's
+// square (the edge x c axes), (2) the plane slab along c (the plane-box
+// test).  A dropped box is separated along a SAT axis by more than the
+// margin (2% of a cell + 64 ulp of the largest coordinate), far beyond the
+// rounding of the float SAT, so the exact test would reject it too: the
+// marked set equals testing the full bbox.
 // Work items: columns (a, b) when pruning, else every bbox cell.
 struct ShellSetup {
-  float cs[3], q0[3], nr[3], Pa[3], Pb[3];
-  float ha, hb, w;
-  tv p0, p1, p2;
-  int lo[3], n[3];
-  int c, ax, bx;
+  float cs[3];                 // cell size (x, y, z)
+  tv p0, p1, p2;               // the triangle
+  // pruning, in the axes (a, b, c) = (c+1, c+2, c) mod 3; without pruning
+  // (a, b, c) = (x, y, z) and every bbox cell is an item
+  float amin_a, amin_b, amin_c, cs_a, cs_b, q0_a, q0_b, q0_c, nr_a, nr_b;
+  float Pa1, Pb1, Pa2, Pb2;    // projected triangle relative to p0 (ccw)
+  float ha, hb, w, inr, ics;
+  int lo_a, lo_b, lo_c, n_b, n_c, hi_c;
+  int c;
   bool prune;
   uint32_t items;
 };
 
 __device__ bool shell_setup(const JobDesc& J, uint32_t f, ShellSetup& S) {
   const uint32_t dims[3] = {J.X, J.Y, J.Z};
-  for (int a = 0; a < 3; ++a) S.cs[a] = __fdiv_rn(SUB(J.amax[a], J.amin[a]), (float)dims[a]);
+  for (int a = 0; a < 3; ++a) S.cs[a] = J.cs[a];
   const uint32_t* fi = J.faces + 3 * (size_t)f;
   if (fi[0] >= J.nverts || fi[1] >= J.nverts || fi[2] >= J.nverts) return false;
   const float* q0 = J.verts + 3 * (size_t)fi[0];
   const float* q1 = J.verts + 3 * (size_t)fi[1];
   const float* q2 = J.verts + 3 * (size_t)fi[2];
+  int lo[3], n[3];
   for (int a = 0; a < 3; ++a) {
     float mn, mx;
     mm3(q0[a], q1[a], q2[a], mn, mx);
-    S.lo[a] = vf_clampi(float_cell(__fdiv_rn(SUB(mn, J.amin[a]), S.cs[a]), dims[a]) - 1, 0, dims[a] - 1);
-    const int hi = vf_clampi(float_cell(__fdiv_rn(SUB(mx, J.amin[a]), S.cs[a]), dims[a]) + 1, 0, dims[a] - 1);
-    S.n[a] = hi - S.lo[a] + 1;
-    S.q0[a] = q0[a];
+    // one cell of margin on each side: far above the reciprocal's rounding
+    lo[a] = vf_clampi(float_cell(SUB(mn, J.amin[a]) * J.ics[a], dims[a]) - 1, 0, dims[a] - 1);
+    const int hi = vf_clampi(float_cell(SUB(mx, J.amin[a]) * J.ics[a], dims[a]) + 1, 0, dims[a] - 1);
+    n[a] = hi - lo[a] + 1;
   }
   S.p0 = {q0[0], q0[1], q0[2]};
   S.p1 = {q1[0], q1[1], q1[2]};
   S.p2 = {q2[0], q2[1], q2[2]};
   const float e1[3] = {q1[0] - q0[0], q1[1] - q0[1], q1[2] - q0[2]};
   const float e2[3] = {q2[0] - q0[0], q2[1] - q0[1], q2[2] - q0[2]};
-  S.nr[0] = e1[1] * e2[2] - e1[2] * e2[1];
-  S.nr[1] = e1[2] * e2[0] - e1[0] * e2[2];
-  S.nr[2] = e1[0] * e2[1] - e1[1] * e2[0];
-  int c = 0;
-  if (fabsf(S.nr[1]) > fabsf(S.nr[c])) c = 1;
-  if (fabsf(S.nr[2]) > fabsf(S.nr[c])) c = 2;
-  S.c = c;
-  S.ax = (c + 1) % 3;
-  S.bx = (c + 2) % 3;
+  const float nr[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                       e1[0] * e2[1] - e1[1] * e2[0]};
+  int c = fabsf(nr[1]) > fabsf(nr[0]) ? 1 : 0;
+  if (fabsf(nr[2]) > fabsf(c ? nr[1] : nr[0])) c = 2;
   const float e1n = fabsf(e1[0]) + fabsf(e1[1]) + fabsf(e1[2]);
   const float e2n = fabsf(e2[0]) + fabsf(e2[1]) + fabsf(e2[2]);
-  S.prune = fabsf(S.nr[c]) > 1e-3f * e1n * e2n && fabsf(S.nr[c]) > 0.0f;
+  const float nrc_abs = fabsf(c == 0 ? nr[0] : (c == 1 ? nr[1] : nr[2]));
+  S.prune = nrc_abs > 1e-3f * e1n * e2n && nrc_abs > 0.0f;
   if (!S.prune) {
-    S.items = (uint32_t)(S.n[0] * S.n[1] * S.n[2]);
+    S.c = 2;
+    S.lo_a = lo[0]; S.lo_b = lo[1]; S.lo_c = lo[2];
+    S.n_b = n[1]; S.n_c = n[2]; S.hi_c = lo[2] + n[2] - 1;
+    S.nr_a = S.nr_b = S.inr = S.Pa1 = S.Pb1 = S.Pa2 = S.Pb2 = S.ha = S.hb = S.w = 0.0f;
+    S.items = (uint32_t)(n[0] * n[1] * n[2]);
     return true;
   }
-  // projected triangle (relative to q0), counter-clockwise
-  float P1a = e1[S.ax], P1b = e1[S.bx], P2a = e2[S.ax], P2b = e2[S.bx];
-  if (S.nr[c] < 0.0f) { float t = P1a; P1a = P2a; P2a = t; t = P1b; P1b = P2b; P2b = t; }
-  S.Pa[0] = 0.0f; S.Pa[1] = P1a; S.Pa[2] = P2a;
-  S.Pb[0] = 0.0f; S.Pb[1] = P1b; S.Pb[2] = P2b;
-  S.ha = 0.75f * S.cs[S.ax];  // half cell + quarter-cell margin
-  S.hb = 0.75f * S.cs[S.bx];
-  const float hc = 0.75f * S.cs[c];
-  S.w = hc + fabsf(S.nr[S.ax]) / fabsf(S.nr[c]) * S.ha + fabsf(S.nr[S.bx]) / fabsf(S.nr[c]) * S.hb;
-  S.items = (uint32_t)(S.n[S.ax] * S.n[S.bx]);
+  const int ax = (c + 1) % 3, bx = (c + 2) % 3;
+  // register selects instead of dynamic indexing (keeps the arrays out of
+  // local memory)
+#define SEL(v, i) ((i) == 0 ? (v)[0] : ((i) == 1 ? (v)[1] : (v)[2]))
+  S.c = c;
+  S.lo_a = SEL(lo, ax); S.lo_b = SEL(lo, bx); S.lo_c = SEL(lo, c);
+  const int n_a = SEL(n, ax);
+  S.n_b = SEL(n, bx); S.n_c = SEL(n, c); S.hi_c = S.lo_c + S.n_c - 1;
+  S.amin_a = SEL(J.amin, ax); S.amin_b = SEL(J.amin, bx); S.amin_c = SEL(J.amin, c);
+  S.cs_a = SEL(S.cs, ax); S.cs_b = SEL(S.cs, bx);
+  const float cs_c = SEL(S.cs, c);
+  S.q0_a = SEL(q0, ax); S.q0_b = SEL(q0, bx); S.q0_c = SEL(q0, c);
+  S.nr_a = SEL(nr, ax); S.nr_b = SEL(nr, bx);
+  const float nr_c = SEL(nr, c);
+  float P1a = SEL(e1, ax), P1b = SEL(e1, bx), P2a = SEL(e2, ax), P2b = SEL(e2, bx);
+#define SEL2(v, i) ((i) == 0 ? (v)[0] : ((i) == 1 ? (v)[1] : (v)[2]))
+#undef SEL
+  if (nr_c < 0.0f) { float t = P1a; P1a = P2a; P2a = t; t = P1b; P1b = P2b; P2b = t; }
+  S.Pa1 = P1a; S.Pb1 = P1b; S.Pa2 = P2a; S.Pb2 = P2b;
+  // half cell + margin.  The margin (2% of a cell + 64 ulp of the largest
+  // coordinate in play) is far above the rounding of the exact float SAT and
+  // of these bounds, so no cell the exact test accepts is dropped.
+  float M = 0.0f;
+  for (int a = 0; a < 3; ++a) {
+    M = fmaxf(M, fmaxf(fabsf(J.amin[a]), fabsf(J.amax[a])));
+    M = fmaxf(M, fmaxf(fabsf(q0[a]), fmaxf(fabsf(q1[a]), fabsf(q2[a]))));
+  }
+  const float ulp64 = M * 7.62939453125e-6f;  // 64 * 2^-23 * M
+  S.ha = 0.52f * S.cs_a + ulp64;
+  S.hb = 0.52f * S.cs_b + ulp64;
+  const float hc = 0.52f * cs_c + ulp64;
+  S.inr = __frcp_rn(nr_c);
+  S.w = hc + (fabsf(S.nr_a) * S.ha + fabsf(S.nr_b) * S.hb) * fabsf(S.inr);
+  S.ics = SEL2(J.ics, c);
+#undef SEL2
+  S.items = (uint32_t)(n_a * S.n_b);
   return true;
 }
 
-__device__ void shell_item(const JobDesc& J, const ShellSetup& S, uint32_t q) {
+__device__ __forceinline__ bool edge_keeps(float x0, float y0, float x1, float y1, float ca,
+                                           float cb, float ha, float hb) {
+  const float dx = x1 - x0, dy = y1 - y0;
+  const float E = dx * (cb - y0) - dy * (ca - x0);
+  return E + fabsf(dx) * hb + fabsf(dy) * ha >= 0.0f;
+}
+
+// the candidate cells of work item q: column (ia, ib) along c, cells
+// klo .. klo + n - 1 (n = 0: the column is pruned).  Items of a face without
+// pruning are single cells (ia, ib, klo) = (i, j, k) with c = z.
+__device__ __forceinline__ void shell_column(const ShellSetup& S, uint32_t q, int& ia, int& ib,
+                                             int& klo, int& n) {
+  n = 0;
   if (!S.prune) {
-    const int k = S.lo[2] + (int)(q % S.n[2]);
-    const int jj = S.lo[1] + (int)((q / S.n[2]) % S.n[1]);
-    const int i = S.lo[0] + (int)(q / (S.n[2] * S.n[1]));
-    test_cell(J, S.cs, S.p0, S.p1, S.p2, i, jj, k);
+    klo = S.lo_c + (int)(q % S.n_c);
+    ib = S.lo_b + (int)((q / S.n_c) % S.n_b);
+    ia = S.lo_a + (int)(q / (S.n_c * S.n_b));
+    n = 1;
     return;
   }
-  const int ax = S.ax, bx = S.bx, c = S.c;
-  const int ia = S.lo[ax] + (int)(q / S.n[bx]), ib = S.lo[bx] + (int)(q % S.n[bx]);
-  const float ca = (J.amin[ax] + S.cs[ax] * ((float)ia + 0.5f)) - S.q0[ax];
-  const float cb = (J.amin[bx] + S.cs[bx] * ((float)ib + 0.5f)) - S.q0[bx];
-#pragma unroll
-  for (int e = 0; e < 3; ++e) {
-    const int f2 = (e + 1) % 3;
-    const float dx = S.Pa[f2] - S.Pa[e], dy = S.Pb[f2] - S.Pb[e];
-    const float E = dx * (cb - S.Pb[e]) - dy * (ca - S.Pa[e]);
-    if (E + fabsf(dx) * S.hb + fabsf(dy) * S.ha < 0.0f) return;
-  }
-  const float tc = S.q0[c] - (S.nr[ax] * ca + S.nr[bx] * cb) / S.nr[c];
-  const int klo = max(S.lo[c], (int)floorf((tc - S.w - J.amin[c]) / S.cs[c] - 0.5f));
-  const int khi = min(S.lo[c] + S.n[c] - 1, (int)ceilf((tc + S.w - J.amin[c]) / S.cs[c] - 0.5f));
-  for (int k = klo; k <= khi; ++k) {
-    int idx[3];
-    idx[ax] = ia;
-    idx[bx] = ib;
-    idx[c] = k;
-    test_cell(J, S.cs, S.p0, S.p1, S.p2, idx[0], idx[1], idx[2]);
-  }
+  ia = S.lo_a + (int)(q / S.n_b);
+  ib = S.lo_b + (int)(q % S.n_b);
+  const float ca = (S.amin_a + S.cs_a * ((float)ia + 0.5f)) - S.q0_a;
+  const float cb = (S.amin_b + S.cs_b * ((float)ib + 0.5f)) - S.q0_b;
+  if (!edge_keeps(0.0f, 0.0f, S.Pa1, S.Pb1, ca, cb, S.ha, S.hb)) return;
+  if (!edge_keeps(S.Pa1, S.Pb1, S.Pa2, S.Pb2, ca, cb, S.ha, S.hb)) return;
+  if (!edge_keeps(S.Pa2, S.Pb2, 0.0f, 0.0f, ca, cb, S.ha, S.hb)) return;
+  // slab bounds (conservative: the margin is far above these roundings)
+  const float tc = S.q0_c - (S.nr_a * ca + S.nr_b * cb) * S.inr;
+  // cells whose centre is within w of the plane along c
+  klo = max(S.lo_c, (int)ceilf((tc - S.w - S.amin_c) * S.ics - 0.5f));
+  const int khi = min(S.hi_c, (int)floorf((tc + S.w - S.amin_c) * S.ics - 0.5f));
+  n = max(khi - klo + 1, 0);
 }
 
-__global__ void k_shell_count(const JobDesc* jobs, int njobs, uint32_t total, uint32_t* scnt) {
+// Per-face setup packed into 6 float4 (computed once per face here, then
+// read by every lane that takes an item of the face):
+//   (p0.xyz, p1.x) (p1.yz, p2.xy) (p2.z, nr_a, nr_b, 1/nr_c) (Pa1, Pb1, Pa2, Pb2)
+//   (ha, hb, w, job) (c | prune << 2, lo_a | lo_b << 16, lo_c | hi_c << 16, n_b | n_c << 16)
+__global__ void k_shell_count(const JobDesc* jobs, int njobs, uint32_t total, uint32_t* scnt,
+                              float4* srec) {
   for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
-    const JobDesc& J = jobs[job_of_face(jobs, njobs, g)];
+    const int j = job_of_face(jobs, njobs, g);
+    const JobDesc& J = jobs[j];
     ShellSetup S;
-    scnt[g] = shell_setup(J, g - J.face_base, S) ? S.items : 0u;
+    if (!shell_setup(J, g - J.face_base, S)) {
+      scnt[g] = 0u;
+      continue;
+    }
+    scnt[g] = S.items;
+    float4* r = srec + 6 * (size_t)g;
+    r[0] = make_float4(S.p0.x, S.p0.y, S.p0.z, S.p1.x);
+    r[1] = make_float4(S.p1.y, S.p1.z, S.p2.x, S.p2.y);
+    r[2] = make_float4(S.p2.z, S.nr_a, S.nr_b, S.inr);
+    r[3] = make_float4(S.Pa1, S.Pb1, S.Pa2, S.Pb2);
+    r[4] = make_float4(S.ha, S.hb, S.w, __int_as_float(j));
+    r[5] = make_float4(__int_as_float(S.c | (S.prune ? 4 : 0)), __int_as_float(S.lo_a | (S.lo_b << 16)),
+                       __int_as_float(S.lo_c | (S.hi_c << 16)), __int_as_float(S.n_b | (S.n_c << 16)));
   }
 }
 
-__global__ void __launch_bounds__(256) k_shell_flat(const JobDesc* jobs, int njobs,
-                                                    const uint32_t* scnt,
-                                                    const unsigned long long* sbase,
-                                                    const unsigned long long* stotal,
-                                                    uint32_t total_faces) {
+__device__ __forceinline__ int shell_unpack(const JobDesc* jobs, const float4* rec, ShellSetup& S) {
+  const float4 r0 = rec[0], r1 = rec[1], r2 = rec[2], r3 = rec[3], r4 = rec[4], r5 = rec[5];
+  S.p0 = {r0.x, r0.y, r0.z};
+  S.p1 = {r0.w, r1.x, r1.y};
+  S.p2 = {r1.z, r1.w, r2.x};
+  S.nr_a = r2.y; S.nr_b = r2.z; S.inr = r2.w;
+  S.Pa1 = r3.x; S.Pb1 = r3.y; S.Pa2 = r3.z; S.Pb2 = r3.w;
+  S.ha = r4.x; S.hb = r4.y; S.w = r4.z;
+  const int j = __float_as_int(r4.w);
+  const int cp = __float_as_int(r5.x), lab = __float_as_int(r5.y), lch = __float_as_int(r5.z),
+            nbc = __float_as_int(r5.w);
+  S.c = cp & 3;
+  S.prune = (cp & 4) != 0;
+  S.lo_a = lab & 0xFFFF; S.lo_b = lab >> 16;
+  S.lo_c = lch & 0xFFFF; S.hi_c = lch >> 16;
+  S.n_b = nbc & 0xFFFF; S.n_c = nbc >> 16;
+  const JobDesc& J = jobs[j];
+  const int c = S.c, ax = c == 2 ? 0 : c + 1, bx = c == 0 ? 2 : (c == 1 ? 0 : 1);
+#define SEL(v, i) ((i) == 0 ? (v)[0] : ((i) == 1 ? (v)[1] : (v)[2]))
+  const float p0[3] = {S.p0.x, S.p0.y, S.p0.z};
+  S.cs[0] = J.cs[0]; S.cs[1] = J.cs[1]; S.cs[2] = J.cs[2];
+  S.amin_a = SEL(J.amin, ax); S.amin_b = SEL(J.amin, bx); S.amin_c = SEL(J.amin, c);
+  S.cs_a = SEL(J.cs, ax); S.cs_b = SEL(J.cs, bx);
+  S.ics = SEL(J.ics, c);
+  S.q0_a = SEL(p0, ax); S.q0_b = SEL(p0, bx); S.q0_c = SEL(p0, c);
+#undef SEL
+  return j;
+}
+
+// Warp-interleaved runs over the (face, column) items.  Each lane prunes its
+// column to a range of candidate cells; the cells of all 32 columns are then
+// dealt out to the lanes, one exact SAT per lane per round, so lanes with
+// pruned or short columns do not idle while others test.
+__global__ void __launch_bounds__(256, 3) k_shell_flat(const JobDesc* jobs, const uint32_t* scnt,
+                                                       const unsigned long long* sbase,
+                                                       const unsigned long long* stotal,
+                                                       uint32_t total_faces, const float4* srec) {
   const unsigned long long total = *stotal;
   const int lane = threadIdx.x & 31;
   const unsigned long long nwruns = (total + WARP_RUN - 1) / WARP_RUN;
@@ -644,17 +731,63 @@ __global__ void __launch_bounds__(256) k_shell_flat(const JobDesc* jobs, int njo
     g = __shfl_sync(0xFFFFFFFFu, g, 0);
     uint32_t cached = 0xFFFFFFFFu;
     ShellSetup S;
-    const JobDesc* J = nullptr;
+    S.c = 2;
+    S.p0 = S.p1 = S.p2 = {0.0f, 0.0f, 0.0f};
+    S.cs[0] = S.cs[1] = S.cs[2] = 0.0f;
+    int jidx = 0;
     unsigned long long fb = 0;
-    for (unsigned long long p = base + lane; p < end; p += 32) {
-      while (p >= sbase[g] + scnt[g]) ++g;
-      if (g != cached) {
-        cached = g;
-        J = &jobs[job_of_face(jobs, njobs, g)];
-        shell_setup(*J, g - J->face_base, S);
-        fb = sbase[g];
+    for (unsigned long long p0 = base; p0 < end; p0 += 32) {
+      const unsigned long long p = p0 + lane;
+      int ia = 0, ib = 0, klo = 0, n = 0;
+      if (p < end) {
+        while (p >= sbase[g] + scnt[g]) ++g;
+        if (g != cached) {
+          cached = g;
+          jidx = shell_unpack(jobs, srec + 6 * (size_t)g, S);
+          fb = sbase[g];
+        }
+        shell_column(S, (uint32_t)(p - fb), ia, ib, klo, n);
       }
-      shell_item(*J, S, (uint32_t)(p - fb));
+      // exclusive scan of the lanes' cell counts
+      int incl = n;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      const int ncells = __shfl_sync(0xFFFFFFFFu, incl, 31);
+      const int excl = incl - n;
+      for (int t0 = 0; t0 < ncells; t0 += 32) {
+        const int t = t0 + lane;
+        // owner: the last lane whose first cell is <= t
+        int src = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+          const int e = __shfl_sync(0xFFFFFFFFu, excl, src + step);
+          if (e <= t) src += step;
+        }
+        const tv q0 = {__shfl_sync(0xFFFFFFFFu, S.p0.x, src), __shfl_sync(0xFFFFFFFFu, S.p0.y, src),
+                       __shfl_sync(0xFFFFFFFFu, S.p0.z, src)};
+        const tv q1 = {__shfl_sync(0xFFFFFFFFu, S.p1.x, src), __shfl_sync(0xFFFFFFFFu, S.p1.y, src),
+                       __shfl_sync(0xFFFFFFFFu, S.p1.z, src)};
+        const tv q2 = {__shfl_sync(0xFFFFFFFFu, S.p2.x, src), __shfl_sync(0xFFFFFFFFu, S.p2.y, src),
+                       __shfl_sync(0xFFFFFFFFu, S.p2.z, src)};
+        const float cs[3] = {__shfl_sync(0xFFFFFFFFu, S.cs[0], src),
+                             __shfl_sync(0xFFFFFFFFu, S.cs[1], src),
+                             __shfl_sync(0xFFFFFFFFu, S.cs[2], src)};
+        const int sj = __shfl_sync(0xFFFFFFFFu, jidx, src);
+        const int sc = __shfl_sync(0xFFFFFFFFu, S.c, src);
+        const int sa = __shfl_sync(0xFFFFFFFFu, ia, src);
+        const int sb = __shfl_sync(0xFFFFFFFFu, ib, src);
+        const int sk = __shfl_sync(0xFFFFFFFFu, klo, src) + t - __shfl_sync(0xFFFFFFFFu, excl, src);
+        if (t < ncells) {
+          // (a, b, c) -> (x, y, z): c = 0: (k, a, b); c = 1: (b, k, a); c = 2: (a, b, k)
+          const int x = sc == 0 ? sk : (sc == 1 ? sb : sa);
+          const int y = sc == 0 ? sa : (sc == 1 ? sk : sb);
+          const int z = sc == 0 ? sb : (sc == 1 ? sa : sk);
+          test_cell(jobs[sj], cs, q0, q1, q2, x, y, z);
+        }
+      }
     }
   }
 }
@@ -770,11 +903,12 @@ void shell_sat(cudaStream_t st, const JobDesc* dj, int njobs, uint32_t total_fac
                const FaceScratch& fs, int num_sms) {
   if (!total_faces) return;
   const uint32_t nb = (total_faces + 1023) / 1024;
-  k_shell_count<<<grid_for(total_faces, 256, 65535), 256, 0, st>>>(dj, njobs, total_faces, fs.pcnt);
+  k_shell_count<<<grid_for(total_faces, 256, 65535), 256, 0, st>>>(dj, njobs, total_faces, fs.pcnt,
+                                                                   fs.srec);
   k_scan_local<<<nb, 1024, 0, st>>>(fs.pcnt, fs.pbase, fs.psums, total_faces);
   k_scan_sums<<<1, 1024, 0, st>>>(fs.psums, nb, fs.ptotal);
   k_scan_add<<<(total_faces + 255) / 256, 256, 0, st>>>(fs.pbase, fs.psums, total_faces);
-  k_shell_flat<<<num_sms * 16, 256, 0, st>>>(dj, njobs, fs.pcnt, fs.pbase, fs.ptotal, total_faces);
+  k_shell_flat<<<num_sms * 12, 256, 0, st>>>(dj, fs.pcnt, fs.pbase, fs.ptotal, total_faces, fs.srec);
 }
 void combine(cudaStream_t st, const JobDesc* dj, const uint32_t* brick_job,
              uint32_t total_bricks, uint8_t* live, int dual) {
