@@ -235,6 +235,7 @@ def main():
     ctx.synchronize()
     L.vf_ctx_event_record(ctx.h, 0)
     launches, flood_ms, flood_bytes, visits, passes, sweeps, maxit = 0, 0.0, 0, 0, 0, 0, 0
+    act_rows, key_changes = 0, 0
     stage_tot = {}
     for _ in range(args.steps):
         rb.execute(download=False)
@@ -246,6 +247,8 @@ def main():
         passes += st["flood_passes"]
         sweeps += st["flood_sweeps"]
         maxit += st["flood_maxit_hits"]
+        act_rows += st["flood_active_row_sweeps"]
+        key_changes += st["flood_key_changes"]
         for k, v in ctx.stage_ms().items():
             stage_tot[k] = stage_tot.get(k, 0.0) + v
     L.vf_ctx_event_record(ctx.h, 1)
@@ -325,6 +328,8 @@ def main():
             "passes_per_launch": passes / args.steps,
             "sweeps_per_visit": sweeps / max(visits, 1),
             "visits_at_sweep_cap": maxit / args.steps,
+            "active_rows_per_sweep": act_rows / max(sweeps, 1),
+            "key_changes_per_visit": key_changes / max(visits, 1),
             "launch_ms": flood_launch_ms,
             "traffic": (traffic or {}).get("bytes_per_launch_scaled")}
     line = {"metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world,

@@ -124,6 +124,7 @@ EXPORTS = {
     "vf_batch_execute": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "vf_ctx_stage_ms": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_ctx_flood_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vf_ctx_flood_counters": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_server_create": (C.c_int, [C.c_void_p, C.c_size_t, C.c_uint32, C.c_uint32, C.c_void_p]),
     "vf_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "vf_server_poll": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int]),
@@ -206,9 +207,12 @@ class Context:
         _check(lib().vf_ctx_last_stats(self.h, C.byref(la), C.byref(ms), C.byref(by), C.byref(vis)))
         pa, sw, mh = C.c_uint64(), C.c_uint64(), C.c_uint64()
         _check(lib().vf_ctx_flood_stats(self.h, C.byref(pa), C.byref(sw), C.byref(mh)))
+        cn = (C.c_uint64 * 8)()
+        _check(lib().vf_ctx_flood_counters(self.h, cn, 8))
         return {"launches": la.value, "flood_ms": ms.value, "flood_bytes": by.value,
                 "flood_visits": vis.value, "flood_passes": pa.value, "flood_sweeps": sw.value,
-                "flood_maxit_hits": mh.value}
+                "flood_maxit_hits": mh.value, "flood_active_row_sweeps": cn[6],
+                "flood_key_changes": cn[7]}
 
 
 _default_ctx = None

@@ -540,6 +540,13 @@ vf_status vf_ctx_flood_stats(vf_ctx* ctx, uint64_t* passes, uint64_t* sweeps, ui
   return VF_OK;
 }
 
+vf_status vf_ctx_flood_counters(vf_ctx* ctx, uint64_t* out, uint32_t n) {
+  if (!ctx || (n && !out)) return fail(VF_ERR_INVALID, "NULL argument");
+  for (uint32_t i = 0; i < n && i < 8; ++i) out[i] = ctx->c.last_flood_counters[i];
+  for (uint32_t i = 8; i < n; ++i) out[i] = 0;
+  return VF_OK;
+}
+
 vf_status vf_ctx_stage_ms(vf_ctx* ctx, float* ms, uint32_t n) {
   if (!ctx || (n && !ms)) return fail(VF_ERR_INVALID, "NULL argument");
   for (uint32_t i = 0; i < n && i < 11; ++i) ms[i] = ctx->c.last_stage_ms[i];

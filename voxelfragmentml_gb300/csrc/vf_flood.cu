@@ -127,7 +127,8 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
       l = a.live[brick_id(J, nx, ny, nz)];
     live27[t] = l;
   }
-  if (t == 0) { *dirs = 0; *reenq = 0; }
+  __shared__ uint32_t scnt[2];
+  if (t == 0) { *dirs = 0; *reenq = 0; scnt[0] = 0; scnt[1] = 0; }
   __syncthreads();
   // stage keys: rows [x0-1, x0+17) x [y0-1, y0+17), z [z0-4, z0+36)
   for (int q = t; q < KROWS * KZW; q += blockDim.x) {
@@ -153,7 +154,7 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     const uint4 w = *reinterpret_cast<const uint4*>(own_row + 4 + 4 * q);
     k[4 * q] = w.x; k[4 * q + 1] = w.y; k[4 * q + 2] = w.z; k[4 * q + 3] = w.w;
   }
-  uint32_t changed = 0, overflow = 0;
+  uint32_t changed = 0, overflow = 0, nact = 0, nchg = 0;
   // rflag[b][row]: the row changed in the previous sweep.  Every interior row
   // runs in sweep 0 (new halo data); later only rows next to a change run.
   for (int q = t; q < KROWS; q += blockDim.x) {
@@ -250,6 +251,8 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     rflag[(cur ^ 1) * KROWS + own] = chg != 0;
     changed |= chg;
     cur ^= 1;
+    if (active) ++nact;
+    nchg += __popc(chg);
     if (!__syncthreads_or(chg != 0)) break;
   }
   const int x = x0 + tx, y = y0 + ty;
@@ -288,12 +291,19 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     dm &= ~(1u << 13);  // self
     if (dm) atomicOr(dirs, dm);
   }
+  // statistics: active row-sweeps and key changes (block sums in shared memory)
+  if (nact) atomicAdd(&scnt[0], nact);
+  if (nchg) atomicAdd(&scnt[1], nchg);
   if (t == 0) {
     if (it == MAXIT) *reenq = 1;
     atomicAdd(a.stats + 4, (uint32_t)it + 1u);  // sweeps (statistics)
     if (it == MAXIT) atomicAdd(a.stats + 5, 1u);
   }
   __syncthreads();
+  if (t == 0) {
+    atomicAdd(a.stats + 6, scnt[0]);
+    atomicAdd(a.stats + 7, scnt[1]);
+  }
   if (t < 32) {
     const uint32_t dm = *dirs;
     bool want = false;

@@ -521,7 +521,8 @@ static vfk::FloodScratch flood_scratch(Batch& B) {
   fs.qhead = sc + 4;     // [3]
   fs.barrier = sc + 8;   // [2]
   fs.err = sc + 12;      // [1]
-  fs.stats = sc + 16;    // [8]: visits, passes, -, timeouts, sweeps, MAXIT hits
+  fs.stats = sc + 16;    // [8]: visits, passes, -, timeouts, sweeps, MAXIT hits,
+                         // active row-sweeps, changed voxels
   fs.epoch = static_cast<uint32_t*>(B.epoch.p);
   fs.max_passes = 1u << 20;
   fs.total_bricks = B.sz.bricks;
@@ -697,7 +698,9 @@ vf_status Batch::finish(vf_job_result* res) {
     ctx->last_flood_passes = h_scal[17];
     ctx->last_flood_sweeps = h_scal[20];
     ctx->last_flood_maxit = h_scal[21];
+    for (int i = 0; i < 8; ++i) ctx->last_flood_counters[i] = h_scal[16 + i];
   } else {
+    for (int i = 0; i < 8; ++i) ctx->last_flood_counters[i] = 0;
     ctx->last_flood_ms = 0.f;
     ctx->last_flood_visits = 0;
     ctx->last_flood_passes = 0;
