@@ -147,7 +147,7 @@ def reference_arm(args):
         return 0
     from voxelfragmentml_gb300 import workloads as W
     jobs = W.mixed(256)
-    sample = cpu_sample(jobs, args.cpu_stride)
+    sample = cpu_sample(jobs, args.ref_stride)
     meshes = {j["index"]: W.mesh_for(j) for j in sample}
     for _ in range(args.warmup):
         run_cpu(sample[:1], meshes)
@@ -159,7 +159,7 @@ def reference_arm(args):
     value = tot_v / tot_s
     cores = os.cpu_count()
     desc = (f"CPU oracle (restatement of the reference's flood/seed/voxelize/erode code; "
-            f"the reference is Windows+OpenGL only) on every {args.cpu_stride}th job of "
+            f"the reference is Windows+OpenGL only) on every {args.ref_stride}th job of "
             f"mixed-256 ({len(sample)} jobs, {tot_v // args.steps} voxels) per step")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "voxels/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -193,7 +193,10 @@ def main():
     ap.add_argument("--plain-jobs", type=int, default=32)
     ap.add_argument("--serve-rate", type=float, default=400.0)
     ap.add_argument("--serve-seconds", type=float, default=3.0)
-    ap.add_argument("--cpu-stride", type=int, default=16)
+    ap.add_argument("--cpu-stride", type=int, default=2,
+                    help="cpu_baseline sample: every n-th job of the workload (2: about 10-15 s)")
+    ap.add_argument("--ref-stride", type=int, default=4,
+                    help="--impl reference: every n-th job per step")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     args = ap.parse_args()

@@ -84,6 +84,10 @@ struct JobDesc {
   int32_t boundary_size;
   float* lattice;       // perturbation lattice values, 3 per point
   uint32_t lat_nx, lat_ny, lat_nz;
+  // label download: device-accessible destination (mapped pinned host memory
+  // or device memory; null = copy-engine download) and first global row
+  uint16_t* out;
+  unsigned long long row_base;
   // stage selection bits for the kernel that receives this table
   uint32_t active;
   float* emask;         // erosion mask (k^3 floats)

@@ -579,6 +579,36 @@ __global__ void __launch_bounds__(256) k_counts(const JobDesc* jobs, JobState* s
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// label download: one warp per (x, y) row, the final grid (row pitch Zp) into
+// the caller's buffer (row pitch Z); 8-byte stores when Z % 4 == 0 and the
+// destination is 8-byte aligned
+__global__ void __launch_bounds__(256) k_pack(const JobDesc* jobs, int njobs,
+                                              unsigned long long total_rows) {
+  const int lane = threadIdx.x & 31;
+  const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+  for (unsigned long long r = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+       r < total_rows; r += nw) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (jobs[mid].row_base <= r) lo = mid; else hi = mid - 1;
+    }
+    const JobDesc& J = jobs[lo];
+    if (!J.out) continue;
+    const unsigned long long lr = r - J.row_base;
+    const uint16_t* src = J.grid + lr * J.Zp;
+    uint16_t* dst = J.out + lr * J.Z;
+    if ((J.Z & 3u) == 0u && ((reinterpret_cast<uintptr_t>(J.out) & 7u) == 0u)) {
+      const uint2* s2 = reinterpret_cast<const uint2*>(src);
+      uint2* d2 = reinterpret_cast<uint2*>(dst);
+      for (uint32_t q = lane; q < J.Z / 4; q += 32) d2[q] = __ldcs(s2 + q);
+    } else {
+      for (uint32_t q = lane; q < J.Z; q += 32) dst[q] = src[q];
+    }
+  }
+}
 }  // namespace
 
 namespace vfk {
@@ -661,6 +691,11 @@ void remove_isolated(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
 void count_values(cudaStream_t st, const JobDesc* dj, JobState* ds, const uint32_t* list,
                   const uint32_t* count, uint32_t max_count, const uint32_t* brick_job) {
   if (max_count) k_counts<<<brick_grid(max_count), 256, 0, st>>>(dj, ds, list, count, brick_job);
+}
+
+void pack_labels(cudaStream_t st, const JobDesc* dj, int njobs, uint64_t total_rows, int num_sms) {
+  if (njobs > 0 && total_rows)
+    k_pack<<<num_sms * 8, 256, 0, st>>>(dj, njobs, (unsigned long long)total_rows);
 }
 
 }  // namespace vfk

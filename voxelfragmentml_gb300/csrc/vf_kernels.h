@@ -36,6 +36,10 @@ void mark_live(cudaStream_t st, const JobDesc* dj, const uint32_t* brick_job,
 void compact_live(cudaStream_t st, const uint8_t* live, uint32_t total_bricks,
                   uint32_t* list, uint32_t* count);
 
+// labels of every job with a device-accessible `out` (T_CNT table: the
+// final buffer) into `out`, rows of Z without the z padding
+void pack_labels(cudaStream_t st, const JobDesc* dj, int njobs, uint64_t total_rows, int num_sms);
+
 // ---- seeds ----
 void sample_seeds(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs);
 

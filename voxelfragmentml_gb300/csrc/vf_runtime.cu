@@ -382,6 +382,22 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
     d.emask = static_cast<float*>(emask.p) + p.o_emask;
     d.elimit = p.elimit;
     d.ek = (int32_t)p.ek;
+    // labels straight from the kernel into the caller's buffer when the GPU
+    // can address it (pinned host memory is mapped under unified addressing)
+    p.packed = false;
+    d.out = nullptr;
+    d.row_base = sz.rows;
+    sz.rows += (uint64_t)p.X * p.Y;
+    if (j.out_labels && ((uintptr_t)j.out_labels & 1) == 0) {
+      cudaPointerAttributes at;
+      if (cudaPointerGetAttributes(&at, j.out_labels) == cudaSuccess && at.devicePointer &&
+          at.type != cudaMemoryTypeUnregistered) {
+        d.out = static_cast<uint16_t*>(at.devicePointer);
+        p.packed = true;
+      } else {
+        cudaGetLastError();
+      }
+    }
     uint16_t* buf[2] = {g0, g1};
     int cur = 0;
     auto put = [&](uint32_t t, bool active, int src, int dst, int bs) {
@@ -638,13 +654,25 @@ vf_status Batch::enqueue_batched(bool do_upload, bool do_download) {
   mark(10);
   VF_CK(cudaGetLastError());
   // downloads
+  if ((stages & ST_DOWNLOAD) && do_download) {
+    bool any_packed = false;
+    for (uint32_t i = 0; i < n; ++i) any_packed |= plans[i].packed;
+    if (any_packed) {
+      vfk::pack_labels(st, dtable(T_CNT), (int)n, sz.rows, ctx->num_sms);
+      launches += 1;
+    }
+  }
   for (uint32_t i = 0; i < n && (stages & ST_DOWNLOAD) && do_download; ++i) {
     const vf_job& j = *jobs[i];
     const JobPlan& p = plans[i];
     const uint16_t* src = static_cast<uint16_t*>(p.final_cur ? grid1.p : grid0.p) + p.o_grid;
-    if (j.out_labels)
-      VF_CK(cudaMemcpy2DAsync(j.out_labels, (size_t)p.Z * 2, src, (size_t)p.Zp * 2, (size_t)p.Z * 2,
-                              (size_t)p.X * p.Y, cudaMemcpyDeviceToHost, st));
+    if (j.out_labels && !p.packed) {
+      if (p.Zp == p.Z)
+        VF_CK(cudaMemcpyAsync(j.out_labels, src, (size_t)p.X * p.Y * p.Z * 2, cudaMemcpyDeviceToHost, st));
+      else
+        VF_CK(cudaMemcpy2DAsync(j.out_labels, (size_t)p.Z * 2, src, (size_t)p.Zp * 2, (size_t)p.Z * 2,
+                                (size_t)p.X * p.Y, cudaMemcpyDeviceToHost, st));
+    }
     if (j.out_counts && j.ncounts)
       VF_CK(cudaMemcpyAsync(j.out_counts, static_cast<uint32_t*>(counts.p) + p.o_counts,
                             sizeof(uint32_t) * j.ncounts, cudaMemcpyDeviceToHost, st));

@@ -35,12 +35,14 @@ struct JobPlan {
   std::vector<float> emask;
   int final_cur;
   bool prefix_possible;
+  bool packed;  // labels written to out_labels by the pack kernel
 };
 
 struct Sizes {
   size_t grid = 0, keys = 0, par = 0, tets = 0, range = 0, ys = 0, seeds = 0, counts = 0,
          lat = 0, verts = 0, faces = 0, emask = 0, etab = 0;
   uint32_t bricks = 0, faces_total = 0, max_iters = 0;
+  uint64_t rows = 0;  // sum of X * Y over the jobs
 };
 
 struct Ctx;
