@@ -174,13 +174,11 @@ def reference_arm(args):
     return 0
 
 
-def _traffic():
-    """Per-launch DRAM bytes of the flood kernel from the committed ncu summary."""
-    try:
-        with open(os.path.join(ROOT, "profiles", "roofline_traffic.json")) as fh:
-            return json.load(fh)
-    except Exception:
-        return None
+# DRAM bytes per flood brick visit: dram__bytes_read.sum + dram__bytes_write.sum of
+# one k_relax launch over the first 48 jobs of mixed-256 (ncu, one GB300), divided
+# by that launch's 52557 brick visits.  The roofline's `traffic` is this figure
+# times the visits the timed launch made.
+K_RELAX_DRAM_BYTES_PER_VISIT = 2783539456 / 52557
 
 
 def main():
@@ -321,7 +319,6 @@ def main():
     flood_launch_ms = flood_ms / args.steps
     flood_launch_bytes = flood_bytes / args.steps
     achieved = (flood_launch_bytes / 1e9) / (flood_launch_ms / 1000.0) if flood_launch_ms else 0.0
-    traffic = _traffic()
     roof = {"kernel": "k_relax (flood brick relaxation, one cooperative launch per step)",
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_kind": f"{peak_kind} copy bandwidth",
@@ -334,7 +331,8 @@ def main():
             "active_rows_per_sweep": act_rows / max(sweeps, 1),
             "key_changes_per_visit": key_changes / max(visits, 1),
             "launch_ms": flood_launch_ms,
-            "traffic": (traffic or {}).get("bytes_per_launch_scaled")}
+            "traffic": K_RELAX_DRAM_BYTES_PER_VISIT * visits / args.steps,
+            "traffic_source": "ncu DRAM bytes per brick visit (48-job capture) x visits of this launch"}
     line = {"metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16",
