@@ -340,7 +340,8 @@ def main():
             "config": {"workload": WORKLOAD, "jobs": len(specs), "voxels_per_step": voxels,
                        "l2": "inputs larger than L2 (label grids 2.8 GB per step)",
                        "parallelism": "replicas" if world > 1 else "single GPU",
-                       "path": "batched (one persistent brick-queue kernel per stage)"},
+                       "path": "batched (one persistent brick-queue kernel per stage)",
+                       "cuda_graph": bool(getattr(rb, "graph", False))},
             "e2e": {"value": e2e_value, "unit": "voxels/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms / args.steps,
                     "wall_ms_per_step": 1000.0 * wall_e2e / args.steps},

@@ -285,6 +285,10 @@ vf_status vf_ctx_flood_stats(vf_ctx* ctx, uint64_t* passes, uint64_t* sweeps,
  * [6] active rows summed over sweeps, [7] voxel key changes.  n <= 8 are
  * filled, the rest zeroed. */
 vf_status vf_ctx_flood_counters(vf_ctx* ctx, uint64_t* out, uint32_t n);
+/* *replayed = 1 when the last vf_batch_execute ran its stage chain as a
+ * CUDA graph (captured on the first execute after vf_batch_prepare, replayed
+ * afterwards), 0 when it launched the stages directly. */
+vf_status vf_ctx_last_graph(vf_ctx* ctx, int* replayed);
 
 #ifdef __cplusplus
 }

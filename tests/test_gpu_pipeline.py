@@ -18,7 +18,7 @@ def _oracle(oracle_lib):
     return oracle_lib
 
 
-def _job(vf, i, ncounts=512):
+def _job(vf, i, ncounts=512, pinned=False):
     """A small job of the mixed workload: uneven dims, metric and noise drawn
     per job."""
     rng = np.random.default_rng(1000 + i)
@@ -32,7 +32,7 @@ def _job(vf, i, ncounts=512):
         num_seeds=int(rng.integers(2, 12)), seed=7 + i, seed_location=vf.BOTH,
         noise_amplitude=float(rng.uniform(0, 3)) if i % 3 else 0.0, noise_period=16,
         erode=int(i % 4 == 1), erosion_type=int(rng.integers(0, 3)), erosion_iterations=1)
-    return vf.JobSpec(v, f, p, dims=dims, aabb=(mn, mx), ncounts=ncounts, tag=i)
+    return vf.JobSpec(v, f, p, dims=dims, aabb=(mn, mx), ncounts=ncounts, tag=i, pinned=pinned)
 
 
 def _oracle_job(spec):
@@ -58,6 +58,45 @@ def test_mixed_batch_matches_oracle_and_alone(vf, ctx):
         alone = _job(vf, i)
         (r,) = vf.batch_run([alone], ctx)
         assert np.array_equal(alone.labels, specs[i].labels)
+
+
+def test_resident_batch_graph_replays_match(vf, ctx):
+    # prepare once, execute three times: the first execute captures the stage
+    # chain as a CUDA graph, the next ones replay it; every run gives the
+    # batch_run bits
+    specs = [_job(vf, i, pinned=True) for i in range(10)]
+    ref = [_job(vf, i) for i in range(10)]
+    vf.batch_run(ref, ctx)
+    rb = vf.ResidentBatch(specs, ctx)
+    for k in range(3):
+        for s in specs:
+            s.labels[...] = 0xFFFF
+            s.counts[...] = 0
+        res = rb.execute(download=True)
+        assert rb.graph, "resident chain without host steps runs as a CUDA graph"
+        for a, b, r in zip(specs, ref, res):
+            assert r.status == 0
+            assert np.array_equal(a.labels, b.labels), f"execute {k} job {a.tag}"
+            assert np.array_equal(a.counts, b.counts)
+
+
+def test_resident_batch_with_host_steps_runs_direct(vf, ctx):
+    # sub-seed prefixes need the host-driven competition loop: no graph, same bits
+    specs, ref = [], []
+    for lst in (specs, ref):
+        for i in range(3):
+            s = _job(vf, 40 + i)
+            s.params.algorithm = vf.FLOOD
+            s.params.num_extra_seeds = 3
+            lst.append(s)
+    vf.batch_run(ref, ctx)
+    rb = vf.ResidentBatch(specs, ctx)
+    for k in range(2):
+        res = rb.execute(download=True)
+        assert not rb.graph
+        for a, b, r in zip(specs, ref, res):
+            assert r.status == 0
+            assert np.array_equal(a.labels, b.labels)
 
 
 def test_plain_matches_batched(vf, ctx):

@@ -125,6 +125,7 @@ EXPORTS = {
     "vf_ctx_stage_ms": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_ctx_flood_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "vf_ctx_flood_counters": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "vf_ctx_last_graph": (C.c_int, [C.c_void_p, C.c_void_p]),
     "vf_server_create": (C.c_int, [C.c_void_p, C.c_size_t, C.c_uint32, C.c_uint32, C.c_void_p]),
     "vf_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "vf_server_poll": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int]),
@@ -384,8 +385,17 @@ class JobSpec:
             dims = dims_for_aabb(self.aabb[0], self.aabb[1], max_dim)
         self.dims = tuple(int(d) for d in dims)
         self.params = params
-        self.labels = np.zeros(self.dims, np.uint16) if want_labels else None
-        self.counts = np.zeros(ncounts, np.uint32) if ncounts else None
+        if pinned:
+            # page-locked outputs: the library writes labels straight into them
+            self.labels = pinned_array(self.dims, np.uint16) if want_labels else None
+            self.counts = pinned_array((ncounts,), np.uint32) if ncounts else None
+            if self.labels is not None:
+                self.labels[...] = 0
+            if self.counts is not None:
+                self.counts[...] = 0
+        else:
+            self.labels = np.zeros(self.dims, np.uint16) if want_labels else None
+            self.counts = np.zeros(ncounts, np.uint32) if ncounts else None
         self.tag = tag
 
     def job(self) -> Job:
@@ -436,6 +446,9 @@ class ResidentBatch:
         st = lib().vf_batch_execute(self.ctx.h, 1 if download else 0, res)
         if st != OK and all(r.status == OK for r in res):
             _check(st)
+        g = C.c_int(0)
+        _check(lib().vf_ctx_last_graph(self.ctx.h, C.byref(g)))
+        self.graph = bool(g.value)  # the stage chain ran as a CUDA graph
         return list(res)
 
 

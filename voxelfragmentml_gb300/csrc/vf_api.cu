@@ -527,7 +527,7 @@ vf_status vf_batch_execute(vf_ctx* ctx, int download, vf_job_result* results) {
   if (!ctx->c.resident) return fail(VF_ERR_INVALID, "no prepared batch (call vf_batch_prepare)");
   cudaSetDevice(ctx->c.device);
   vfr::Batch& B = ctx->c.batch;
-  vf_status s = B.enqueue_batched(false, download != 0);
+  vf_status s = B.execute_resident(download != 0);
   if (s) return s;
   return B.finish(results);
 }
@@ -537,6 +537,12 @@ vf_status vf_ctx_flood_stats(vf_ctx* ctx, uint64_t* passes, uint64_t* sweeps, ui
   if (passes) *passes = ctx->c.last_flood_passes;
   if (sweeps) *sweeps = ctx->c.last_flood_sweeps;
   if (maxit_hits) *maxit_hits = ctx->c.last_flood_maxit;
+  return VF_OK;
+}
+
+vf_status vf_ctx_last_graph(vf_ctx* ctx, int* replayed) {
+  if (!ctx || !replayed) return fail(VF_ERR_INVALID, "NULL argument");
+  *replayed = ctx->c.batch.last_run_graph ? 1 : 0;
   return VF_OK;
 }
 

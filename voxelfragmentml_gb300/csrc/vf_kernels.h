@@ -82,6 +82,8 @@ void flood_seed_bricks(cudaStream_t st, const JobDesc* dj, JobState* ds, int njo
                        uint32_t* list, uint32_t* count);
 void flood_seed(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs,
                 const FloodScratch& fs, const uint8_t* live);
+// sets k_relax's shared-memory attribute and occupancy (once per process)
+void flood_prepare(int num_sms);
 cudaError_t flood_relax(cudaStream_t st, const JobDesc* dj, JobState* ds,
                         const uint32_t* brick_job, const uint8_t* live,
                         const FloodScratch& fs, int num_sms, int* blocks_used);

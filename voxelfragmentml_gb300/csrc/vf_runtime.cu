@@ -79,7 +79,59 @@ vf_status Batch::init(Ctx* c, bool own) {
   return VF_OK;
 }
 
+// events for timing and completion: inside a stream capture they must be
+// recorded as external event nodes so that the host can wait on them and
+// time them when the graph runs
+cudaError_t Batch::record_event(cudaEvent_t e, cudaStream_t st) {
+  return capturing ? cudaEventRecordWithFlags(e, st, cudaEventRecordExternal) : cudaEventRecord(e, st);
+}
+
+void Batch::drop_graphs() {
+  for (int i = 0; i < 2; ++i) {
+    if (gexec[i]) cudaGraphExecDestroy(gexec[i]);
+    gexec[i] = nullptr;
+    glaunches[i] = 0;
+  }
+}
+
+vf_status Batch::execute_resident(bool download) {
+  bool host_steps = false;
+  for (const JobPlan& p : plans) host_steps |= p.prefix_possible;
+  last_run_graph = false;
+  if (!graphs_ok || host_steps) return enqueue_batched(false, download);
+  const int gi = download ? 1 : 0;
+  if (!gexec[gi]) {
+    vfk::flood_prepare(ctx->num_sms);  // function attributes outside the capture
+    if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      graphs_ok = false;
+      return enqueue_batched(false, download);
+    }
+    capturing = true;
+    vf_status s = enqueue_batched(false, download);
+    capturing = false;
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(stream, &g);
+    cudaGraphExec_t ex = nullptr;
+    const cudaError_t ei = (!s && ec == cudaSuccess && g) ? cudaGraphInstantiate(&ex, g, 0) : cudaErrorUnknown;
+    if (g) cudaGraphDestroy(g);
+    if (s || ei != cudaSuccess) {
+      cudaGetLastError();
+      if (ex) cudaGraphExecDestroy(ex);
+      graphs_ok = false;  // run this chain with direct launches from now on
+      return enqueue_batched(false, download);
+    }
+    gexec[gi] = ex;
+    glaunches[gi] = launches;
+  }
+  launches = glaunches[gi];
+  VF_CK(cudaGraphLaunch(gexec[gi], stream));
+  last_run_graph = true;
+  return VF_OK;
+}
+
 void Batch::release() {
+  drop_graphs();
   if (!ctx) return;
   for (DevBuf* b : {&grid0, &grid1, &keys, &par, &tets, &range, &ys, &seeds, &counts, &lat,
                     &verts, &faces, &emask, &etab, &tables, &state, &brick_job, &live, &list, &lcount,
@@ -215,6 +267,8 @@ size_t job_footprint(const vf_job& j) {
 }
 
 vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
+  drop_graphs();  // captured chains refer to the previous plan's tables and buffers
+  graphs_ok = true;
   jobs.assign(js, js + n);
   plans.assign(n, JobPlan());
   sz = Sizes();
@@ -552,7 +606,7 @@ vf_status Batch::enqueue_batched(bool do_upload, bool do_download) {
   flood_timed = false;
   for (int i = 0; i < NSTAGE_EV; ++i) stage_rec[i] = false;
   std::function<void(int)> mark = [&](int i) {
-    if (cudaEventRecord(ev_stage[i], st) == cudaSuccess) stage_rec[i] = true;
+    if (record_event(ev_stage[i], st) == cudaSuccess) stage_rec[i] = true;
   };
   mark(0);
   vf_status s = do_upload ? upload_inputs_impl(*this) : VF_OK;
@@ -603,10 +657,10 @@ vf_status Batch::enqueue_batched(bool do_upload, bool do_download) {
     vfk::flood_seed_bricks(st, tf, ds, n, lv, lst, lc);
     vfk::flood_init_keys(st, tf, lst, lc, maxc, bj, lv);
     vfk::flood_seed(st, tf, ds, n, fs, lv);
-    VF_CK(cudaEventRecord(ev_flood0, st));
+    VF_CK(record_event(ev_flood0, st));
     cudaError_t e = vfk::flood_relax(st, tf, ds, bj, lv, fs, ctx->num_sms, &relax_blocks);
     if (e != cudaSuccess) return fail(VF_ERR_CUDA, std::string("flood relax launch: ") + cudaGetErrorString(e));
-    VF_CK(cudaEventRecord(ev_flood1, st));
+    VF_CK(record_event(ev_flood1, st));
     flood_timed = true;
     vfk::flood_finalize(st, tf, ds, lst, lc, maxc, bj, 0);
     launches += 5;
@@ -680,7 +734,7 @@ vf_status Batch::enqueue_batched(bool do_upload, bool do_download) {
   VF_CK(cudaMemcpyAsync(h_state, ds, sizeof(JobState) * n, cudaMemcpyDeviceToHost, st));
   VF_CK(cudaMemcpyAsync(h_scal, scal.p, 64 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   mark(11);
-  VF_CK(cudaEventRecord(ev_done, st));
+  VF_CK(record_event(ev_done, st));
   return VF_OK;
 }
 

@@ -91,6 +91,18 @@ struct Batch {
   void release();
   vf_status plan(const vf_job* const* js, uint32_t n);
   vf_status enqueue_batched(bool upload_inputs = true, bool download = true);
+  // the resident stage chain (no uploads) as a CUDA graph: captured on the
+  // first execute after plan(), replayed afterwards; falls back to direct
+  // launches when the chain has host steps (sub-seed prefix competition) or
+  // cannot be captured
+  vf_status execute_resident(bool download);
+  void drop_graphs();
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // [download]
+  uint64_t glaunches[2] = {0, 0};
+  bool graphs_ok = true;
+  bool last_run_graph = false;
+  bool capturing = false;
+  cudaError_t record_event(cudaEvent_t e, cudaStream_t st);
   vf_status upload_inputs();
   vf_status enqueue_plain_and_wait(vf_job_result* res, bool skip_vox);
   vf_status finish(vf_job_result* res);

@@ -70,7 +70,7 @@ def to_spec(job, V, want_labels=True, ncounts=256, pinned=False):
         pf[...] = f
         v, f = pv, pf
     spec = V.JobSpec(v, f, p, dims=dims, aabb=(mn, mx), want_labels=False, ncounts=ncounts,
-                     tag=job["index"])
+                     tag=job["index"], pinned=pinned)
     if want_labels:
         spec.labels = V.pinned_array(spec.dims, np.uint16) if pinned else np.zeros(spec.dims, np.uint16)
     return spec
