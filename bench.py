@@ -197,6 +197,7 @@ def main():
                     help="--impl reference: every n-th job per step")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default settings)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -220,6 +221,9 @@ def main():
     voxels = sum(int(np.prod(s.dims)) for s in specs)
     h2d = sum(s.verts.nbytes + s.faces.nbytes for s in specs)
     d2h = sum(s.labels.nbytes + s.counts.nbytes for s in specs)
+
+    # ---- launch settings from the autotuner (a 64-job sample) -------------
+    tuning = ctx.autotune(specs[:min(64, len(specs))]) if not args.no_tune else ctx.tuning()
 
     # ---- value: inputs resident in HBM ------------------------------------
     rb = V.ResidentBatch(specs, ctx)
@@ -341,7 +345,8 @@ def main():
                        "l2": "inputs larger than L2 (label grids 2.8 GB per step)",
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "path": "batched (one persistent brick-queue kernel per stage)",
-                       "cuda_graph": bool(getattr(rb, "graph", False))},
+                       "cuda_graph": bool(getattr(rb, "graph", False)),
+                       "tuning": tuning},
             "e2e": {"value": e2e_value, "unit": "voxels/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms / args.steps,
                     "wall_ms_per_step": 1000.0 * wall_e2e / args.steps},

@@ -290,6 +290,20 @@ vf_status vf_ctx_flood_counters(vf_ctx* ctx, uint64_t* out, uint32_t n);
  * afterwards), 0 when it launched the stages directly. */
 vf_status vf_ctx_last_graph(vf_ctx* ctx, int* replayed);
 
+/* ---- tuning (no counterpart in the reference) ----------------------------
+ * Launch settings of a context, in this order: [0] parity-fill CTAs per SM,
+ * [1] shell-test CTAs per SM, [2] flood relaxation sweeps per brick visit
+ * (BFS waves a brick advances per pass before it re-queues itself),
+ * [3] flood CTAs per SM (0: as many as fit).  Results never depend on them. */
+vf_status vf_ctx_set_tuning(vf_ctx* ctx, const int32_t* values, uint32_t n);
+vf_status vf_ctx_get_tuning(vf_ctx* ctx, int32_t* values, uint32_t n);
+/* Autotuner: prepares `jobs` as a resident batch (as vf_batch_prepare, which
+ * it replaces) and runs it under candidate settings, one knob at a time,
+ * keeping for each knob the value with the lowest device time of its stage.
+ * The chosen settings stay on ctx (n of them copied to `chosen`). */
+vf_status vf_autotune(vf_ctx* ctx, const vf_job* jobs, uint32_t njobs, int32_t* chosen,
+                      uint32_t n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -99,6 +99,32 @@ def test_resident_batch_with_host_steps_runs_direct(vf, ctx):
             assert np.array_equal(a.labels, b.labels)
 
 
+def test_autotune_and_settings_do_not_change_results(vf, ctx):
+    ref = [_job(vf, i) for i in range(8)]
+    vf.batch_run(ref, ctx)
+    saved = ctx.tuning()
+    try:
+        chosen = ctx.autotune([_job(vf, i) for i in range(8)])
+        assert chosen["parity_grid"] in (4, 8, 16, 32) and chosen["shell_grid"] in (6, 12, 24)
+        assert chosen["flood_sweeps"] in (8, 16, 32, 96) and chosen["flood_ctas"] in (0, 1)
+        assert ctx.tuning() == chosen
+        # extreme settings: one sweep per brick visit (every brick re-queues
+        # itself until its keys settle), one CTA per SM, minimal grids
+        for kw in (chosen, dict(flood_sweeps=1, flood_ctas=1, parity_grid=1, shell_grid=1),
+                   dict(flood_sweeps=3, flood_ctas=0, parity_grid=64, shell_grid=64)):
+            ctx.set_tuning(**kw)
+            got = [_job(vf, i) for i in range(8)]
+            for r in vf.batch_run(got, ctx):
+                assert r.status == 0
+            for a, b in zip(got, ref):
+                assert np.array_equal(a.labels, b.labels), kw
+                assert np.array_equal(a.counts, b.counts)
+        with pytest.raises(vf.VFError):
+            ctx.set_tuning(flood_sweeps=0)
+    finally:
+        ctx.set_tuning(**saved)
+
+
 def test_plain_matches_batched(vf, ctx):
     specs = [_job(vf, i) for i in range(6)]
     plain = [_job(vf, i) for i in range(6)]

@@ -126,6 +126,9 @@ EXPORTS = {
     "vf_ctx_flood_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "vf_ctx_flood_counters": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_ctx_last_graph": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "vf_ctx_set_tuning": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "vf_ctx_get_tuning": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "vf_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
     "vf_server_create": (C.c_int, [C.c_void_p, C.c_size_t, C.c_uint32, C.c_uint32, C.c_void_p]),
     "vf_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "vf_server_poll": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int]),
@@ -201,6 +204,27 @@ class Context:
         a = (C.c_float * 11)()
         _check(lib().vf_ctx_stage_ms(self.h, a, 11))
         return dict(zip(STAGES, list(a)))
+
+    TUNING = ("parity_grid", "shell_grid", "flood_sweeps", "flood_ctas")
+
+    def tuning(self) -> dict:
+        v = (C.c_int32 * 4)()
+        _check(lib().vf_ctx_get_tuning(self.h, v, 4))
+        return dict(zip(self.TUNING, list(v)))
+
+    def set_tuning(self, **kw):
+        cur = self.tuning()
+        cur.update(kw)
+        v = (C.c_int32 * 4)(*[int(cur[k]) for k in self.TUNING])
+        _check(lib().vf_ctx_set_tuning(self.h, v, 4))
+
+    def autotune(self, specs) -> dict:
+        """vf_autotune over the jobs of `specs` (JobSpec list); returns the
+        chosen settings, which stay on this context."""
+        jobs = (Job * len(specs))(*[s.job() for s in specs])
+        v = (C.c_int32 * 4)()
+        _check(lib().vf_autotune(self.h, jobs, len(specs), v, 4))
+        return dict(zip(self.TUNING, list(v)))
 
     def last_stats(self):
         la, vis, by = C.c_uint64(), C.c_uint64(), C.c_uint64()

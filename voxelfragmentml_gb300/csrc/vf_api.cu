@@ -532,6 +532,79 @@ vf_status vf_batch_execute(vf_ctx* ctx, int download, vf_job_result* results) {
   return B.finish(results);
 }
 
+// ---- tuning ------------------------------------------------------------------
+static vf_status set_tuning(vfr::Ctx& c, const int32_t* v, uint32_t n) {
+  vfr::Tuning t = c.tune;
+  if (n > 0) t.parity_grid = v[0];
+  if (n > 1) t.shell_grid = v[1];
+  if (n > 2) t.flood_sweeps = v[2];
+  if (n > 3) t.flood_ctas = v[3];
+  if (t.parity_grid < 1 || t.parity_grid > 64 || t.shell_grid < 1 || t.shell_grid > 64 ||
+      t.flood_sweeps < 1 || t.flood_sweeps > 96 || t.flood_ctas < 0 || t.flood_ctas > 8)
+    return fail(VF_ERR_RANGE, "tuning: grids in [1, 64] CTAs/SM, sweeps in [1, 96], flood CTAs/SM in [0, 8]");
+  c.tune = t;
+  c.batch.drop_graphs();  // captured chains hold the old launch settings
+  return VF_OK;
+}
+
+vf_status vf_ctx_set_tuning(vf_ctx* ctx, const int32_t* values, uint32_t n) {
+  if (!ctx || (n && !values)) return fail(VF_ERR_INVALID, "NULL argument");
+  return set_tuning(ctx->c, values, n);
+}
+
+vf_status vf_ctx_get_tuning(vf_ctx* ctx, int32_t* values, uint32_t n) {
+  if (!ctx || (n && !values)) return fail(VF_ERR_INVALID, "NULL argument");
+  const int32_t v[4] = {ctx->c.tune.parity_grid, ctx->c.tune.shell_grid, ctx->c.tune.flood_sweeps,
+                        ctx->c.tune.flood_ctas};
+  for (uint32_t i = 0; i < n; ++i) values[i] = i < 4 ? v[i] : 0;
+  return VF_OK;
+}
+
+vf_status vf_autotune(vf_ctx* ctx, const vf_job* jobs, uint32_t njobs, int32_t* chosen, uint32_t n) {
+  if (!ctx || !jobs || !njobs || (n && !chosen)) return fail(VF_ERR_INVALID, "NULL argument or no jobs");
+  vf_status s = vf_batch_prepare(ctx, jobs, njobs);
+  if (s) return s;
+  vfr::Ctx& c = ctx->c;
+  vfr::Batch& B = c.batch;
+  // one direct run of the stage chain; returns the device ms of stage `stage`
+  auto run = [&](int stage, float* ms) -> vf_status {
+    vf_status r = B.enqueue_batched(false, false);
+    if (!r) r = B.finish(nullptr);
+    if (r) return r;
+    *ms = c.last_stage_ms[stage];
+    return VF_OK;
+  };
+  float warm = 0.f;
+  if ((s = run(0, &warm))) return s;
+  struct Knob { int index, stage; std::vector<int32_t> cand; };
+  const Knob knobs[] = {{0, 2, {4, 8, 16, 32}},      // parity grid   (stage: parity)
+                        {1, 3, {6, 12, 24}},         // shell grid    (stage: shell)
+                        {2, 6, {8, 16, 32, 96}},     // sweeps/visit  (stage: fracture)
+                        {3, 6, {1, 0}}};             // flood CTAs/SM (stage: fracture)
+  for (const Knob& k : knobs) {
+    int32_t best_v = 0;
+    float best = 3.0e38f;
+    for (int32_t v : k.cand) {
+      int32_t cur[4];
+      vf_ctx_get_tuning(ctx, cur, 4);
+      cur[k.index] = v;
+      if ((s = set_tuning(c, cur, 4))) return s;
+      float t = 3.0e38f;
+      for (int rep = 0; rep < 2; ++rep) {
+        float ms = 0.f;
+        if ((s = run(k.stage, &ms))) return s;
+        t = std::min(t, ms);
+      }
+      if (t < best) { best = t; best_v = v; }
+    }
+    int32_t cur[4];
+    vf_ctx_get_tuning(ctx, cur, 4);
+    cur[k.index] = best_v;
+    if ((s = set_tuning(c, cur, 4))) return s;
+  }
+  return chosen ? vf_ctx_get_tuning(ctx, chosen, n) : VF_OK;
+}
+
 vf_status vf_ctx_flood_stats(vf_ctx* ctx, uint64_t* passes, uint64_t* sweeps, uint64_t* maxit_hits) {
   if (!ctx) return fail(VF_ERR_INVALID, "ctx is NULL");
   if (passes) *passes = ctx->c.last_flood_passes;

@@ -37,7 +37,7 @@ constexpr int KNX = VF_BX + 2, KNY = VF_BY + 2;
 constexpr int KROWS = KNX * KNY;
 constexpr int KZW = 10;                // 16-byte chunks per staged row: z in [z0-4, z0+36)
 constexpr int TILE_BYTES = KROWS * KP * 4;
-constexpr int MAXIT = 96;              // relaxation sweeps per brick visit
+constexpr int MAXIT = 96;              // default cap of relaxation sweeps per brick visit
 
 struct FloodArgs {
   const JobDesc* jobs;
@@ -52,6 +52,7 @@ struct FloodArgs {
   uint32_t* err;
   uint32_t* stats;   // [0] visits, [1] passes, [2] overflow, [3] timeout
   uint32_t max_passes;
+  int max_sweeps;    // sweeps per brick visit before the brick re-queues itself
 };
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
@@ -166,7 +167,7 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
   __syncthreads();
   const int own = (tx + 1) * KNY + (ty + 1);
   int it = 0, cur = 0;
-  for (; it < MAXIT; ++it) {
+  for (; it < a.max_sweeps; ++it) {
     const uint8_t* pf = rflag + cur * KROWS;
     bool active;
     if (CONN == 26) {
@@ -295,9 +296,9 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
   if (nact) atomicAdd(&scnt[0], nact);
   if (nchg) atomicAdd(&scnt[1], nchg);
   if (t == 0) {
-    if (it == MAXIT) *reenq = 1;
+    if (it == a.max_sweeps) *reenq = 1;
     atomicAdd(a.stats + 4, (uint32_t)it + 1u);  // sweeps (statistics)
-    if (it == MAXIT) atomicAdd(a.stats + 5, 1u);
+    if (it == a.max_sweeps) atomicAdd(a.stats + 5, 1u);
   }
   __syncthreads();
   if (t == 0) {
@@ -667,7 +668,9 @@ cudaError_t flood_relax(cudaStream_t st, const JobDesc* dj, JobState* ds,
   a.err = fs.err;
   a.stats = fs.stats;
   a.max_passes = fs.max_passes;
-  const int blocks = relax_blocks(num_sms);
+  a.max_sweeps = (fs.max_sweeps > 0 && fs.max_sweeps <= MAXIT) ? fs.max_sweeps : MAXIT;
+  int blocks = relax_blocks(num_sms);
+  if (fs.ctas_per_sm > 0 && fs.ctas_per_sm * num_sms < blocks) blocks = fs.ctas_per_sm * num_sms;
   if (blocks_used) *blocks_used = blocks;
   void* args[] = {&a};
   return cudaLaunchCooperativeKernel((const void*)k_relax, dim3(blocks), dim3(256), args,

@@ -23,10 +23,10 @@ void centroid_and_slices(cudaStream_t st, const JobDesc* dj, JobState* ds, int n
 void tetra_prep(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs,
                 uint32_t total_faces, const FaceScratch& fs);
 void parity_raster(cudaStream_t st, const JobDesc* dj, const JobState* ds, int njobs,
-                   uint32_t total_faces, const FaceScratch& fs, int num_sms);
+                   uint32_t total_faces, const FaceScratch& fs, int num_sms, int grid_mult = 16);
 // reuses the face scratch after the parity raster (counts, scan, runs)
 void shell_sat(cudaStream_t st, const JobDesc* dj, int njobs, uint32_t total_faces,
-               const FaceScratch& fs, int num_sms);
+               const FaceScratch& fs, int num_sms, int grid_mult = 12);
 // writes 0/1 labels (grid, and grid2 when dual) for every brick of every
 // job and sets live[b]
 void combine(cudaStream_t st, const JobDesc* dj, const uint32_t* brick_job,
@@ -74,6 +74,8 @@ struct FloodScratch {
   uint32_t* stats;       // [4] brick visits, passes, overflow, timeout
   uint32_t max_passes;
   uint32_t total_bricks;
+  int max_sweeps = 0;    // tuning: sweeps per brick visit (0: default cap)
+  int ctas_per_sm = 0;   // tuning: resident CTAs per SM (0: as many as fit)
 };
 void flood_init_keys(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
                      const uint32_t* count, uint32_t max_count, const uint32_t* brick_job,

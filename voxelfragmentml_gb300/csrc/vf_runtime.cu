@@ -572,9 +572,9 @@ static void voxelize_stages(Batch& B, const std::function<void(int)>& mark) {
   vfk::centroid_and_slices(st, tv, ds, n);
   vfk::tetra_prep(st, tv, ds, n, B.sz.faces_total, fsc);
   mark(2);
-  vfk::parity_raster(st, tv, ds, n, B.sz.faces_total, fsc, B.ctx->num_sms);
+  vfk::parity_raster(st, tv, ds, n, B.sz.faces_total, fsc, B.ctx->num_sms, B.ctx->tune.parity_grid);
   mark(3);
-  vfk::shell_sat(st, tv, n, B.sz.faces_total, fsc, B.ctx->num_sms);
+  vfk::shell_sat(st, tv, n, B.sz.faces_total, fsc, B.ctx->num_sms, B.ctx->tune.shell_grid);
   mark(4);
   vfk::combine(st, tv, static_cast<uint32_t*>(B.brick_job.p), B.sz.bricks,
                static_cast<uint8_t*>(B.live.p), 1);
@@ -596,6 +596,8 @@ static vfk::FloodScratch flood_scratch(Batch& B) {
   fs.epoch = static_cast<uint32_t*>(B.epoch.p);
   fs.max_passes = 1u << 20;
   fs.total_bricks = B.sz.bricks;
+  fs.max_sweeps = B.ctx->tune.flood_sweeps;
+  fs.ctas_per_sm = B.ctx->tune.flood_ctas;
   return fs;
 }
 

@@ -110,9 +110,18 @@ struct Batch {
   const JobDesc* dtable(uint32_t t) const;
 };
 
+// launch settings chosen by vf_autotune (results never depend on them)
+struct Tuning {
+  int32_t parity_grid = 16;   // k_parity_flat CTAs per SM
+  int32_t shell_grid = 12;    // k_shell_flat CTAs per SM
+  int32_t flood_sweeps = 96;  // relaxation sweeps per brick visit (waves per pass)
+  int32_t flood_ctas = 0;     // k_relax resident CTAs per SM (0: as many as fit)
+};
+
 struct Ctx {
   int device = 0;
   int num_sms = 0;
+  Tuning tune;
   cudaStream_t stream = nullptr;
   size_t budget = 0;
   size_t in_use = 0;

@@ -886,13 +886,13 @@ void tetra_prep(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs,
     k_tetra<<<grid_for(total_faces, 256, 65535), 256, 0, st>>>(dj, ds, njobs, total_faces, fs.pcnt);
 }
 void parity_raster(cudaStream_t st, const JobDesc* dj, const JobState* ds, int njobs,
-                   uint32_t total_faces, const FaceScratch& fs, int num_sms) {
+                   uint32_t total_faces, const FaceScratch& fs, int num_sms, int grid_mult) {
   if (!total_faces) return;
   const uint32_t nb = (total_faces + 1023) / 1024;
   k_scan_local<<<nb, 1024, 0, st>>>(fs.pcnt, fs.pbase, fs.psums, total_faces);
   k_scan_sums<<<1, 1024, 0, st>>>(fs.psums, nb, fs.ptotal);
   k_scan_add<<<(total_faces + 255) / 256, 256, 0, st>>>(fs.pbase, fs.psums, total_faces);
-  k_parity_flat<<<num_sms * 16, 256, 0, st>>>(dj, njobs, fs.pcnt, fs.pbase, fs.ptotal, total_faces);
+  k_parity_flat<<<num_sms * grid_mult, 256, 0, st>>>(dj, njobs, fs.pcnt, fs.pbase, fs.ptotal, total_faces);
   const unsigned gy = (unsigned)(njobs < 65535 ? njobs : 65535);
   k_odd_edges<<<dim3(num_sms, gy), 256, 0, st>>>(dj, ds, njobs);
   int px = num_sms * 8 / njobs;
@@ -900,7 +900,7 @@ void parity_raster(cudaStream_t st, const JobDesc* dj, const JobState* ds, int n
   k_prefix_x<<<dim3(px, gy), 256, 0, st>>>(dj, njobs);
 }
 void shell_sat(cudaStream_t st, const JobDesc* dj, int njobs, uint32_t total_faces,
-               const FaceScratch& fs, int num_sms) {
+               const FaceScratch& fs, int num_sms, int grid_mult) {
   if (!total_faces) return;
   const uint32_t nb = (total_faces + 1023) / 1024;
   k_shell_count<<<grid_for(total_faces, 256, 65535), 256, 0, st>>>(dj, njobs, total_faces, fs.pcnt,
@@ -908,7 +908,7 @@ void shell_sat(cudaStream_t st, const JobDesc* dj, int njobs, uint32_t total_fac
   k_scan_local<<<nb, 1024, 0, st>>>(fs.pcnt, fs.pbase, fs.psums, total_faces);
   k_scan_sums<<<1, 1024, 0, st>>>(fs.psums, nb, fs.ptotal);
   k_scan_add<<<(total_faces + 255) / 256, 256, 0, st>>>(fs.pbase, fs.psums, total_faces);
-  k_shell_flat<<<num_sms * 12, 256, 0, st>>>(dj, fs.pcnt, fs.pbase, fs.ptotal, total_faces, fs.srec);
+  k_shell_flat<<<num_sms * grid_mult, 256, 0, st>>>(dj, fs.pcnt, fs.pbase, fs.ptotal, total_faces, fs.srec);
 }
 void combine(cudaStream_t st, const JobDesc* dj, const uint32_t* brick_job,
              uint32_t total_bricks, uint8_t* live, int dual) {
