@@ -127,6 +127,13 @@ vf_status vf_dims_for_aabb(const float aabb_min[3], const float aabb_max[3],
 vf_status vf_grid_upload(vf_grid* g, const uint16_t* host_grid);
 vf_status vf_grid_download(vf_grid* g, uint16_t* host_grid);
 
+/* RegularGrid::exportRLE (RegularGrid.cpp:672-714) into memory: u32 X, Y, Z,
+ * then one {u16 value, u32 repetitions} record per run of equal labels in
+ * x-major order, packed little endian.  *written = the size in bytes; out =
+ * NULL with cap = 0 only queries it; VF_ERR_RANGE if cap is smaller or the
+ * grid has 2^32 voxels or more. */
+vf_status vf_grid_export_rle(vf_grid* g, uint8_t* out, size_t cap, size_t* written);
+
 /* RegularGrid::fill(Model3D*) (RegularGrid.cpp:173-212): occupancy = FP32
  * tri-box SAT shell (Intersections3D.h:204-258) OR tetra-parity interior
  * (Tetravoxelizer.cpp:42-92, 198-315).  verts: 3 floats per vertex, faces:

@@ -377,3 +377,54 @@ def test_golden_all_in_one_batch(vf, ctx):
     res = vf.batch_run(specs, ctx)
     for n, s, r in zip(CASES, specs, res):
         _check_gold(n, s, r)
+
+
+# ---- RLE export (RegularGrid::exportRLE) on the GPU --------------------------
+def _rle_decode(buf):
+    X, Y, Z = np.frombuffer(buf[:12], "<u4")
+    runs = np.frombuffer(buf[12:], dtype=np.dtype([("v", "<u2"), ("n", "<u4")]))
+    return np.repeat(runs["v"], runs["n"]).reshape(X, Y, Z)
+
+
+def test_rle_export_reference_fixture(vf, ctx):
+    # the reference's own exported grid: decoded, uploaded, exported again on
+    # the GPU, byte for byte
+    buf = open(os.path.join(GOLD, "AL_12B_grid_128r.rle"), "rb").read()
+    g = _rle_decode(buf)
+    grid = vf.RegularGrid(g.shape, None, None, ctx)
+    grid.upload(g)
+    assert grid.exportRLE() == buf
+
+
+@pytest.mark.parametrize("kind", ["random_runs", "uniform", "alternating", "sparse", "odd_z"])
+def test_rle_export_matches_oracle(vf, ctx, kind):
+    rng = np.random.default_rng(sum(map(ord, kind)))
+    shape = {"odd_z": (9, 7, 13), "alternating": (17, 5, 40)}.get(kind, (33, 20, 52))
+    if kind == "random_runs":
+        g = np.repeat(rng.integers(0, 6, size=shape[0] * shape[1] * shape[2] // 7 + 1), 7)
+        g = g[:np.prod(shape)].reshape(shape).astype(np.uint16)
+    elif kind == "uniform":
+        g = np.full(shape, 3, np.uint16)
+    elif kind == "alternating":
+        g = (np.arange(np.prod(shape)) % 2 + 2).reshape(shape).astype(np.uint16)
+    elif kind == "sparse":
+        g = np.zeros(shape, np.uint16)
+        g[rng.random(shape) < 0.02] = 0x8005  # bit 15 set: the full 16-bit value is exported
+    else:
+        g = rng.integers(0, 3, size=shape).astype(np.uint16)
+    grid = vf.RegularGrid(shape, None, None, ctx)
+    grid.upload(g)
+    got = grid.exportRLE()
+    assert got == O.rle_encode(g)
+    assert np.array_equal(_rle_decode(got), g)
+
+
+def test_rle_export_after_fracture(vf, ctx, occ64):
+    occ, mn, mx = occ64
+    g = vf.RegularGrid(occ.shape, mn, mx, ctx)
+    g.upload(occ)
+    fr = vf.FloodFracturer()
+    fr.setDistanceFunction(vf.MANHATTAN)
+    fr.build(g, O.seeder_uniform(occ, 8, 5, 2))
+    g.detectBoundaries(1)
+    assert g.exportRLE() == O.rle_encode(g.data())

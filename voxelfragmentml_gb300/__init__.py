@@ -126,6 +126,7 @@ EXPORTS = {
     "vf_ctx_flood_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "vf_ctx_flood_counters": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_ctx_last_graph": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "vf_grid_export_rle": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "vf_ctx_set_tuning": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_ctx_get_tuning": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
@@ -297,6 +298,19 @@ class RegularGrid:
 
     def detectBoundaries(self, boundary_size: int = 1):
         _check(lib().vf_detect_boundaries(self.h, boundary_size))
+
+    def exportRLE(self, path=None) -> bytes:
+        """RegularGrid::exportRLE: the grid as run-length records (computed on
+        the GPU); also written to `path` when given."""
+        n = C.c_size_t(0)
+        _check(lib().vf_grid_export_rle(self.h, None, 0, C.byref(n)))
+        buf = (C.c_ubyte * max(n.value, 1))()
+        _check(lib().vf_grid_export_rle(self.h, buf, n.value, C.byref(n)))
+        data = bytes(buf)[:n.value]
+        if path is not None:
+            with open(path, "wb") as fh:
+                fh.write(data)
+        return data
 
     def erode(self, erosion_type=ELLIPSE, size=3, iterations=3, probability=0.5,
               threshold=0.5, seed=80):

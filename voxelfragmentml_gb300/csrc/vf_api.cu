@@ -255,6 +255,50 @@ vf_status vf_grid_download(vf_grid* g, uint16_t* host) {
   return VF_OK;
 }
 
+vf_status vf_grid_export_rle(vf_grid* g, uint8_t* out, size_t cap, size_t* written) {
+  if (!g || !written) return fail(VF_ERR_INVALID, "NULL argument");
+  cudaSetDevice(g->ctx->c.device);
+  vfr::Batch& B = g->b;
+  const vfr::JobPlan& p = B.plans[0];
+  const uint64_t rows = (uint64_t)p.X * p.Y, nvox = rows * p.Z;
+  if (nvox >= 0xFFFFFFFFull) return fail(VF_ERR_RANGE, "RLE export: grids of 2^32 voxels or more");
+  vfr::Ctx& c = g->ctx->c;
+  vf_status s;
+  if ((s = c.alloc(B.rle_cnt, rows * 4)) || (s = c.alloc(B.rle_base, rows * 8)) ||
+      (s = c.alloc(B.rle_sums, ((rows + 1023) / 1024 + 2) * 8)) || (s = c.alloc(B.rle_tot, 64)))
+    return s;
+  cudaStream_t st = B.stream;
+  const uint16_t* grid = static_cast<const uint16_t*>(B.grid0.p);
+  vfk::rle_count(st, grid, p.X, p.Y, p.Z, p.Zp, static_cast<uint32_t*>(B.rle_cnt.p), c.num_sms);
+  unsigned long long* tot = static_cast<unsigned long long*>(B.rle_tot.p);
+  vfk::exclusive_scan(st, static_cast<uint32_t*>(B.rle_cnt.p),
+                      static_cast<unsigned long long*>(B.rle_base.p),
+                      static_cast<unsigned long long*>(B.rle_sums.p), (uint32_t)rows, tot);
+  unsigned long long nruns = 0;
+  VF_CK(cudaMemcpyAsync(&nruns, tot, 8, cudaMemcpyDeviceToHost, st));
+  VF_CK(cudaStreamSynchronize(st));
+  const size_t need = 12 + 6 * (size_t)nruns;
+  *written = need;
+  if (!out) {
+    if (cap) return fail(VF_ERR_INVALID, "out is NULL");
+    return VF_OK;  // size query
+  }
+  if (cap < need) return fail(VF_ERR_RANGE, "RLE export: buffer smaller than " + std::to_string(need) + " bytes");
+  if ((s = c.alloc(B.rle_starts, std::max<size_t>(nruns, 1) * 8)) ||
+      (s = c.alloc(B.rle_rec, std::max<size_t>(nruns, 1) * 6)))
+    return s;
+  vfk::rle_write(st, grid, p.X, p.Y, p.Z, p.Zp, static_cast<unsigned long long*>(B.rle_base.p), tot,
+                 static_cast<unsigned long long*>(B.rle_starts.p), static_cast<uint16_t*>(B.rle_rec.p),
+                 c.num_sms);
+  const uint32_t d[3] = {p.X, p.Y, p.Z};
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 4; ++b) out[4 * a + b] = (uint8_t)(d[a] >> (8 * b));
+  if (nruns) VF_CK(cudaMemcpyAsync(out + 12, B.rle_rec.p, 6 * (size_t)nruns, cudaMemcpyDeviceToHost, st));
+  VF_CK(cudaStreamSynchronize(st));
+  VF_CK(cudaGetLastError());
+  return VF_OK;
+}
+
 vf_status vf_voxelize(vf_grid* g, const float* verts, uint32_t nverts, const uint32_t* faces,
                       uint32_t nfaces) {
   if (!g) return fail(VF_ERR_INVALID, "grid is NULL");

@@ -40,6 +40,21 @@ void compact_live(cudaStream_t st, const uint8_t* live, uint32_t total_bricks,
 // final buffer) into `out`, rows of Z without the z padding
 void pack_labels(cudaStream_t st, const JobDesc* dj, int njobs, uint64_t total_rows, int num_sms);
 
+// exclusive prefix sum of n u32 into u64 (sums: ceil(n / 1024) + 1 scratch
+// words); *total = the sum
+void exclusive_scan(cudaStream_t st, const uint32_t* in, unsigned long long* out,
+                    unsigned long long* sums, uint32_t n, unsigned long long* total);
+
+// ---- RLE export (vf_rle.cu) ----
+// run starts counted per (x, y) row of a grid [X][Y][Zp]
+void rle_count(cudaStream_t st, const uint16_t* g, uint32_t X, uint32_t Y, uint32_t Z, uint32_t Zp,
+               uint32_t* row_cnt, int num_sms);
+// records {u16 value, u32 repetitions} as 3 u16 per run, from the scanned
+// row counts; starts: scratch of one u64 per run
+void rle_write(cudaStream_t st, const uint16_t* g, uint32_t X, uint32_t Y, uint32_t Z, uint32_t Zp,
+               const unsigned long long* row_base, const unsigned long long* nruns,
+               unsigned long long* starts, uint16_t* records, int num_sms);
+
 // ---- seeds ----
 void sample_seeds(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs);
 

@@ -136,7 +136,8 @@ void Batch::release() {
   for (DevBuf* b : {&grid0, &grid1, &keys, &par, &tets, &range, &ys, &seeds, &counts, &lat,
                     &verts, &faces, &emask, &etab, &tables, &state, &brick_job, &live, &list, &lcount,
                     &q[0], &q[1], &q[2], &scal, &epoch, &front[0], &front[1], &pcnt, &pbase,
-                    &psums, &srec})
+                    &psums, &srec, &rle_cnt, &rle_base, &rle_sums, &rle_tot, &rle_starts,
+                    &rle_rec})
     ctx->free_buf(*b);
   if (h_tables) cudaFreeHost(h_tables);
   if (h_state) cudaFreeHost(h_state);

@@ -59,6 +59,7 @@ struct Batch {
   bool own_stream = false;
   DevBuf grid0, grid1, keys, par, tets, range, ys, seeds, counts, lat, verts, faces, emask;
   DevBuf etab;  // mesh edge parity tables (voxelizer)
+  DevBuf rle_cnt, rle_base, rle_sums, rle_tot, rle_starts, rle_rec;  // RLE export scratch
   DevBuf tables, state, brick_job, live, list, lcount, q[3], scal, epoch, front[2];
   DevBuf pcnt, pbase, psums, srec;  // flattened per-face work lists, shell setup
   void* h_tables = nullptr;  // pinned staging

@@ -899,6 +899,18 @@ void parity_raster(cudaStream_t st, const JobDesc* dj, const JobState* ds, int n
   px = px < 1 ? 1 : (px > 64 ? 64 : px);
   k_prefix_x<<<dim3(px, gy), 256, 0, st>>>(dj, njobs);
 }
+void exclusive_scan(cudaStream_t st, const uint32_t* in, unsigned long long* out,
+                    unsigned long long* sums, uint32_t n, unsigned long long* total) {
+  if (!n) {
+    cudaMemsetAsync(total, 0, sizeof(unsigned long long), st);
+    return;
+  }
+  const uint32_t nb = (n + 1023) / 1024;
+  k_scan_local<<<nb, 1024, 0, st>>>(in, out, sums, n);
+  k_scan_sums<<<1, 1024, 0, st>>>(sums, nb, total);
+  k_scan_add<<<(n + 255) / 256, 256, 0, st>>>(out, sums, n);
+}
+
 void shell_sat(cudaStream_t st, const JobDesc* dj, int njobs, uint32_t total_faces,
                const FaceScratch& fs, int num_sms, int grid_mult) {
   if (!total_faces) return;
