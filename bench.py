@@ -189,8 +189,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--jobs", type=int, default=256)
     ap.add_argument("--plain-jobs", type=int, default=32)
-    ap.add_argument("--serve-rate", type=float, default=400.0)
-    ap.add_argument("--serve-seconds", type=float, default=3.0)
+    ap.add_argument("--serve-rates", default="100,400,1000,2000",
+                    help="Poisson arrival rates (jobs/s) of the serving sweep")
+    ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrivals per rate")
+    ap.add_argument("--configs", action="store_true",
+                    help="single-instance configurations 1-3 (128^3, 256^3, 512^3 vessels): "
+                         "one JSON line each with batched, plain and CPU times and a parity check")
     ap.add_argument("--cpu-stride", type=int, default=2,
                     help="cpu_baseline sample: every n-th job of the workload (2: about 10-15 s)")
     ap.add_argument("--ref-stride", type=int, default=4,
@@ -201,6 +205,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.configs:
+        return single_configs(args)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -308,7 +314,11 @@ def main():
     # ---- serving: Poisson arrivals, continuous batching -----------------
     serving = None
     if not args.no_serve and args.serve_seconds > 0:
-        serving = serve(V, ctx, jobs, args.serve_rate, args.serve_seconds)
+        rates = [float(r) for r in args.serve_rates.split(",") if r]
+        sweep = serve_sweep(V, ctx, jobs, rates, args.serve_seconds)
+        serving = {"sweep": sweep,
+                   "note": "Poisson arrivals of mixed-256 jobs (pool of 64 distinct jobs cycled) "
+                           "through vf_server_*: latency = submit to labels in host memory"}
 
     # ---- CPU baseline (oracle) on a bounded sample -----------------------
     cpu = None
@@ -361,44 +371,131 @@ def main():
     return 0
 
 
-def serve(V, ctx, jobs, rate, seconds, pool=64, copies=4):
-    """Poisson arrivals of mixed-256 jobs at `rate` jobs/s for `seconds`."""
+def serve_sweep(V, ctx, jobs, rates, seconds, pool=64, copies=4):
+    """Poisson arrivals of mixed-256 jobs at each rate (jobs/s) for `seconds`."""
     from voxelfragmentml_gb300 import workloads as W
     base = [W.to_spec(j, V, want_labels=False, ncounts=256, pinned=True) for j in jobs[:pool]]
     outs = {}
     for k in range(copies):
         for i, s in enumerate(base):
             outs[(i, k)] = V.pinned_array(s.dims, np.uint16)
-    srv = V.Server(ctx, max_inflight=3, max_batch=32)
-    rng = np.random.default_rng(7)
-    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * seconds * 2) + 16))
-    arrivals = arrivals[arrivals < seconds]
-    results = []
-    t0 = time.perf_counter()
-    vox = 0
-    for n, at in enumerate(arrivals):
-        now = time.perf_counter() - t0
-        if at > now:
-            time.sleep(at - now)
-        i = n % pool
-        s = base[i]
-        s.labels = outs[(i, (n // pool) % copies)]
-        s.tag = n
-        srv.submit(s)
-        vox += int(np.prod(s.dims))
-        results += srv.poll(256, 0)
-    deadline = time.perf_counter() + 120
-    while len(results) < len(arrivals) and time.perf_counter() < deadline:
-        results += srv.poll(256, 50)
-    span = time.perf_counter() - t0
-    srv.close()
-    lat = sorted(r.done_ms - r.submit_ms for r in results)
-    ok = sum(1 for r in results if r.status == 0)
-    return {"rate_jobs_per_s": rate, "seconds": seconds, "submitted": int(len(arrivals)),
-            "completed_ok": ok, "p50_ms": float(np.percentile(lat, 50)) if lat else None,
-            "p99_ms": float(np.percentile(lat, 99)) if lat else None,
-            "sustained_voxels_per_s": vox / span,
-            "note": "latency = submit to labels on host; pool of 64 distinct jobs cycled"}
+    sweep = []
+    for rate in rates:
+        srv = V.Server(ctx, max_inflight=3, max_batch=32)
+        rng = np.random.default_rng(7)
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * seconds * 2) + 16))
+        arrivals = arrivals[arrivals < seconds]
+        results = []
+        t0 = time.perf_counter()
+        vox = 0
+        for n, at in enumerate(arrivals):
+            now = time.perf_counter() - t0
+            if at > now:
+                time.sleep(at - now)
+            i = n % pool
+            s = base[i]
+            s.labels = outs[(i, (n // pool) % copies)]
+            s.tag = n
+            srv.submit(s)
+            vox += int(np.prod(s.dims))
+            results += srv.poll(256, 0)
+        offered = time.perf_counter() - t0
+        deadline = time.perf_counter() + 120
+        while len(results) < len(arrivals) and time.perf_counter() < deadline:
+            results += srv.poll(256, 50)
+        span = time.perf_counter() - t0
+        srv.close()
+        lat = sorted(r.done_ms - r.submit_ms for r in results)
+        ok = sum(1 for r in results if r.status == 0)
+        sweep.append({"rate_jobs_per_s": rate, "seconds": seconds, "submitted": int(len(arrivals)),
+                      "achieved_arrival_rate": len(arrivals) / max(offered, 1e-9),
+                      "completed_ok": ok,
+                      "p50_ms": float(np.percentile(lat, 50)) if lat else None,
+                      "p99_ms": float(np.percentile(lat, 99)) if lat else None,
+                      "sustained_voxels_per_s": vox / span})
+    return sweep
+
+
+def single_configs(args):
+    """Configurations 1-3 as single jobs: device time with resident inputs,
+    end-to-end vf_batch_run, the plain per-job path, the CPU oracle, and the
+    labels checked against the oracle's."""
+    import oracle as O
+    import voxelfragmentml_gb300 as V
+    from voxelfragmentml_gb300 import build as B, workloads as W
+    B.build()
+    O.build()
+    cfgs = [
+        ("1: 128x96 vessel, 128^3, 8 fragments, Manhattan",
+         W.single(128, 128, 96, 8, 1, 0.0, 16, False, 42, 42)),
+        ("2: 256x192 vessel, 256^3, 16 fragments, Euclidean, noise A=2 P=16, one 3x3x3 erosion",
+         W.single(256, 256, 192, 16, 0, 2.0, 16, True, 42, 42)),
+        ("3: 512x384 vessel, 512^3, 64 fragments, Chebyshev, noise A=2 P=16",
+         W.single(512, 512, 384, 64, 2, 2.0, 16, False, 42, 42)),
+    ]
+    ctx = V.Context(0)
+    L = V.lib()
+    import ctypes as C
+    for name, job in cfgs:
+        spec = W.to_spec(job, V, want_labels=True, ncounts=256, pinned=True)
+        vox = int(np.prod(spec.dims))
+        rb = V.ResidentBatch([spec], ctx)
+        for _ in range(2):
+            rb.execute(download=False)
+        ctx.synchronize()
+        reps = 5
+        L.vf_ctx_event_record(ctx.h, 0)
+        for _ in range(reps):
+            rb.execute(download=False)
+        L.vf_ctx_event_record(ctx.h, 1)
+        ctx.synchronize()
+        ms = C.c_float()
+        L.vf_ctx_event_elapsed(ctx.h, 0, 1, C.byref(ms))
+        dev_ms = ms.value / reps
+        stages = ctx.stage_ms()
+        st = ctx.last_stats()
+        V.batch_run([spec], ctx)
+        t = time.perf_counter()
+        for _ in range(reps):
+            (r,) = V.batch_run([spec], ctx)
+        e2e_ms = 1000.0 * (time.perf_counter() - t) / reps
+        got = spec.labels.copy()
+        plain = W.to_spec(job, V, want_labels=True, ncounts=256, pinned=True)
+        V.plain_run([plain], ctx)
+        t = time.perf_counter()
+        (pr,) = V.plain_run([plain], ctx)
+        plain_ms = 1000.0 * (time.perf_counter() - t)
+        v, f = W.mesh_for(job)
+        q = O.Params()
+        base = dict(algorithm=1, distance=2, num_seeds=8, num_extra_seeds=0, merge_distance=0,
+                    seed_location=2, seed=80, noise_amplitude=0.0, noise_period=16, erode=0,
+                    erosion_type=1, erosion_size=3, erosion_iterations=3, erosion_probability=0.5,
+                    erosion_threshold=0.5, boundary_size=1)
+        base.update(W.params_for(job, V))
+        for k, val in base.items():
+            setattr(q, k, val)
+        t = time.perf_counter()
+        lab, cnt, _ = O.run_job(v, f, spec.dims, spec.aabb[0], spec.aabb[1], q)
+        cpu_ms = 1000.0 * (time.perf_counter() - t)
+        flood_bytes = 4.0 * 8192 * st["flood_visits"]
+        print(json.dumps({
+            "config": name, "dims": list(spec.dims), "voxels": vox, "triangles": int(spec.faces.shape[0]),
+            "batched_device_ms": dev_ms, "batched_voxels_per_s": vox / (dev_ms / 1e3),
+            "e2e_ms": e2e_ms, "e2e_voxels_per_s": vox / (e2e_ms / 1e3),
+            "plain_ms": plain_ms, "plain_voxels_per_s": vox / (plain_ms / 1e3),
+            "plain_bfs_waves": int(pr.flood_passes),
+            "cpu_oracle_ms": cpu_ms, "cpu_voxels_per_s": vox / (cpu_ms / 1e3), "cpu_cores": os.cpu_count(),
+            "stages_ms": stages,
+            "flood": {"k_relax_ms": st["flood_ms"], "brick_visits": st["flood_visits"],
+                      "passes": st["flood_passes"],
+                      "hbm_frac": (flood_bytes / (st["flood_ms"] / 1e3) / 1e9) / _peaks()[0]
+                      if st["flood_ms"] else None},
+            "labels_equal_oracle": bool(np.array_equal(got, lab)),
+            "plain_equals_batched": bool(np.array_equal(plain.labels, got)),
+            "counts_equal_oracle": bool(np.array_equal(spec.counts, cnt[:spec.counts.shape[0]])
+                                        and not cnt[spec.counts.shape[0]:].any())}), flush=True)
+    ctx.close()
+    return 0
 
 
 if __name__ == "__main__":
