@@ -208,14 +208,12 @@ def main():
     if args.configs:
         return single_configs(args)
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
+    from voxelfragmentml_gb300 import replicas as R
+    # replicas: every rank runs the whole workload on its own GPU; no collective on
+    # the data path (jobs are independent), timings max-reduced over gloo
+    world = R.init()
+    rank = R.rank()
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        # replicas: every rank runs the whole workload on its own GPU; no collective on
-        # the data path (jobs are independent)
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
     from voxelfragmentml_gb300 import build as B
     B.build()
     import voxelfragmentml_gb300 as V
@@ -241,8 +239,7 @@ def main():
     L = V.lib()
     clocks = Clocks()
     clocks.start()
-    if world > 1:
-        dist.barrier()
+    R.barrier()
     ctx.synchronize()
     L.vf_ctx_event_record(ctx.h, 0)
     launches, flood_ms, flood_bytes, visits, passes, sweeps, maxit = 0, 0.0, 0, 0, 0, 0, 0
@@ -268,11 +265,7 @@ def main():
     msv = C.c_float()
     L.vf_ctx_event_elapsed(ctx.h, 0, 1, C.byref(msv))
     dev_ms = msv.value
-    if world > 1:
-        import torch
-        t = torch.tensor([dev_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_ms = float(t.item())
+    dev_ms = R.max_over_ranks(dev_ms)
     ms_per_step = dev_ms / args.steps
     value = voxels * args.steps * world / (dev_ms / 1000.0)
 
@@ -288,7 +281,7 @@ def main():
     ctx.synchronize()
     wall_e2e = time.perf_counter() - t0
     L.vf_ctx_event_elapsed(ctx.h, 2, 3, C.byref(msv))
-    e2e_ms = max(msv.value, 1e-6)
+    e2e_ms = R.max_over_ranks(max(msv.value, 1e-6))
     e2e_value = voxels * args.steps * world / (e2e_ms / 1000.0)
     clk = clocks.stop()
     assert all(r.status == 0 for r in res)
@@ -366,8 +359,7 @@ def main():
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
-    if world > 1:
-        dist.destroy_process_group()
+    R.finalize()
     return 0
 
 
