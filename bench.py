@@ -243,7 +243,7 @@ def main():
     ctx.synchronize()
     L.vf_ctx_event_record(ctx.h, 0)
     launches, flood_ms, flood_bytes, visits, passes, sweeps, maxit = 0, 0.0, 0, 0, 0, 0, 0
-    act_rows, key_changes = 0, 0
+    act_rows, key_changes, busy_warps = 0, 0, 0
     stage_tot = {}
     for _ in range(args.steps):
         rb.execute(download=False)
@@ -257,6 +257,7 @@ def main():
         maxit += st["flood_maxit_hits"]
         act_rows += st["flood_active_row_sweeps"]
         key_changes += st["flood_key_changes"]
+        busy_warps += st["flood_busy_warp_sweeps"]
         for k, v in ctx.stage_ms().items():
             stage_tot[k] = stage_tot.get(k, 0.0) + v
     L.vf_ctx_event_record(ctx.h, 1)
@@ -336,6 +337,7 @@ def main():
             "sweeps_per_visit": sweeps / max(visits, 1),
             "visits_at_sweep_cap": maxit / args.steps,
             "active_rows_per_sweep": act_rows / max(sweeps, 1),
+            "busy_warps_per_sweep": busy_warps / max(sweeps, 1),
             "key_changes_per_visit": key_changes / max(visits, 1),
             "launch_ms": flood_launch_ms,
             "traffic": K_RELAX_DRAM_BYTES_PER_VISIT * visits / args.steps,

@@ -288,9 +288,9 @@ vf_status vf_ctx_stage_ms(vf_ctx* ctx, float* ms, uint32_t n);
 vf_status vf_ctx_flood_stats(vf_ctx* ctx, uint64_t* passes, uint64_t* sweeps,
                              uint64_t* maxit_hits);
 /* raw flood counters of the last batched run: [0] brick visits, [1] passes,
- * [2] unused, [3] barrier timeouts, [4] sweeps, [5] visits at the sweep cap,
- * [6] active rows summed over sweeps, [7] voxel key changes.  n <= 8 are
- * filled, the rest zeroed. */
+ * [2] warps with work summed over sweeps (8 warps per brick), [3] barrier
+ * timeouts, [4] sweeps, [5] visits at the sweep cap, [6] active rows summed
+ * over sweeps, [7] voxel key changes.  n <= 8 are filled, the rest zeroed. */
 vf_status vf_ctx_flood_counters(vf_ctx* ctx, uint64_t* out, uint32_t n);
 /* *replayed = 1 when the last vf_batch_execute ran its stage chain as a
  * CUDA graph (captured on the first execute after vf_batch_prepare, replayed

@@ -238,6 +238,7 @@ class Context:
         return {"launches": la.value, "flood_ms": ms.value, "flood_bytes": by.value,
                 "flood_visits": vis.value, "flood_passes": pa.value, "flood_sweeps": sw.value,
                 "flood_maxit_hits": mh.value, "flood_active_row_sweeps": cn[6],
+                "flood_busy_warp_sweeps": cn[2],
                 "flood_key_changes": cn[7]}
 
 

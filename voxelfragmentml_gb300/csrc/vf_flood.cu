@@ -50,7 +50,8 @@ struct FloodArgs {
   uint32_t* epoch;
   uint32_t* bar;     // [2]
   uint32_t* err;
-  uint32_t* stats;   // [0] visits, [1] passes, [2] overflow, [3] timeout
+  uint32_t* stats;   // [0] visits, [1] passes, [2] busy warp-sweeps, [3] timeout, [4] sweeps,
+                     // [5] visits at the sweep cap, [6] active row-sweeps, [7] key changes
   uint32_t max_passes;
   int max_sweeps;    // sweeps per brick visit before the brick re-queues itself
 };
@@ -128,8 +129,8 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
       l = a.live[brick_id(J, nx, ny, nz)];
     live27[t] = l;
   }
-  __shared__ uint32_t scnt[2];
-  if (t == 0) { *dirs = 0; *reenq = 0; scnt[0] = 0; scnt[1] = 0; }
+  __shared__ uint32_t scnt[3];
+  if (t == 0) { *dirs = 0; *reenq = 0; scnt[0] = 0; scnt[1] = 0; scnt[2] = 0; }
   __syncthreads();
   // stage keys: rows [x0-1, x0+17) x [y0-1, y0+17), z [z0-4, z0+36)
   for (int q = t; q < KROWS * KZW; q += blockDim.x) {
@@ -155,7 +156,7 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     const uint4 w = *reinterpret_cast<const uint4*>(own_row + 4 + 4 * q);
     k[4 * q] = w.x; k[4 * q + 1] = w.y; k[4 * q + 2] = w.z; k[4 * q + 3] = w.w;
   }
-  uint32_t changed = 0, overflow = 0, nact = 0, nchg = 0;
+  uint32_t changed = 0, overflow = 0, nact = 0, nchg = 0, nwarp = 0;
   // rflag[b][row]: the row changed in the previous sweep.  Every interior row
   // runs in sweep 0 (new halo data); later only rows next to a change run.
   for (int q = t; q < KROWS; q += blockDim.x) {
@@ -253,6 +254,7 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     changed |= chg;
     cur ^= 1;
     if (active) ++nact;
+    nwarp += __any_sync(0xFFFFFFFFu, active) ? 1u : 0u;  // warps with work in this sweep
     nchg += __popc(chg);
     if (!__syncthreads_or(chg != 0)) break;
   }
@@ -295,6 +297,7 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
   // statistics: active row-sweeps and key changes (block sums in shared memory)
   if (nact) atomicAdd(&scnt[0], nact);
   if (nchg) atomicAdd(&scnt[1], nchg);
+  if ((t & 31) == 0 && nwarp) atomicAdd(&scnt[2], nwarp);
   if (t == 0) {
     if (it == a.max_sweeps) *reenq = 1;
     atomicAdd(a.stats + 4, (uint32_t)it + 1u);  // sweeps (statistics)
@@ -304,6 +307,7 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
   if (t == 0) {
     atomicAdd(a.stats + 6, scnt[0]);
     atomicAdd(a.stats + 7, scnt[1]);
+    atomicAdd(a.stats + 2, scnt[2]);
   }
   if (t < 32) {
     const uint32_t dm = *dirs;
@@ -376,13 +380,19 @@ __global__ void __launch_bounds__(256) k_init_keys(const JobDesc* jobs, const ui
     const uint32_t x = bx * VF_BX + threadIdx.x / VF_BY, y = by * VF_BY + threadIdx.x % VF_BY;
     const uint32_t z0 = bz * VF_BZ;
     if (x >= J.X || y >= J.Y) continue;
-    const uint32_t* g = reinterpret_cast<const uint32_t*>(J.grid + vf_gidx(J, x, y, z0));
+    const uint2* g = reinterpret_cast<const uint2*>(J.grid + vf_gidx(J, x, y, z0));
     uint4* d = reinterpret_cast<uint4*>(J.keys + vf_kidx(J, x, y, z0));
     const uint32_t nq = min((uint32_t)VF_BZ, J.Zk - z0) / 4;
-    for (uint32_t q = 0; q < nq; ++q) {
-      const uint32_t a0 = g[2 * q], a1 = g[2 * q + 1];  // Zp >= Zk, both multiples of 4
-      __stcg(d + q, make_uint4((a0 & 0xFFFFu) ? 1u : 0u, (a0 >> 16) ? 1u : 0u,
-                               (a1 & 0xFFFFu) ? 1u : 0u, (a1 >> 16) ? 1u : 0u));
+    // the row's label loads first, then the key stores (Zp >= Zk, both
+    // multiples of 4: 4 labels = one 8-byte word)
+    uint2 a[VF_BZ / 4];
+#pragma unroll
+    for (uint32_t q = 0; q < VF_BZ / 4; ++q) a[q] = q < nq ? g[q] : make_uint2(0, 0);
+#pragma unroll
+    for (uint32_t q = 0; q < VF_BZ / 4; ++q) {
+      if (q >= nq) break;
+      __stcg(d + q, make_uint4((a[q].x & 0xFFFFu) ? 1u : 0u, (a[q].x >> 16) ? 1u : 0u,
+                               (a[q].y & 0xFFFFu) ? 1u : 0u, (a[q].y >> 16) ? 1u : 0u));
     }
   }
 }
@@ -452,11 +462,17 @@ __global__ void __launch_bounds__(256) k_finalize(const JobDesc* jobs, const Job
     const uint32_t z0 = bz * VF_BZ;
     if (x >= J.X || y >= J.Y) continue;
     const uint4* kk = reinterpret_cast<const uint4*>(J.keys + vf_kidx(J, x, y, z0));
-    uint32_t* g = reinterpret_cast<uint32_t*>(J.grid + vf_gidx(J, x, y, z0));
+    uint2* g = reinterpret_cast<uint2*>(J.grid + vf_gidx(J, x, y, z0));
     const uint32_t nq = min((uint32_t)VF_BZ, J.Zk - z0) / 4;
-    for (uint32_t q = 0; q < nq; ++q) {
-      const uint4 k4 = __ldcg(kk + q);
-      const uint32_t ks[4] = {k4.x, k4.y, k4.z, k4.w};
+    // all key loads of the row first (the row's 8 loads in flight together),
+    // then the label lookups and the stores
+    uint4 k4[VF_BZ / 4];
+#pragma unroll
+    for (uint32_t q = 0; q < VF_BZ / 4; ++q) k4[q] = q < nq ? __ldcg(kk + q) : make_uint4(0, 0, 0, 0);
+#pragma unroll
+    for (uint32_t q = 0; q < VF_BZ / 4; ++q) {
+      if (q >= nq) break;
+      const uint32_t ks[4] = {k4[q].x, k4[q].y, k4[q].z, k4[q].w};
       uint32_t lab[4];
 #pragma unroll
       for (int h = 0; h < 4; ++h) {
@@ -471,8 +487,7 @@ __global__ void __launch_bounds__(256) k_finalize(const JobDesc* jobs, const Job
         }
         lab[h] = v;
       }
-      g[2 * q] = lab[0] | (lab[1] << 16);
-      g[2 * q + 1] = lab[2] | (lab[3] << 16);
+      g[q] = make_uint2(lab[0] | (lab[1] << 16), lab[2] | (lab[3] << 16));
     }
   }
 }

@@ -592,8 +592,8 @@ static vfk::FloodScratch flood_scratch(Batch& B) {
   fs.qhead = sc + 4;     // [3]
   fs.barrier = sc + 8;   // [2]
   fs.err = sc + 12;      // [1]
-  fs.stats = sc + 16;    // [8]: visits, passes, -, timeouts, sweeps, MAXIT hits,
-                         // active row-sweeps, changed voxels
+  fs.stats = sc + 16;    // [8]: visits, passes, busy warp-sweeps, timeouts, sweeps,
+                         // sweep-cap hits, active row-sweeps, changed voxels
   fs.epoch = static_cast<uint32_t*>(B.epoch.p);
   fs.max_passes = 1u << 20;
   fs.total_bricks = B.sz.bricks;
