@@ -437,6 +437,119 @@ __global__ void __launch_bounds__(256) k_detect(const JobDesc* jobs, const uint3
   }
 }
 
+// detectBoundaries with boundary size <= 1, by window extrema.  Over the
+// labelled voxels of the clamped 3x3x3 window (masked value u = w & 0x7FFF,
+// labelled when u > 1; voxels outside the grid or the live bricks are 0),
+// let mn / mx be the smallest / largest u.  A voxel g > 1 is a boundary in
+// the reference's test (some labelled u != g) exactly when a labelled voxel
+// exists and not all of them equal g: mn != none and (mn != g or mx != g).
+// The window extrema are separable: phase 1 takes the z-window of every
+// staged row (brick + 1-voxel halo) into two u16x2 planes, phase 2 the 3x3
+// rows around each brick row, both with paired 16-bit min/max.
+constexpr int D1_ROWS = (VF_BX + 2) * (VF_BY + 2);
+constexpr int D1_W = VF_BZ / 2;  // u16 pairs per row
+constexpr int D1_BYTES = Tile<1>::BYTES + 2 * D1_ROWS * D1_W * 4;
+
+__global__ void __launch_bounds__(256, 3) k_detect1(const JobDesc* jobs, const uint32_t* list,
+                                                 const uint32_t* count, const uint32_t* brick_job) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint16_t* tile = reinterpret_cast<uint16_t*>(smem_raw);
+  uint32_t* zmin = reinterpret_cast<uint32_t*>(smem_raw + Tile<1>::BYTES);
+  uint32_t* zmax = zmin + D1_ROWS * D1_W;
+  const uint32_t n = *count;
+  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+    const uint32_t b = list[it];
+    const JobDesc& J = jobs[brick_job[b]];
+    if (!J.active) continue;  // uniform across the CTA
+    uint32_t x0, y0, z0;
+    brick_coords(J, b, x0, y0, z0);
+    __syncthreads();
+    load_tile<1>(J, J.grid, x0, y0, z0, tile);
+    __syncthreads();
+    const bool self_only = J.boundary_size <= 0;  // uniform across the CTA
+    if (!self_only) {
+      // phase 1: z-window extrema of every staged row
+      for (int r = threadIdx.x; r < D1_ROWS; r += blockDim.x) {
+        const uint16_t* row = tile + r * ZW + 8;  // z = z0 + 0
+        uint32_t lo_prev, hi_prev, lo_cur, hi_cur;
+        auto lab = [](uint16_t w, uint32_t& lo, uint32_t& hi) {
+          const uint32_t u = w & 0x7FFFu;
+          lo = u > VOXEL_FREE ? u : 0xFFFFu;
+          hi = u > VOXEL_FREE ? u : 0u;
+        };
+        lab(row[-1], lo_prev, hi_prev);
+        lab(row[0], lo_cur, hi_cur);
+        uint32_t* mnr = zmin + r * D1_W;
+        uint32_t* mxr = zmax + r * D1_W;
+        for (int p = 0; p < D1_W; ++p) {
+          uint32_t lo1, hi1, lo2, hi2;
+          lab(row[2 * p + 1], lo1, hi1);
+          lab(row[2 * p + 2], lo2, hi2);
+          const uint32_t mn0 = min(lo_prev, min(lo_cur, lo1)), mx0 = max(hi_prev, max(hi_cur, hi1));
+          const uint32_t mn1 = min(lo_cur, min(lo1, lo2)), mx1 = max(hi_cur, max(hi1, hi2));
+          mnr[p] = mn0 | (mn1 << 16);
+          mxr[p] = mx0 | (mx1 << 16);
+          lo_prev = lo1; hi_prev = hi1;
+          lo_cur = lo2; hi_cur = hi2;
+        }
+      }
+      __syncthreads();
+    }
+    const int lx = threadIdx.x / VF_BY, ly = threadIdx.x % VF_BY;
+    const uint32_t x = x0 + lx, y = y0 + ly;
+    if (x >= J.X || y >= J.Y) continue;
+    const uint16_t* own = tile + ((lx + 1) * Tile<1>::NY + (ly + 1)) * ZW + 8;
+    // rows are written 8 voxels (16 bytes) at a time, and only where a voxel
+    // was marked; z >= Zp is outside the row
+    uint4* dst = reinterpret_cast<uint4*>(J.grid + vf_gidx(J, x, y, z0));
+    const uint32_t nq = min((uint32_t)VF_BZ, J.Zp - z0) / 8;
+#pragma unroll 1
+    for (uint32_t q = 0; q < nq; ++q) {
+      uint32_t out[4];
+      bool any = false;
+      if (self_only) {
+        // the window is the voxel itself: only a marked voxel can differ from
+        // its own masked value
+#pragma unroll
+        for (int h = 0; h < 8; ++h) {
+          const uint16_t g = own[8 * q + h];
+          const uint32_t u = g & 0x7FFFu;
+          const bool bd = g > VOXEL_FREE && u > VOXEL_FREE && u != g;
+          const uint32_t o = bd ? (uint32_t)(g | 0x8000u) : (uint32_t)g;
+          if (h & 1) out[h >> 1] |= o << 16; else out[h >> 1] = o;
+          any |= bd;
+        }
+      } else {
+        // phase 2: the 3x3 rows around this row
+        uint4 mn = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+        uint4 mx = make_uint4(0, 0, 0, 0);
+#pragma unroll 3
+        for (int r = 0; r < 9; ++r) {
+          const int row = (lx + r / 3) * Tile<1>::NY + (ly + r % 3);
+          const uint4 a = reinterpret_cast<const uint4*>(zmin + row * D1_W)[q];
+          const uint4 c = reinterpret_cast<const uint4*>(zmax + row * D1_W)[q];
+          mn.x = __vminu2(mn.x, a.x); mn.y = __vminu2(mn.y, a.y);
+          mn.z = __vminu2(mn.z, a.z); mn.w = __vminu2(mn.w, a.w);
+          mx.x = __vmaxu2(mx.x, c.x); mx.y = __vmaxu2(mx.y, c.y);
+          mx.z = __vmaxu2(mx.z, c.z); mx.w = __vmaxu2(mx.w, c.w);
+        }
+        const uint32_t mns[4] = {mn.x, mn.y, mn.z, mn.w}, mxs[4] = {mx.x, mx.y, mx.z, mx.w};
+#pragma unroll
+        for (int h = 0; h < 8; ++h) {
+          const uint32_t lo = (mns[h >> 1] >> (16 * (h & 1))) & 0xFFFFu;
+          const uint32_t hi = (mxs[h >> 1] >> (16 * (h & 1))) & 0xFFFFu;
+          const uint16_t g = own[8 * q + h];
+          const bool bd = g > VOXEL_FREE && lo != 0xFFFFu && (lo != g || hi != g);
+          const uint32_t o = bd ? (uint32_t)(g | 0x8000u) : (uint32_t)g;
+          if (h & 1) out[h >> 1] |= o << 16; else out[h >> 1] = o;
+          any |= bd;
+        }
+      }
+      if (any) dst[q] = make_uint4(out[0], out[1], out[2], out[3]);
+    }
+  }
+}
+
 // erodeGrid-comp.glsl:26-59: src -> dst.  Gate bool(unmaskedBit(v,15)) holds
 // for every labelled voxel; full 16-bit equality; globalCount = clamped
 // window size; noise[idx % 1e6] from the counter RNG.
@@ -652,9 +765,14 @@ static void detect_h(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
 }
 void detect_boundaries(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
                        const uint32_t* count, uint32_t max_count, const uint32_t* brick_job) {
-  // boundary sizes 0..3 share the H = 3 tile; 1 (the default) uses H = 1
+  // boundary sizes 0..1 (the default): window extrema; 2..3: detect_boundaries_wide
   if (!max_count) return;
-  detect_h<1>(st, dj, list, count, max_count, brick_job);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_detect1, cudaFuncAttributeMaxDynamicSharedMemorySize, D1_BYTES);
+    attr = true;
+  }
+  k_detect1<<<brick_grid(max_count), 256, D1_BYTES, st>>>(dj, list, count, brick_job);
 }
 void detect_boundaries_wide(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
                             const uint32_t* count, uint32_t max_count, const uint32_t* brick_job) {
