@@ -334,34 +334,6 @@ __device__ __forceinline__ float lerp_(float a, float b, float t) {
   return __fadd_rn(a, __fmul_rn(t, __fsub_rn(b, a)));
 }
 
-__device__ __forceinline__ uint16_t perturb_voxel(const JobDesc& J, const uint16_t* src, uint32_t x,
-                                                  uint32_t y, uint32_t z, uint16_t g) {
-  const uint32_t P = J.noise_period;
-  const float fp = (float)P;
-  const uint32_t i0 = x / P, i1 = y / P, i2 = z / P;
-  const float t0 = __fdiv_rn((float)(x % P), fp), t1 = __fdiv_rn((float)(y % P), fp),
-              t2 = __fdiv_rn((float)(z % P), fp);
-  const uint32_t sy = J.lat_nz * 3, sx = J.lat_ny * sy;
-  const float* L = J.lattice + (size_t)i0 * sx + (size_t)i1 * sy + (size_t)i2 * 3;
-  int o[3];
-#pragma unroll
-  for (int ch = 0; ch < 3; ++ch) {
-    const float c000 = L[ch], c001 = L[3 + ch];
-    const float c010 = L[sy + ch], c011 = L[sy + 3 + ch];
-    const float c100 = L[sx + ch], c101 = L[sx + 3 + ch];
-    const float c110 = L[sx + sy + ch], c111 = L[sx + sy + 3 + ch];
-    const float c00 = lerp_(c000, c001, t2), c01 = lerp_(c010, c011, t2);
-    const float c10 = lerp_(c100, c101, t2), c11 = lerp_(c110, c111, t2);
-    const float c0 = lerp_(c00, c01, t1), c1 = lerp_(c10, c11, t1);
-    const float nz = lerp_(c0, c1, t0);
-    o[ch] = (int)floorf(__fadd_rn(__fmul_rn(J.noise_amplitude, nz), 0.5f));
-  }
-  const long ux = (long)x + o[0], uy = (long)y + o[1], uz = (long)z + o[2];
-  if (ux < 0 || uy < 0 || uz < 0 || ux >= (long)J.X || uy >= (long)J.Y || uz >= (long)J.Z) return g;
-  const uint16_t u = src[vf_gidx(J, (uint32_t)ux, (uint32_t)uy, (uint32_t)uz)];
-  return u > VOXEL_FREE ? u : g;
-}
-
 __global__ void __launch_bounds__(256) k_perturb(const JobDesc* jobs, const uint32_t* list,
                                                  const uint32_t* count, const uint32_t* brick_job) {
   const uint32_t n = *count;
@@ -385,9 +357,49 @@ __global__ void __launch_bounds__(256) k_perturb(const JobDesc* jobs, const uint
       v[8 * q + 4] = w.z & 0xFFFF; v[8 * q + 5] = w.z >> 16;
       v[8 * q + 6] = w.w & 0xFFFF; v[8 * q + 7] = w.w >> 16;
     }
-#pragma unroll 4
-    for (int z = 0; z < VF_BZ; ++z)
-      if (v[z] > VOXEL_FREE) v[z] = perturb_voxel(J, src, x, y, z0 + z, v[z]);
+    // Per labelled voxel: a 3-channel trilinear value noise n(v / P) from the
+    // lattice (lerp along z, then y, then x, as the oracle), offset
+    // floor(A * n + 0.5) per axis, and the label found there if it is labelled.
+    // The lattice cell of this row changes only every P voxels along z: its
+    // 8 corners x 3 channels stay in registers; t0, t1 are per row.
+    const uint32_t P = J.noise_period;
+    const float fp = (float)P;
+    const float t0 = __fdiv_rn((float)(x % P), fp), t1 = __fdiv_rn((float)(y % P), fp);
+    const uint32_t sy = J.lat_nz * 3, sx = J.lat_ny * sy;
+    const float* Lrow = J.lattice + (size_t)(x / P) * sx + (size_t)(y / P) * sy;
+    float cn[3][8];
+    uint32_t cached = 0xFFFFFFFFu;
+#pragma unroll 1
+    for (int z = 0; z < VF_BZ; ++z) {
+      if (v[z] <= VOXEL_FREE) continue;
+      const uint32_t gz = z0 + z;
+      const uint32_t i2 = gz / P;
+      if (i2 != cached) {
+        cached = i2;
+        const float* L = Lrow + (size_t)i2 * 3;
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+          cn[ch][0] = L[ch];           cn[ch][1] = L[3 + ch];
+          cn[ch][2] = L[sy + ch];      cn[ch][3] = L[sy + 3 + ch];
+          cn[ch][4] = L[sx + ch];      cn[ch][5] = L[sx + 3 + ch];
+          cn[ch][6] = L[sx + sy + ch]; cn[ch][7] = L[sx + sy + 3 + ch];
+        }
+      }
+      const float t2 = __fdiv_rn((float)(gz % P), fp);
+      int o[3];
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) {
+        const float c00 = lerp_(cn[ch][0], cn[ch][1], t2), c01 = lerp_(cn[ch][2], cn[ch][3], t2);
+        const float c10 = lerp_(cn[ch][4], cn[ch][5], t2), c11 = lerp_(cn[ch][6], cn[ch][7], t2);
+        const float c0 = lerp_(c00, c01, t1), c1 = lerp_(c10, c11, t1);
+        const float nz = lerp_(c0, c1, t0);
+        o[ch] = (int)floorf(__fadd_rn(__fmul_rn(J.noise_amplitude, nz), 0.5f));
+      }
+      const long ux = (long)x + o[0], uy = (long)y + o[1], uz = (long)gz + o[2];
+      if (ux < 0 || uy < 0 || uz < 0 || ux >= (long)J.X || uy >= (long)J.Y || uz >= (long)J.Z) continue;
+      const uint16_t u = src[vf_gidx(J, (uint32_t)ux, (uint32_t)uy, (uint32_t)uz)];
+      if (u > VOXEL_FREE) v[z] = u;
+    }
     store_row(J, J.grid2, x, y, z0, v);
   }
 }
