@@ -283,6 +283,7 @@ def main():
     wall_e2e = time.perf_counter() - t0
     L.vf_ctx_event_elapsed(ctx.h, 2, 3, C.byref(msv))
     e2e_ms = R.max_over_ranks(max(msv.value, 1e-6))
+    e2e_stages = ctx.stage_ms()  # the last end-to-end step, per stage
     e2e_value = voxels * args.steps * world / (e2e_ms / 1000.0)
     clk = clocks.stop()
     assert all(r.status == 0 for r in res)
@@ -354,6 +355,7 @@ def main():
                        "tuning": tuning},
             "e2e": {"value": e2e_value, "unit": "voxels/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms / args.steps,
+                    "stages_ms_last_step": {k: round(v, 3) for k, v in e2e_stages.items()},
                     "wall_ms_per_step": 1000.0 * wall_e2e / args.steps},
             "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
             "gpu_launches": launches, "plain": plain, "serving": serving,

@@ -125,6 +125,25 @@ def test_autotune_and_settings_do_not_change_results(vf, ctx):
         ctx.set_tuning(**saved)
 
 
+def test_pinned_outputs_any_dims_match_pageable(vf, ctx):
+    # pinned outputs are written by the download kernels (16-byte units when
+    # Z % 4 == 0, rows otherwise); pageable ones by copies: same bits
+    dims_list = [(30, 27, 25), (31, 22, 36), (24, 40, 44), (17, 19, 23)]
+    mk = lambda pinned: [_job(vf, 60 + i, pinned=pinned) for i in range(len(dims_list))]
+    a, b = mk(True), mk(False)
+    for lst in (a, b):
+        for s, d in zip(lst, dims_list):
+            s.dims = d
+            if s.labels is not None:
+                s.labels = (vf.pinned_array(d, np.uint16) if lst is a else np.zeros(d, np.uint16))
+                s.labels[...] = 0
+    ra, rb_ = vf.batch_run(a, ctx), vf.batch_run(b, ctx)
+    for x, y, r1, r2 in zip(a, b, ra, rb_):
+        assert r1.status == 0 and r2.status == 0
+        assert np.array_equal(x.labels, y.labels) and np.array_equal(x.counts, y.counts)
+        assert (x.labels != 0).any()
+
+
 def test_plain_matches_batched(vf, ctx):
     specs = [_job(vf, i) for i in range(6)]
     plain = [_job(vf, i) for i in range(6)]

@@ -11,6 +11,8 @@
 //
 // The CTAs of a launch loop over the live-brick list (its length is read on
 // the device, so launches need no host synchronisation).
+#include <algorithm>
+
 #include "vf_kernels.h"
 
 #include <cfloat>
@@ -706,6 +708,34 @@ __global__ void __launch_bounds__(256) k_counts(const JobDesc* jobs, JobState* s
 
 
 // ---------------------------------------------------------------------------
+// label download, 16-byte path (Z % 4 == 0, destination 16-byte aligned):
+// the job's output is a flat array of X*Y*Z labels written in 16-byte units
+// (8 labels); each unit is two 8-byte halves, and a half never crosses a row
+// (Z % 4 == 0), so it is one 8-byte load from row (e / Z) at z = e % Z.  Units
+// go to consecutive lanes, so every warp store is 512 contiguous bytes.
+__global__ void __launch_bounds__(256) k_pack16(const JobDesc* jobs, int njobs) {
+  for (int j = blockIdx.y; j < njobs; j += gridDim.y) {
+    const JobDesc& J = jobs[j];
+    if (!J.out || (J.Z & 3u) || (reinterpret_cast<uintptr_t>(J.out) & 15u)) continue;
+    const unsigned long long total = (unsigned long long)J.X * J.Y * J.Z;
+    const unsigned long long units = total / 8;
+    uint4* d = reinterpret_cast<uint4*>(J.out);
+    for (unsigned long long u = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; u < units;
+         u += (unsigned long long)gridDim.x * blockDim.x) {
+      const unsigned long long e0 = 8 * u, e1 = e0 + 4;
+      const unsigned long long r0 = e0 / J.Z, r1 = e1 / J.Z;
+      const uint2 a = *reinterpret_cast<const uint2*>(J.grid + r0 * J.Zp + (e0 - r0 * J.Z));
+      const uint2 b = *reinterpret_cast<const uint2*>(J.grid + r1 * J.Zp + (e1 - r1 * J.Z));
+      d[u] = make_uint4(a.x, a.y, b.x, b.y);
+    }
+    // the last total % 8 labels (a multiple of 4)
+    if (blockIdx.x == 0 && threadIdx.x == 0 && (total & 7u)) {
+      const unsigned long long e = total - 4, r = e / J.Z;
+      *reinterpret_cast<uint2*>(J.out + e) = *reinterpret_cast<const uint2*>(J.grid + r * J.Zp + (e - r * J.Z));
+    }
+  }
+}
+
 // label download: one warp per (x, y) row, the final grid (row pitch Zp) into
 // the caller's buffer (row pitch Z); 8-byte stores when Z % 4 == 0 and the
 // destination is 8-byte aligned
@@ -722,6 +752,7 @@ __global__ void __launch_bounds__(256) k_pack(const JobDesc* jobs, int njobs,
     }
     const JobDesc& J = jobs[lo];
     if (!J.out) continue;
+    if ((J.Z & 3u) == 0u && (reinterpret_cast<uintptr_t>(J.out) & 15u) == 0u) continue;  // k_pack16
     const unsigned long long lr = r - J.row_base;
     const uint16_t* src = J.grid + lr * J.Zp;
     uint16_t* dst = J.out + lr * J.Z;
@@ -824,8 +855,10 @@ void count_values(cudaStream_t st, const JobDesc* dj, JobState* ds, const uint32
 }
 
 void pack_labels(cudaStream_t st, const JobDesc* dj, int njobs, uint64_t total_rows, int num_sms) {
-  if (njobs > 0 && total_rows)
-    k_pack<<<num_sms * 8, 256, 0, st>>>(dj, njobs, (unsigned long long)total_rows);
+  if (njobs <= 0 || !total_rows) return;
+  const int per_job = std::max(1, num_sms * 8 / njobs);
+  k_pack16<<<dim3(per_job, std::min(njobs, 65535)), 256, 0, st>>>(dj, njobs);
+  k_pack<<<num_sms * 8, 256, 0, st>>>(dj, njobs, (unsigned long long)total_rows);
 }
 
 }  // namespace vfk

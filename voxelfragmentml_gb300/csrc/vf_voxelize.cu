@@ -795,7 +795,11 @@ __global__ void __launch_bounds__(256, 3) k_shell_flat(const JobDesc* jobs, cons
 #undef ADD
 #undef SUB
 
-// one CTA per brick, one thread per (x,y) row of 32 z voxels = one word
+// one CTA per brick, one thread per (x,y) row of 32 z voxels = one word.
+// grid2 (the second label buffer) needs zeros in bricks that are not live:
+// stencil tiles read their halo from them.  Live bricks of grid2 are written
+// in full by the first stage that targets it, so only non-live bricks are
+// cleared there (dual != 0).
 __global__ void __launch_bounds__(256) k_combine(const JobDesc* jobs, const uint32_t* brick_job,
                                                  uint32_t total, uint8_t* live, int dual) {
   for (uint32_t b = blockIdx.x; b < total; b += gridDim.x) {
@@ -804,27 +808,29 @@ __global__ void __launch_bounds__(256) k_combine(const JobDesc* jobs, const uint
     const uint32_t bz = lb % J.nbz, by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
     const uint32_t x = bx * VF_BX + threadIdx.x / VF_BY, y = by * VF_BY + threadIdx.x % VF_BY;
     const uint32_t z0 = bz * VF_BZ;
+    const bool inside = x < J.X && y < J.Y;
     uint32_t word = 0;
-    if (x < J.X && y < J.Y) {
+    if (inside) {
       const size_t w = ((size_t)x * J.Y + y) * J.Zw + bz;
       word = J.par[w] | J.shell[w];
-      // bits at z >= Z are never set, so the row padding is written as 0
-      const uint32_t nz = min((uint32_t)VF_BZ, J.Zp - z0);  // multiple of 8
-      uint4* dst = reinterpret_cast<uint4*>(J.grid + vf_gidx(J, x, y, z0));
-      uint4* dst2 = reinterpret_cast<uint4*>(J.grid2 + vf_gidx(J, x, y, z0));
-      for (uint32_t q = 0; q < nz / 8; ++q) {
-        uint32_t bits = word >> (8 * q);
-        uint4 v;
-        v.x = (bits & 1u) | ((bits >> 1) & 1u) << 16;
-        v.y = ((bits >> 2) & 1u) | ((bits >> 3) & 1u) << 16;
-        v.z = ((bits >> 4) & 1u) | ((bits >> 5) & 1u) << 16;
-        v.w = ((bits >> 6) & 1u) | ((bits >> 7) & 1u) << 16;
-        dst[q] = v;
-        if (dual) dst2[q] = v;
-      }
     }
     const int any = __syncthreads_or(word != 0);
     if (threadIdx.x == 0) live[b] = any ? 1 : 0;
+    if (!inside) continue;
+    // bits at z >= Z are never set, so the row padding is written as 0
+    const uint32_t nz = min((uint32_t)VF_BZ, J.Zp - z0);  // multiple of 8
+    uint4* dst = reinterpret_cast<uint4*>(J.grid + vf_gidx(J, x, y, z0));
+    uint4* dst2 = reinterpret_cast<uint4*>(J.grid2 + vf_gidx(J, x, y, z0));
+    for (uint32_t q = 0; q < nz / 8; ++q) {
+      uint32_t bits = word >> (8 * q);
+      uint4 v;
+      v.x = (bits & 1u) | ((bits >> 1) & 1u) << 16;
+      v.y = ((bits >> 2) & 1u) | ((bits >> 3) & 1u) << 16;
+      v.z = ((bits >> 4) & 1u) | ((bits >> 5) & 1u) << 16;
+      v.w = ((bits >> 6) & 1u) | ((bits >> 7) & 1u) << 16;
+      dst[q] = v;
+      if (dual && !any) dst2[q] = v;  // all zero
+    }
   }
 }
 
