@@ -428,3 +428,53 @@ def test_rle_export_after_fracture(vf, ctx, occ64):
     fr.build(g, O.seeder_uniform(occ, 8, 5, 2))
     g.detectBoundaries(1)
     assert g.exportRLE() == O.rle_encode(g.data())
+
+
+# ---- limits and edge cases --------------------------------------------------
+def test_flood_max_seed_count_and_limit(vf, ctx):
+    rng = np.random.default_rng(11)
+    shape = (40, 36, 44)
+    occ = (rng.random(shape) < 0.9).astype(np.uint16)
+    seeds = O.seeder_uniform(occ, 4095, 3, 2)  # the most a flood takes (12-bit slots)
+    assert seeds.shape[0] == 4095
+    g = vf.RegularGrid(shape, None, None, ctx)
+    g.upload(occ)
+    fr = vf.FloodFracturer()
+    fr.setDistanceFunction(vf.CHEBYSHEV)
+    fr.build(g, seeds)
+    exp, _ = O.flood(occ, seeds, vf.CHEBYSHEV)
+    assert np.array_equal(g.data(), exp)
+    more = np.concatenate([seeds, seeds[:1]])
+    with pytest.raises(vf.VFError) as e:
+        fr.build(g, more)
+    assert e.value.status == vf.ERR_RANGE
+
+
+@pytest.mark.parametrize("dfunc", [1, 2])
+def test_flood_long_thin_grid(vf, ctx, dfunc):
+    # a 2048-voxel corridor: geodesic distances far beyond one brick, more than
+    # a hundred brick passes, two fronts meeting in the middle
+    shape = (2048, 2, 4)
+    occ = np.ones(shape, np.uint16)
+    seeds = np.array([[0, 0, 0, 2], [2047, 1, 3, 3]], np.uint32)
+    g = vf.RegularGrid(shape, None, None, ctx)
+    g.upload(occ)
+    fr = vf.FloodFracturer()
+    fr.setDistanceFunction(dfunc)
+    fr.build(g, seeds)
+    exp, _ = O.flood(occ, seeds, dfunc)
+    assert np.array_equal(g.data(), exp)
+
+
+def test_smallest_grid_and_extreme_labels(vf, ctx):
+    occ = np.ones((2, 2, 2), np.uint16)
+    seeds = np.array([[0, 0, 0, 0x7FFF >> 8 << 8 | 0xFF], [1, 1, 1, 2]], np.uint32)  # labels 0x7FFF, 2
+    g = vf.RegularGrid(occ.shape, None, None, ctx)
+    g.upload(occ)
+    fr = vf.FloodFracturer()
+    fr.setDistanceFunction(vf.MANHATTAN)
+    fr.build(g, seeds)
+    exp, _ = O.flood(occ, seeds, vf.MANHATTAN)
+    assert np.array_equal(g.data(), exp)
+    with pytest.raises(vf.VFError):
+        vf.RegularGrid((1, 8, 8), None, None, ctx)  # dims below 2

@@ -231,3 +231,19 @@ def test_config1_vessel_128(vf, ctx):
     (r,) = vf.batch_run([spec], ctx)
     lab, cnt, _ = _oracle_job(spec)
     assert r.status == 0 and np.array_equal(spec.labels, lab) and np.array_equal(spec.counts, cnt)
+
+
+def test_batch_with_empty_mesh_job(vf, ctx):
+    # a job without triangles (grid and AABB given) stays empty and fails its
+    # seed search alone; its neighbours in the batch are unaffected
+    ok1, ok2 = _job(vf, 7), _job(vf, 8)
+    ref = [_job(vf, 7), _job(vf, 8)]
+    vf.batch_run(ref, ctx)
+    p = vf.Params.default(num_seeds=4, seed_location=vf.BOTH)
+    empty = vf.JobSpec(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32), p,
+                       dims=(20, 24, 28), aabb=((0, 0, 0), (1, 1, 1)), ncounts=256, tag=99)
+    res = vf.batch_run([ok1, empty, ok2], ctx)
+    assert res[0].status == 0 and res[2].status == 0
+    assert res[1].status == vf.ERR_SEED_SEARCH
+    assert not empty.labels.any()
+    assert np.array_equal(ok1.labels, ref[0].labels) and np.array_equal(ok2.labels, ref[1].labels)
