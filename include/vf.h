@@ -158,7 +158,10 @@ vf_status vf_fracture_seeds(vf_grid* g, const vf_params* p, uint32_t* out_xyzw,
  * (FloodFracturer.cpp:98-191: homogenize, seed, BFS waves, disjoint
  * cleanup, undoMask); VF_NAIVE = NaiveFracturer::build (CPU path
  * NaiveFracturer.cpp:26-68).  seeds_xyzw: 4*nseeds uint32, host.
- * Same-wave flood ties go to the lowest seed index. */
+ * Same-wave flood ties go to the lowest seed index.  Flood labels are
+ * frag | prefix << 8 as Seeder::mergeSeeds makes them (Seeder.cpp:150): at
+ * most 0x7FFF with a fragment id (low byte) of at least 2; others are
+ * VF_ERR_INVALID. */
 vf_status vf_fracture(vf_grid* g, int algorithm, int distance,
                       const uint32_t* seeds_xyzw, uint32_t nseeds);
 /* reference-shaped flood: one kernel launch and one host read of the

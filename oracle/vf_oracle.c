@@ -584,7 +584,9 @@ int vfo_flood(uint16_t* grid, uint32_t X, uint32_t Y, uint32_t Z,
   for (uint32_t i = 0; i < nseeds; ++i) {
     if (seeds[4 * i] >= X || seeds[4 * i + 1] >= Y || seeds[4 * i + 2] >= Z)
       return VFO_ERR_INVALID;
-    if (seeds[4 * i + 3] <= VOXEL_FREE || seeds[4 * i + 3] > 0x7FFF) return VFO_ERR_INVALID;
+    /* a label is frag | prefix << 8 (Seeder.cpp:150): its fragment id (low
+     * byte) is a label itself, >= 2; the reference never makes others */
+    if (seeds[4 * i + 3] > 0x7FFF || (seeds[4 * i + 3] & 0xFFu) <= VOXEL_FREE) return VFO_ERR_INVALID;
   }
   /* homogenize (RegularGrid.cpp:533-541) */
   for (size_t i = 0; i < N; ++i)

@@ -435,8 +435,11 @@ def test_flood_max_seed_count_and_limit(vf, ctx):
     rng = np.random.default_rng(11)
     shape = (40, 36, 44)
     occ = (rng.random(shape) < 0.9).astype(np.uint16)
-    seeds = O.seeder_uniform(occ, 4095, 3, 2)  # the most a flood takes (12-bit slots)
+    seeds = O.seeder_uniform(occ, 4095, 3, 2).copy()  # the most a flood takes (12-bit slots)
     assert seeds.shape[0] == 4095
+    # fragment labels 2..255 with sub-seed prefixes, as mergeSeeds makes them
+    i = np.arange(4095)
+    seeds[:, 3] = (i % 254 + 2) | ((i // 254) << 8)
     g = vf.RegularGrid(shape, None, None, ctx)
     g.upload(occ)
     fr = vf.FloodFracturer()
@@ -464,6 +467,21 @@ def test_flood_long_thin_grid(vf, ctx, dfunc):
     fr.build(g, seeds)
     exp, _ = O.flood(occ, seeds, dfunc)
     assert np.array_equal(g.data(), exp)
+
+
+def test_flood_rejects_labels_without_fragment_id(vf, ctx, occ64):
+    occ, mn, mx = occ64
+    seeds = O.seeder_uniform(occ, 4, 9, 2).copy()
+    g = vf.RegularGrid(occ.shape, mn, mx, ctx)
+    g.upload(occ)
+    fr = vf.FloodFracturer()
+    for bad in (0x100, 0x201, 0x8002):
+        seeds[1, 3] = bad
+        with pytest.raises(vf.VFError) as e:
+            fr.build(g, seeds)
+        assert e.value.status == vf.ERR_INVALID
+        with pytest.raises(O.OracleError):
+            O.flood(occ, seeds, vf.MANHATTAN)
 
 
 def test_smallest_grid_and_extreme_labels(vf, ctx):

@@ -168,7 +168,7 @@ extern "C" vf_status vf_flood_noalloc(const uint16_t* d_grid, uint16_t* d_labels
   NA_CK(cudaMemcpyAsync(&ferr, fs.err, 4, cudaMemcpyDeviceToHost, st));
   NA_CK(cudaStreamSynchronize(st));
 #undef NA_CK
-  if (err & VF_JERR_INVALID) return fail(VF_ERR_INVALID, "vf_flood_noalloc: seed outside the grid or label not in 2..0x7FFF");
+  if (err & VF_JERR_INVALID) return fail(VF_ERR_INVALID, "vf_flood_noalloc: seed outside the grid or label not a valid fragment label (<= 0x7FFF, low byte >= 2)");
   if (has_prefix)
     return fail(VF_ERR_INVALID, "vf_flood_noalloc: seed labels with sub-seed prefixes (> 255) need vf_fracture");
   if (ferr) return fail(VF_ERR_TIMEOUT, "vf_flood_noalloc: flood did not converge (bounded wait expired)");

@@ -47,7 +47,8 @@ __global__ void kp_seed(const JobDesc* jobs, JobState* st, uint32_t* frontier, u
   for (uint32_t i = 0; i < s.nseeds; ++i) {
     const uint32_t x = J.seeds[4 * i], y = J.seeds[4 * i + 1], z = J.seeds[4 * i + 2],
                    w = J.seeds[4 * i + 3];
-    if (x >= J.X || y >= J.Y || z >= J.Z || w <= VOXEL_FREE || w > 0x7FFFu) {
+    // label = frag | prefix << 8 (Seeder.cpp:150), fragment id >= 2
+    if (x >= J.X || y >= J.Y || z >= J.Z || w > 0x7FFFu || (w & 0xFFu) <= VOXEL_FREE) {
       s.err |= VF_JERR_INVALID;
       continue;
     }
