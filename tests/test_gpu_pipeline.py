@@ -247,3 +247,19 @@ def test_batch_with_empty_mesh_job(vf, ctx):
     assert res[1].status == vf.ERR_SEED_SEARCH
     assert not empty.labels.any()
     assert np.array_equal(ok1.labels, ref[0].labels) and np.array_equal(ok2.labels, ref[1].labels)
+
+
+def test_large_batch_matches_small_batches(vf, ctx):
+    # 40 jobs in one batch (pinned and pageable outputs mixed) and the same
+    # jobs in batches of 8 give the same bits
+    n = 40
+    big = [_job(vf, 100 + i, pinned=(i % 2 == 0)) for i in range(n)]
+    small = [_job(vf, 100 + i) for i in range(n)]
+    res = vf.batch_run(big, ctx)
+    for k in range(0, n, 8):
+        for r in vf.batch_run(small[k:k + 8], ctx):
+            assert r.status == 0
+    for a, b, r in zip(big, small, res):
+        assert r.status == 0 and r.user_tag == a.tag
+        assert np.array_equal(a.labels, b.labels), f"job {a.tag}"
+        assert np.array_equal(a.counts, b.counts)
