@@ -457,7 +457,23 @@ __device__ __forceinline__ void mm3(float a, float b, float c, float& mn, float&
   if (c < mn) mn = c;
   if (c > mx) mx = c;
 }
-__device__ bool tri_box(const tv& p0, const tv& p1, const tv& p2, const tv& c, const tv& r) {
+// The SAT as a conjunction of tests, each evaluated exactly as
+// Intersections3D.h:204-258 does; MASK selects which run (a separating axis
+// makes the result false whatever the order).  Bits 0-8: the edge-cross-axis
+// tests (edge e0: x01 y02 z12; e1: x01 y02 z0; e2: x2 y1 z12), bits 9-11: the
+// box axes x, y, z, bit 12: the plane-box test.
+constexpr uint32_t SAT_ALL = 0x1FFFu;
+// tests that use only the two axes other than C: the same for every cell of
+// a column along C (the x-axis family uses y, z; the box axes other than C)
+__host__ __device__ constexpr uint32_t sat_column_mask(int C) {
+  return C == 0 ? ((1u << 0) | (1u << 3) | (1u << 6) | (1u << 10) | (1u << 11))
+       : C == 1 ? ((1u << 1) | (1u << 4) | (1u << 7) | (1u << 9) | (1u << 11))
+                : ((1u << 2) | (1u << 5) | (1u << 8) | (1u << 9) | (1u << 10));
+}
+
+template <uint32_t MASK>
+__device__ __forceinline__ bool tri_box_sel(const tv& p0, const tv& p1, const tv& p2, const tv& c,
+                                            const tv& r) {
   satd d;
   d.r = r;
   d.v0 = {SUB(p0.x, c.x), SUB(p0.y, c.y), SUB(p0.z, c.z)};
@@ -467,24 +483,31 @@ __device__ bool tri_box(const tv& p0, const tv& p1, const tv& p2, const tv& c, c
   tv e1 = {SUB(d.v2.x, d.v1.x), SUB(d.v2.y, d.v1.y), SUB(d.v2.z, d.v1.z)};
   tv e2 = {SUB(d.v0.x, d.v2.x), SUB(d.v0.y, d.v2.y), SUB(d.v0.z, d.v2.z)};
   float fx = fabsf(e0.x), fy = fabsf(e0.y), fz = fabsf(e0.z);
-  if (!x01(d, e0.z, e0.y, fz, fy)) return false;
-  if (!y02(d, e0.z, e0.x, fz, fx)) return false;
-  if (!z12(d, e0.y, e0.x, fy, fx)) return false;
+  if ((MASK & (1u << 0)) && !x01(d, e0.z, e0.y, fz, fy)) return false;
+  if ((MASK & (1u << 1)) && !y02(d, e0.z, e0.x, fz, fx)) return false;
+  if ((MASK & (1u << 2)) && !z12(d, e0.y, e0.x, fy, fx)) return false;
   fx = fabsf(e1.x); fy = fabsf(e1.y); fz = fabsf(e1.z);
-  if (!x01(d, e1.z, e1.y, fz, fy)) return false;
-  if (!y02(d, e1.z, e1.x, fz, fx)) return false;
-  if (!z0(d, e1.y, e1.x, fy, fx)) return false;
+  if ((MASK & (1u << 3)) && !x01(d, e1.z, e1.y, fz, fy)) return false;
+  if ((MASK & (1u << 4)) && !y02(d, e1.z, e1.x, fz, fx)) return false;
+  if ((MASK & (1u << 5)) && !z0(d, e1.y, e1.x, fy, fx)) return false;
   fx = fabsf(e2.x); fy = fabsf(e2.y); fz = fabsf(e2.z);
-  if (!x2(d, e2.z, e2.y, fz, fy)) return false;
-  if (!y1(d, e2.z, e2.x, fz, fx)) return false;
-  if (!z12(d, e2.y, e2.x, fy, fx)) return false;
+  if ((MASK & (1u << 6)) && !x2(d, e2.z, e2.y, fz, fy)) return false;
+  if ((MASK & (1u << 7)) && !y1(d, e2.z, e2.x, fz, fx)) return false;
+  if ((MASK & (1u << 8)) && !z12(d, e2.y, e2.x, fy, fx)) return false;
   float mn, mx;
-  mm3(d.v0.x, d.v1.x, d.v2.x, mn, mx);
-  if (mn > d.r.x || mx < -d.r.x) return false;
-  mm3(d.v0.y, d.v1.y, d.v2.y, mn, mx);
-  if (mn > d.r.y || mx < -d.r.y) return false;
-  mm3(d.v0.z, d.v1.z, d.v2.z, mn, mx);
-  if (mn > d.r.z || mx < -d.r.z) return false;
+  if (MASK & (1u << 9)) {
+    mm3(d.v0.x, d.v1.x, d.v2.x, mn, mx);
+    if (mn > d.r.x || mx < -d.r.x) return false;
+  }
+  if (MASK & (1u << 10)) {
+    mm3(d.v0.y, d.v1.y, d.v2.y, mn, mx);
+    if (mn > d.r.y || mx < -d.r.y) return false;
+  }
+  if (MASK & (1u << 11)) {
+    mm3(d.v0.z, d.v1.z, d.v2.z, mn, mx);
+    if (mn > d.r.z || mx < -d.r.z) return false;
+  }
+  if (!(MASK & (1u << 12))) return true;
   tv n = {SUB(MUL(e0.y, e1.z), MUL(e1.y, e0.z)), SUB(MUL(e0.z, e1.x), MUL(e1.z, e0.x)),
           SUB(MUL(e0.x, e1.y), MUL(e1.x, e0.y))};
   // planeBoxOverlap
@@ -499,36 +522,49 @@ __device__ bool tri_box(const tv& p0, const tv& p1, const tv& p2, const tv& c, c
   return false;
 }
 
+// the voxel box of cell (i, j, k) as RegularGrid::getAABBs builds it
+__device__ __forceinline__ void cell_box(const JobDesc& J, const float* cs, int i, int jj, int k,
+                                         tv& ce, tv& r) {
+  tv bmin = {ADD(J.amin[0], MUL(cs[0], (float)i)), ADD(J.amin[1], MUL(cs[1], (float)jj)),
+             ADD(J.amin[2], MUL(cs[2], (float)k))};
+  tv bmax = {ADD(bmin.x, cs[0]), ADD(bmin.y, cs[1]), ADD(bmin.z, cs[2])};
+  // (max + min) / 2: x * 0.5 and x / 2 are the same correctly rounded value
+  ce = {MUL(ADD(bmax.x, bmin.x), 0.5f), MUL(ADD(bmax.y, bmin.y), 0.5f),
+        MUL(ADD(bmax.z, bmin.z), 0.5f)};
+  r = {SUB(bmax.x, ce.x), SUB(bmax.y, ce.y), SUB(bmax.z, ce.z)};
+}
+
 __device__ __forceinline__ int float_cell(float f, int n) {
   if (!(f > -1.0e9f)) f = -1.0e9f;
   if (f > 1.0e9f) f = 1.0e9f;
   return vf_clampi((int)floorf(f), -2, n + 1);
 }
 
-// the exact test of one voxel (reference operation order) and the mark
+// the exact test of one voxel (reference operation order) and the mark.
+// column_done: the column tests of axis c already passed for this cell's
+// column, so only the rest of the SAT runs; c < 0: the whole SAT
 __device__ __forceinline__ void test_cell(const JobDesc& J, const float* cs, const tv& p0,
-                                          const tv& p1, const tv& p2, int i, int jj, int k) {
-  tv bmin = {ADD(J.amin[0], MUL(cs[0], (float)i)), ADD(J.amin[1], MUL(cs[1], (float)jj)),
-             ADD(J.amin[2], MUL(cs[2], (float)k))};
-  tv bmax = {ADD(bmin.x, cs[0]), ADD(bmin.y, cs[1]), ADD(bmin.z, cs[2])};
-  // (max + min) / 2: x * 0.5 and x / 2 are the same correctly rounded value
-  tv ce = {MUL(ADD(bmax.x, bmin.x), 0.5f), MUL(ADD(bmax.y, bmin.y), 0.5f),
-           MUL(ADD(bmax.z, bmin.z), 0.5f)};
-  tv r = {SUB(bmax.x, ce.x), SUB(bmax.y, ce.y), SUB(bmax.z, ce.z)};
-  if (tri_box(p0, p1, p2, ce, r))
-    atomicOr(J.shell + ((size_t)i * J.Y + jj) * J.Zw + (k >> 5), 1u << (k & 31));
+                                          const tv& p1, const tv& p2, int i, int jj, int k, int c) {
+  tv ce, r;
+  cell_box(J, cs, i, jj, k, ce, r);
+  bool hit;
+  if (c == 0) hit = tri_box_sel<SAT_ALL ^ sat_column_mask(0)>(p0, p1, p2, ce, r);
+  else if (c == 1) hit = tri_box_sel<SAT_ALL ^ sat_column_mask(1)>(p0, p1, p2, ce, r);
+  else if (c == 2) hit = tri_box_sel<SAT_ALL ^ sat_column_mask(2)>(p0, p1, p2, ce, r);
+  else hit = tri_box_sel<SAT_ALL>(p0, p1, p2, ce, r);
+  if (hit) atomicOr(J.shell + ((size_t)i * J.Y + jj) * J.Zw + (k >> 5), 1u << (k & 31));
 }
 
 // Per-face setup of the shell test.  Candidates: the triangle's cell bbox
-// grown by one cell.  Pruning: two of the SAT's own separating axes are
-// evaluated early with a margin -- (1) the triangle's projection on the
-// plane orthogonal to its dominant normal axis c against each column's
-// square (the edge x c axes), (2) the plane slab along c (the plane-box
-// test).  A dropped box is separated along a SAT axis by more than the
-// margin (2% of a cell + 64 ulp of the largest coordinate), far beyond the
-// rounding of the float SAT, so the exact test would reject it too: the
-// marked set equals testing the full bbox.
-// Work items: columns (a, b) when pruning, else every bbox cell.
+// grown by one cell, as columns along the dominant normal axis c.  Per
+// column, (1) the SAT tests that do not involve axis c (the c-family edge
+// axes and the two other box axes) run exactly, once: they are the same for
+// every cell of the column, and a column they reject holds no hit; (2) the
+// plane slab along c bounds the cells, with a margin (2% of a cell + 64 ulp
+// of the largest coordinate) far beyond the rounding of the float SAT, so no
+// cell the exact test accepts is dropped.  Each remaining cell then runs the
+// rest of the SAT.  The marked set equals testing the full bbox.
+// Work items: columns (a, b) when pruning, else every bbox cell (whole SAT).
 struct ShellSetup {
   float cs[3];                 // cell size (x, y, z)
   tv p0, p1, p2;               // the triangle
@@ -620,13 +656,6 @@ __device__ bool shell_setup(const JobDesc& J, uint32_t f, ShellSetup& S) {
   return true;
 }
 
-__device__ __forceinline__ bool edge_keeps(float x0, float y0, float x1, float y1, float ca,
-                                           float cb, float ha, float hb) {
-  const float dx = x1 - x0, dy = y1 - y0;
-  const float E = dx * (cb - y0) - dy * (ca - x0);
-  return E + fabsf(dx) * hb + fabsf(dy) * ha >= 0.0f;
-}
-
 // the candidate cells of work item q: column (ia, ib) along c, cells
 // klo .. klo + n - 1 (n = 0: the column is pruned).  Items of a face without
 // pruning are single cells (ia, ib, klo) = (i, j, k) with c = z.
@@ -642,11 +671,21 @@ __device__ __forceinline__ void shell_column(const ShellSetup& S, uint32_t q, in
   }
   ia = S.lo_a + (int)(q / S.n_b);
   ib = S.lo_b + (int)(q % S.n_b);
+  // the SAT tests that do not involve axis c, exactly, once per column: the
+  // box of every cell of the column has the same extent along a and b
+  {
+    const float bmin_a = ADD(S.amin_a, MUL(S.cs_a, (float)ia)), bmax_a = ADD(bmin_a, S.cs_a);
+    const float bmin_b = ADD(S.amin_b, MUL(S.cs_b, (float)ib)), bmax_b = ADD(bmin_b, S.cs_b);
+    const float ce_a = MUL(ADD(bmax_a, bmin_a), 0.5f), ce_b = MUL(ADD(bmax_b, bmin_b), 0.5f);
+    const float r_a = SUB(bmax_a, ce_a), r_b = SUB(bmax_b, ce_b);
+    bool keep;
+    if (S.c == 0) keep = tri_box_sel<sat_column_mask(0)>(S.p0, S.p1, S.p2, tv{0.0f, ce_a, ce_b}, tv{0.0f, r_a, r_b});
+    else if (S.c == 1) keep = tri_box_sel<sat_column_mask(1)>(S.p0, S.p1, S.p2, tv{ce_b, 0.0f, ce_a}, tv{r_b, 0.0f, r_a});
+    else keep = tri_box_sel<sat_column_mask(2)>(S.p0, S.p1, S.p2, tv{ce_a, ce_b, 0.0f}, tv{r_a, r_b, 0.0f});
+    if (!keep) return;
+  }
   const float ca = (S.amin_a + S.cs_a * ((float)ia + 0.5f)) - S.q0_a;
   const float cb = (S.amin_b + S.cs_b * ((float)ib + 0.5f)) - S.q0_b;
-  if (!edge_keeps(0.0f, 0.0f, S.Pa1, S.Pb1, ca, cb, S.ha, S.hb)) return;
-  if (!edge_keeps(S.Pa1, S.Pb1, S.Pa2, S.Pb2, ca, cb, S.ha, S.hb)) return;
-  if (!edge_keeps(S.Pa2, S.Pb2, 0.0f, 0.0f, ca, cb, S.ha, S.hb)) return;
   // slab bounds (conservative: the margin is far above these roundings)
   const float tc = S.q0_c - (S.nr_a * ca + S.nr_b * cb) * S.inr;
   // cells whose centre is within w of the plane along c
@@ -776,7 +815,10 @@ __global__ void __launch_bounds__(256, 3) k_shell_flat(const JobDesc* jobs, cons
                              __shfl_sync(0xFFFFFFFFu, S.cs[1], src),
                              __shfl_sync(0xFFFFFFFFu, S.cs[2], src)};
         const int sj = __shfl_sync(0xFFFFFFFFu, jidx, src);
-        const int sc = __shfl_sync(0xFFFFFFFFu, S.c, src);
+        // test mode: the face's axis c (column tests already passed) or -1
+        // (faces without pruning: every item is one cell, whole SAT)
+        const int mode = __shfl_sync(0xFFFFFFFFu, S.prune ? S.c : -1, src);
+        const int sc = mode < 0 ? 2 : mode;
         const int sa = __shfl_sync(0xFFFFFFFFu, ia, src);
         const int sb = __shfl_sync(0xFFFFFFFFu, ib, src);
         const int sk = __shfl_sync(0xFFFFFFFFu, klo, src) + t - __shfl_sync(0xFFFFFFFFu, excl, src);
@@ -785,7 +827,7 @@ __global__ void __launch_bounds__(256, 3) k_shell_flat(const JobDesc* jobs, cons
           const int x = sc == 0 ? sk : (sc == 1 ? sb : sa);
           const int y = sc == 0 ? sa : (sc == 1 ? sk : sb);
           const int z = sc == 0 ? sb : (sc == 1 ? sa : sk);
-          test_cell(jobs[sj], cs, q0, q1, q2, x, y, z);
+          test_cell(jobs[sj], cs, q0, q1, q2, x, y, z, mode);
         }
       }
     }
