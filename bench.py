@@ -340,6 +340,7 @@ def main():
             "active_rows_per_sweep": act_rows / max(sweeps, 1),
             "busy_warps_per_sweep": busy_warps / max(sweeps, 1),
             "key_changes_per_visit": key_changes / max(visits, 1),
+            "bricks_per_pass_last_step": ctx.flood_pass_sizes(),
             "launch_ms": flood_launch_ms,
             "traffic": K_RELAX_DRAM_BYTES_PER_VISIT * visits / args.steps,
             "traffic_source": "ncu DRAM bytes per brick visit (48-job capture) x visits of this launch"}

@@ -295,6 +295,9 @@ vf_status vf_ctx_flood_stats(vf_ctx* ctx, uint64_t* passes, uint64_t* sweeps,
  * timeouts, [4] sweeps, [5] visits at the sweep cap, [6] active rows summed
  * over sweeps, [7] voxel key changes.  n <= 8 are filled, the rest zeroed. */
 vf_status vf_ctx_flood_counters(vf_ctx* ctx, uint64_t* out, uint32_t n);
+/* bricks queued for each pass of the last batched flood (first 256 passes;
+ * zero beyond the pass count). */
+vf_status vf_ctx_flood_pass_sizes(vf_ctx* ctx, uint32_t* out, uint32_t n);
 /* *replayed = 1 when the last vf_batch_execute ran its stage chain as a
  * CUDA graph (captured on the first execute after vf_batch_prepare, replayed
  * afterwards), 0 when it launched the stages directly. */

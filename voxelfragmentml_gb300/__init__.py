@@ -126,6 +126,7 @@ EXPORTS = {
     "vf_ctx_flood_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "vf_ctx_flood_counters": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_ctx_last_graph": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "vf_ctx_flood_pass_sizes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_grid_export_rle": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "vf_ctx_set_tuning": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_ctx_get_tuning": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
@@ -226,6 +227,12 @@ class Context:
         v = (C.c_int32 * 4)()
         _check(lib().vf_autotune(self.h, jobs, len(specs), v, 4))
         return dict(zip(self.TUNING, list(v)))
+
+    def flood_pass_sizes(self):
+        """Bricks queued per pass of the last batched flood."""
+        a = (C.c_uint32 * 256)()
+        _check(lib().vf_ctx_flood_pass_sizes(self.h, a, 256))
+        return [v for v in a if v]
 
     def last_stats(self):
         la, vis, by = C.c_uint64(), C.c_uint64(), C.c_uint64()

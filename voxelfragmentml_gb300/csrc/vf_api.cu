@@ -657,6 +657,13 @@ vf_status vf_ctx_flood_stats(vf_ctx* ctx, uint64_t* passes, uint64_t* sweeps, ui
   return VF_OK;
 }
 
+vf_status vf_ctx_flood_pass_sizes(vf_ctx* ctx, uint32_t* out, uint32_t n) {
+  if (!ctx || (n && !out)) return fail(VF_ERR_INVALID, "NULL argument");
+  const uint64_t passes = ctx->c.last_flood_passes;
+  for (uint32_t i = 0; i < n; ++i) out[i] = (i < 256 && i < passes) ? ctx->c.last_pass_sizes[i] : 0u;
+  return VF_OK;
+}
+
 vf_status vf_ctx_last_graph(vf_ctx* ctx, int* replayed) {
   if (!ctx || !replayed) return fail(VF_ERR_INVALID, "NULL argument");
   *replayed = ctx->c.batch.last_run_graph ? 1 : 0;

@@ -54,6 +54,7 @@ struct FloodArgs {
                      // [5] visits at the sweep cap, [6] active row-sweeps, [7] key changes
   uint32_t max_passes;
   int max_sweeps;    // sweeps per brick visit before the brick re-queues itself
+  uint32_t* pass_sizes;  // bricks queued for each of the first 256 passes (or null)
 };
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
@@ -337,6 +338,7 @@ __global__ void __launch_bounds__(256, 2) k_relax(FloodArgs a) {
       a.qhead[(p + 2) % 3] = 0;
     }
     const uint32_t qn = ld_acquire(&a.qcount[cur]);
+    if (a.pass_sizes && blockIdx.x == 0 && threadIdx.x == 0 && p < 256) a.pass_sizes[p] = qn;
     uint32_t visits = 0;
     for (;;) {
       __syncthreads();
@@ -685,6 +687,7 @@ cudaError_t flood_relax(cudaStream_t st, const JobDesc* dj, JobState* ds,
   a.stats = fs.stats;
   a.max_passes = fs.max_passes;
   a.max_sweeps = (fs.max_sweeps > 0 && fs.max_sweeps <= MAXIT) ? fs.max_sweeps : MAXIT;
+  a.pass_sizes = fs.pass_sizes;
   int blocks = relax_blocks(num_sms);
   if (fs.ctas_per_sm > 0 && fs.ctas_per_sm * num_sms < blocks) blocks = fs.ctas_per_sm * num_sms;
   if (blocks_used) *blocks_used = blocks;

@@ -91,6 +91,7 @@ struct FloodScratch {
   uint32_t total_bricks;
   int max_sweeps = 0;    // tuning: sweeps per brick visit (0: default cap)
   int ctas_per_sm = 0;   // tuning: resident CTAs per SM (0: as many as fit)
+  uint32_t* pass_sizes = nullptr;  // statistics: bricks queued per pass (256)
 };
 void flood_init_keys(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
                      const uint32_t* count, uint32_t max_count, const uint32_t* brick_job,

@@ -75,7 +75,7 @@ vf_status Batch::init(Ctx* c, bool own) {
   VF_CK(cudaEventCreate(&ev_flood1));
   VF_CK(cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming));
   for (int i = 0; i < NSTAGE_EV; ++i) VF_CK(cudaEventCreate(&ev_stage[i]));
-  VF_CK(cudaMallocHost(&h_scal, 64 * sizeof(uint32_t)));
+  VF_CK(cudaMallocHost(&h_scal, 512 * sizeof(uint32_t)));
   return VF_OK;
 }
 
@@ -599,6 +599,7 @@ static vfk::FloodScratch flood_scratch(Batch& B) {
   fs.total_bricks = B.sz.bricks;
   fs.max_sweeps = B.ctx->tune.flood_sweeps;
   fs.ctas_per_sm = B.ctx->tune.flood_ctas;
+  fs.pass_sizes = sc + 128;  // [256]
   return fs;
 }
 
@@ -735,7 +736,7 @@ vf_status Batch::enqueue_batched(bool do_upload, bool do_download) {
                             sizeof(uint32_t) * j.ncounts, cudaMemcpyDeviceToHost, st));
   }
   VF_CK(cudaMemcpyAsync(h_state, ds, sizeof(JobState) * n, cudaMemcpyDeviceToHost, st));
-  VF_CK(cudaMemcpyAsync(h_scal, scal.p, 64 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  VF_CK(cudaMemcpyAsync(h_scal, scal.p, 384 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   mark(11);
   VF_CK(record_event(ev_done, st));
   return VF_OK;
@@ -784,6 +785,7 @@ vf_status Batch::finish(vf_job_result* res) {
     ctx->last_flood_sweeps = h_scal[20];
     ctx->last_flood_maxit = h_scal[21];
     for (int i = 0; i < 8; ++i) ctx->last_flood_counters[i] = h_scal[16 + i];
+    for (int i = 0; i < 256; ++i) ctx->last_pass_sizes[i] = h_scal[128 + i];
   } else {
     for (int i = 0; i < 8; ++i) ctx->last_flood_counters[i] = 0;
     ctx->last_flood_ms = 0.f;
