@@ -258,6 +258,7 @@ def main():
         act_rows += st["flood_active_row_sweeps"]
         key_changes += st["flood_key_changes"]
         busy_warps += st["flood_busy_warp_sweeps"]
+        pass_sizes = ctx.flood_pass_sizes()
         for k, v in ctx.stage_ms().items():
             stage_tot[k] = stage_tot.get(k, 0.0) + v
     L.vf_ctx_event_record(ctx.h, 1)
@@ -340,7 +341,7 @@ def main():
             "active_rows_per_sweep": act_rows / max(sweeps, 1),
             "busy_warps_per_sweep": busy_warps / max(sweeps, 1),
             "key_changes_per_visit": key_changes / max(visits, 1),
-            "bricks_per_pass_last_step": ctx.flood_pass_sizes(),
+            "bricks_per_pass_last_step": pass_sizes,
             "launch_ms": flood_launch_ms,
             "traffic": K_RELAX_DRAM_BYTES_PER_VISIT * visits / args.steps,
             "traffic_source": "ncu DRAM bytes per brick visit (48-job capture) x visits of this launch"}

@@ -293,7 +293,11 @@ vf_status vf_ctx_flood_stats(vf_ctx* ctx, uint64_t* passes, uint64_t* sweeps,
 /* raw flood counters of the last batched run: [0] brick visits, [1] passes,
  * [2] warps with work summed over sweeps (8 warps per brick), [3] barrier
  * timeouts, [4] sweeps, [5] visits at the sweep cap, [6] active rows summed
- * over sweeps, [7] voxel key changes.  n <= 8 are filled, the rest zeroed. */
+ * over sweeps, [7] voxel key changes, [8] 0, or the kind of the first
+ * out-of-range access the relaxation skipped (1 brick id, 2 job id, 3 key
+ * read, 4 queued brick id, 5 key write; the batch then fails with
+ * VF_ERR_TIMEOUT) with [9], [10] its brick and index.  n <= 11 are filled,
+ * the rest zeroed. */
 vf_status vf_ctx_flood_counters(vf_ctx* ctx, uint64_t* out, uint32_t n);
 /* bricks queued for each pass of the last batched flood (first 256 passes;
  * zero beyond the pass count). */

@@ -106,7 +106,7 @@ def test_autotune_and_settings_do_not_change_results(vf, ctx):
     try:
         chosen = ctx.autotune([_job(vf, i) for i in range(8)])
         assert chosen["parity_grid"] in (4, 8, 16, 32) and chosen["shell_grid"] in (6, 12, 24)
-        assert chosen["flood_sweeps"] in (8, 16, 32, 96) and chosen["flood_ctas"] in (0, 1)
+        assert chosen["flood_sweeps"] in (8, 16, 32, 96) and chosen["flood_ctas"] in (0, 2, 3)
         assert ctx.tuning() == chosen
         # extreme settings: one sweep per brick visit (every brick re-queues
         # itself until its keys settle), one CTA per SM, minimal grids

@@ -624,7 +624,7 @@ vf_status vf_autotune(vf_ctx* ctx, const vf_job* jobs, uint32_t njobs, int32_t* 
   const Knob knobs[] = {{0, 2, {4, 8, 16, 32}},      // parity grid   (stage: parity)
                         {1, 3, {6, 12, 24}},         // shell grid    (stage: shell)
                         {2, 6, {8, 16, 32, 96}},     // sweeps/visit  (stage: fracture)
-                        {3, 6, {1, 0}}};             // flood CTAs/SM (stage: fracture)
+                        {3, 6, {2, 3, 0}}};          // flood CTAs/SM (stage: fracture)
   for (const Knob& k : knobs) {
     int32_t best_v = 0;
     float best = 3.0e38f;
@@ -672,8 +672,8 @@ vf_status vf_ctx_last_graph(vf_ctx* ctx, int* replayed) {
 
 vf_status vf_ctx_flood_counters(vf_ctx* ctx, uint64_t* out, uint32_t n) {
   if (!ctx || (n && !out)) return fail(VF_ERR_INVALID, "NULL argument");
-  for (uint32_t i = 0; i < n && i < 8; ++i) out[i] = ctx->c.last_flood_counters[i];
-  for (uint32_t i = 8; i < n; ++i) out[i] = 0;
+  for (uint32_t i = 0; i < n && i < 11; ++i) out[i] = ctx->c.last_flood_counters[i];
+  for (uint32_t i = 11; i < n; ++i) out[i] = 0;
   return VF_OK;
 }
 

@@ -51,16 +51,31 @@ struct FloodArgs {
   uint32_t* bar;     // [2]
   uint32_t* err;
   uint32_t* stats;   // [0] visits, [1] passes, [2] busy warp-sweeps, [3] timeout, [4] sweeps,
-                     // [5] visits at the sweep cap, [6] active row-sweeps, [7] key changes
+                     // [5] visits at the sweep cap, [6] active row-sweeps, [7] key changes,
+                     // [8..10] first out-of-range access (code, two values)
   uint32_t max_passes;
   int max_sweeps;    // sweeps per brick visit before the brick re-queues itself
   uint32_t* pass_sizes;  // bricks queued for each of the first 256 passes (or null)
+  uint32_t nbricks;      // bricks of the batch (queue entries and brick ids are below)
+  uint32_t njobs;        // jobs of the batch
 };
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
   uint32_t v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
+}
+
+// A brick id, job id or key address outside its buffer: the access is
+// skipped, the flood's error word gets bit 3 (the batch reports the job as
+// failed) and the first case is kept in stats[8..10] (code, two values).
+__device__ __noinline__ void flood_anomaly(const FloodArgs& a, uint32_t code, uint32_t v0,
+                                           uint32_t v1) {
+  atomicOr(a.err, 8u);
+  if (atomicCAS(a.stats + 8, 0u, code) == 0u) {
+    a.stats[9] = v0;
+    a.stats[10] = v1;
+  }
 }
 
 // software grid barrier with a bounded spin (~4 s); false on timeout
@@ -103,6 +118,10 @@ __device__ __forceinline__ void enqueue(const FloodArgs& a, uint32_t b, uint32_t
   // warp-aggregated append of the bricks this warp wants on the next queue
   const int lane = threadIdx.x & 31;
   bool push = false;
+  if (want && b >= a.nbricks) {
+    flood_anomaly(a, 4u, b, next_pass);
+    want = false;
+  }
   if (want) push = atomicMax(&a.epoch[b], next_pass + 1u) < next_pass + 1u;
   const unsigned m = __ballot_sync(0xFFFFFFFFu, push);
   if (!m) return;
@@ -114,10 +133,30 @@ __device__ __forceinline__ void enqueue(const FloodArgs& a, uint32_t b, uint32_t
   if (push) a.queue[q][base + __popc(m & ((1u << lane) - 1u))] = b;
 }
 
+// relaxation candidate from a neighbour key: one step further (0 when the
+// neighbour is EMPTY or unreached)
+__device__ __forceinline__ uint32_t step_from(uint32_t m) {
+  return m >= 2u * VF_KEY_STEP ? m - VF_KEY_STEP : 0u;
+}
+// an unreached voxel next to a key one step from the distance limit
+__device__ __forceinline__ bool at_limit(uint32_t kk, uint32_t m) {
+  return kk == VF_KEY_UNREACHED && m >= VF_KEY_MIN_REACHED && m < 2u * VF_KEY_STEP;
+}
+__device__ __forceinline__ uint32_t relax1(uint32_t kk, uint32_t m, uint32_t& overflow) {
+  if (at_limit(kk, m)) overflow = 1;
+  return kk ? max(kk, step_from(m)) : 0u;
+}
+__device__ __forceinline__ uint4 max4(uint4 a, uint4 b) {
+  return make_uint4(max(a.x, b.x), max(a.y, b.y), max(a.z, b.z), max(a.w, b.w));
+}
+__device__ __forceinline__ uint4 lds4(const uint32_t* p) {
+  return *reinterpret_cast<const uint4*>(p);
+}
+
 template <int CONN>
 __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, uint32_t b,
                             uint32_t pass, uint32_t* tile, uint32_t* live27, uint32_t* dirs,
-                            int* reenq, uint8_t* rflag) {
+                            int* reenq, uint32_t* rfw) {
   const uint32_t lb = b - J.brick_base;
   const int bz = lb % J.nbz, by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
   const int x0 = bx * VF_BX, y0 = by * VF_BY, z0 = bz * VF_BZ;
@@ -143,115 +182,132 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
       const int dx = lx < 0 ? 0 : (lx >= VF_BX ? 2 : 1);
       const int dy = ly < 0 ? 0 : (ly >= VF_BY ? 2 : 1);
       const int dz = lz < 0 ? 0 : (lz >= VF_BZ ? 2 : 1);
-      if (live27[dx * 9 + dy * 3 + dz])
-        v = __ldcg(reinterpret_cast<const uint4*>(J.keys + vf_kidx(J, x, y, z)));
+      if (live27[dx * 9 + dy * 3 + dz]) {
+        const size_t ki = vf_kidx(J, x, y, z);
+        const uint32_t* src = J.keys + ki;
+        if (ki + 4 <= (size_t)J.X * J.Y * J.Zk && (reinterpret_cast<uintptr_t>(src) & 15u) == 0)
+          v = __ldcg(reinterpret_cast<const uint4*>(src));
+        else
+          flood_anomaly(a, 3u, b, (uint32_t)ki);
+      }
     }
     *reinterpret_cast<uint4*>(tile + row * KP + part * 4) = v;
   }
   __syncthreads();
   const int tx = t / VF_BY, ty = t % VF_BY;
   uint32_t* own_row = tile + ((tx + 1) * KNY + (ty + 1)) * KP;
-  uint32_t k[VF_BZ];
+  // Row layout (KP u32): [0..3] z0-4 .. z0-1, [4 + z] z0 + z, [36..39] z0+32 ..
+  // z0+35.  The z halo candidates are fixed for the visit (other bricks' keys).
+  uint32_t hlo, hhi;
+  if (CONN == 26) {
+    hlo = 0; hhi = 0;
 #pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    const uint4 w = *reinterpret_cast<const uint4*>(own_row + 4 + 4 * q);
-    k[4 * q] = w.x; k[4 * q + 1] = w.y; k[4 * q + 2] = w.z; k[4 * q + 3] = w.w;
+    for (int r = 0; r < 9; ++r) {
+      const uint32_t* rp = own_row + ((r / 3 - 1) * KNY + (r % 3 - 1)) * KP;
+      hlo = max(hlo, rp[3]);
+      hhi = max(hhi, rp[4 + VF_BZ]);
+    }
+  } else {
+    hlo = own_row[3];
+    hhi = own_row[4 + VF_BZ];
   }
   uint32_t changed = 0, overflow = 0, nact = 0, nchg = 0, nwarp = 0;
-  // rflag[b][row]: the row changed in the previous sweep.  Every interior row
-  // runs in sweep 0 (new halo data); later only rows next to a change run.
-  for (int q = t; q < KROWS; q += blockDim.x) {
-    const int lx = q / KNY, ly = q % KNY;
-    const bool interior = lx >= 1 && lx <= VF_BX && ly >= 1 && ly <= VF_BY;
-    rflag[q] = interior ? 1 : 0;
-    rflag[KROWS + q] = 0;
-  }
+  // rfw[s][w]: ballot of warp w over "my row changed in sweep s-1" (bit
+  // t & 31; warp w holds x-rows 2w and 2w+1, 16 y-rows each).  A row runs
+  // when a neighbour row changed: its own changes are already final along z
+  // (forward and backward pass) against the neighbour values it read.  Sweep
+  // 0 runs every row (new halo data).
+  if (t < 8) rfw[t] = 0xFFFFFFFFu;
   __syncthreads();
-  const int own = (tx + 1) * KNY + (ty + 1);
   int it = 0, cur = 0;
   for (; it < a.max_sweeps; ++it) {
-    const uint8_t* pf = rflag + cur * KROWS;
+    const uint32_t* pw = rfw + cur * 8;
+    const uint32_t m0 = tx > 0 ? (pw[(tx - 1) >> 1] >> (((tx - 1) & 1) * 16)) & 0xFFFFu : 0u;
+    const uint32_t m1 = (pw[tx >> 1] >> ((tx & 1) * 16)) & 0xFFFFu;
+    const uint32_t m2 = tx < VF_BX - 1 ? (pw[(tx + 1) >> 1] >> (((tx + 1) & 1) * 16)) & 0xFFFFu : 0u;
     bool active;
-    if (CONN == 26) {
-      active = false;
-#pragma unroll
-      for (int r = 0; r < 9; ++r) active |= pf[(tx + r / 3) * KNY + (ty + r % 3)] != 0;
-    } else {
-      active = pf[own] | pf[own - KNY] | pf[own + KNY] | pf[own - 1] | pf[own + 1];
-    }
+    if (CONN == 26)
+      active = ((((m0 | m2) << 1) & (7u << ty)) | ((m1 << 1) & (5u << ty))) != 0;
+    else
+      active = ((((m0 | m2) >> ty) & 1u) | ((m1 << 1) & (5u << ty))) != 0;
     uint32_t chg = 0;
     if (active) {
-      uint32_t c[VF_BZ + 2];
-#pragma unroll
-      for (int jz = 0; jz < VF_BZ + 2; ++jz) c[jz] = 0;
+      // forward: cross-row candidates fused with the increasing-z pass
+      uint32_t prev = hlo;
       if (CONN == 26) {
+        uint4 C = make_uint4(0, 0, 0, 0);
 #pragma unroll
-        for (int r = 0; r < 9; ++r) {
-          const uint32_t* rp = tile + ((tx + r / 3) * KNY + (ty + r % 3)) * KP;
-          c[0] = max(c[0], rp[3]);
+        for (int r = 0; r < 9; ++r)
+          C = max4(C, lds4(own_row + ((r / 3 - 1) * KNY + (r % 3 - 1)) * KP + 4));
+        uint4 kv = lds4(own_row + 4);
+        uint32_t cp = hlo;  // window maximum at z-1 of the chunk
+#pragma unroll 1
+        for (int q = 0; q < 8; ++q) {
+          uint4 Cn = make_uint4(hhi, 0, 0, 0), kn = make_uint4(0, 0, 0, 0);
+          if (q + 1 < 8) {
+            Cn = make_uint4(0, 0, 0, 0);
 #pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const uint4 w = *reinterpret_cast<const uint4*>(rp + 4 + 4 * q);
-            c[1 + 4 * q] = max(c[1 + 4 * q], w.x);
-            c[2 + 4 * q] = max(c[2 + 4 * q], w.y);
-            c[3 + 4 * q] = max(c[3 + 4 * q], w.z);
-            c[4 + 4 * q] = max(c[4 + 4 * q], w.w);
+            for (int r = 0; r < 9; ++r)
+              Cn = max4(Cn, lds4(own_row + ((r / 3 - 1) * KNY + (r % 3 - 1)) * KP + 8 + 4 * q));
+            kn = lds4(own_row + 8 + 4 * q);
           }
-          c[VF_BZ + 1] = max(c[VF_BZ + 1], rp[4 + VF_BZ]);
+          const uint32_t w[4] = {max(cp, max(C.x, C.y)), max(C.x, max(C.y, C.z)),
+                                 max(C.y, max(C.z, C.w)), max(C.z, max(C.w, Cn.x))};
+          const uint32_t kk[4] = {kv.x, kv.y, kv.z, kv.w};
+          uint32_t f[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const uint32_t k1 = relax1(kk[j], w[j], overflow);
+            f[j] = relax1(k1, prev, overflow);
+            prev = f[j];
+            if (f[j] != kk[j]) chg |= 1u << (4 * q + j);
+          }
+          if ((chg >> (4 * q)) & 0xFu)
+            *reinterpret_cast<uint4*>(own_row + 4 + 4 * q) = make_uint4(f[0], f[1], f[2], f[3]);
+          cp = C.w; C = Cn; kv = kn;
         }
       } else {
-        const int rs[4][2] = {{0, 1}, {2, 1}, {1, 0}, {1, 2}};
+#pragma unroll 1
+        for (int q = 0; q < 8; ++q) {
+          const uint4 M = max4(max4(lds4(own_row - KNY * KP + 4 + 4 * q), lds4(own_row + KNY * KP + 4 + 4 * q)),
+                               max4(lds4(own_row - KP + 4 + 4 * q), lds4(own_row + KP + 4 + 4 * q)));
+          const uint4 kv = lds4(own_row + 4 + 4 * q);
+          const uint32_t w[4] = {M.x, M.y, M.z, M.w};
+          const uint32_t kk[4] = {kv.x, kv.y, kv.z, kv.w};
+          uint32_t f[4];
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          const uint32_t* rp = tile + ((tx + rs[r][0]) * KNY + (ty + rs[r][1])) * KP;
-#pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const uint4 w = *reinterpret_cast<const uint4*>(rp + 4 + 4 * q);
-            c[1 + 4 * q] = max(c[1 + 4 * q], w.x);
-            c[2 + 4 * q] = max(c[2 + 4 * q], w.y);
-            c[3 + 4 * q] = max(c[3 + 4 * q], w.z);
-            c[4 + 4 * q] = max(c[4 + 4 * q], w.w);
+          for (int j = 0; j < 4; ++j) {
+            const uint32_t k1 = relax1(kk[j], w[j], overflow);
+            f[j] = relax1(k1, prev, overflow);
+            prev = f[j];
+            if (f[j] != kk[j]) chg |= 1u << (4 * q + j);
           }
+          if ((chg >> (4 * q)) & 0xFu)
+            *reinterpret_cast<uint4*>(own_row + 4 + 4 * q) = make_uint4(f[0], f[1], f[2], f[3]);
         }
-        c[0] = own_row[3];              // z - 1 halo of the own row
-        c[VF_BZ + 1] = own_row[4 + VF_BZ];
       }
-      // cross-row candidates (26: the 3x3x3 block; 6: the 4 side rows)
+      // backward in-row pass
+      prev = hhi;
+#pragma unroll 1
+      for (int q = 7; q >= 0; --q) {
+        const uint4 kv = lds4(own_row + 4 + 4 * q);
+        const uint32_t kk[4] = {kv.x, kv.y, kv.z, kv.w};
+        uint32_t f[4];
+        uint32_t cq = 0;
 #pragma unroll
-      for (int z = 0; z < VF_BZ; ++z) {
-        const uint32_t m = CONN == 26 ? max(c[z], max(c[z + 1], c[z + 2])) : c[z + 1];
-        const uint32_t kk = k[z];
-        if (kk == VF_KEY_UNREACHED && m >= VF_KEY_MIN_REACHED && m < 2u * VF_KEY_STEP) overflow = 1;
-        const uint32_t nk = kk ? max(kk, m >= 2u * VF_KEY_STEP ? m - VF_KEY_STEP : 0u) : 0u;
-        if (nk != kk) { k[z] = nk; chg |= 1u << z; }
-      }
-      // in-row sweeps along z, from the z halo: a front along z crosses the
-      // whole row in one sweep
-      uint32_t prev = c[0];
-#pragma unroll
-      for (int z = 0; z < VF_BZ; ++z) {
-        const uint32_t kk = k[z];
-        if (kk == VF_KEY_UNREACHED && prev >= VF_KEY_MIN_REACHED && prev < 2u * VF_KEY_STEP) overflow = 1;
-        const uint32_t nk = kk ? max(kk, prev >= 2u * VF_KEY_STEP ? prev - VF_KEY_STEP : 0u) : 0u;
-        if (nk != kk) { k[z] = nk; chg |= 1u << z; }
-        prev = nk;
-      }
-      prev = c[VF_BZ + 1];
-#pragma unroll
-      for (int z = VF_BZ - 1; z >= 0; --z) {
-        const uint32_t kk = k[z];
-        if (kk == VF_KEY_UNREACHED && prev >= VF_KEY_MIN_REACHED && prev < 2u * VF_KEY_STEP) overflow = 1;
-        const uint32_t nk = kk ? max(kk, prev >= 2u * VF_KEY_STEP ? prev - VF_KEY_STEP : 0u) : 0u;
-        if (nk != kk) { k[z] = nk; chg |= 1u << z; }
-        prev = nk;
-      }
-      if (chg) {
-#pragma unroll
-        for (int z = 0; z < VF_BZ; ++z)
-          if (chg & (1u << z)) own_row[4 + z] = k[z];
+        for (int j = 3; j >= 0; --j) {
+          f[j] = relax1(kk[j], prev, overflow);
+          prev = f[j];
+          if (f[j] != kk[j]) cq |= 1u << j;
+        }
+        if (cq) {
+          *reinterpret_cast<uint4*>(own_row + 4 + 4 * q) = make_uint4(f[0], f[1], f[2], f[3]);
+          chg |= cq << (4 * q);
+        }
       }
     }
-    rflag[(cur ^ 1) * KROWS + own] = chg != 0;
+    const unsigned bal = __ballot_sync(0xFFFFFFFFu, chg != 0);
+    if ((t & 31) == 0) rfw[(cur ^ 1) * 8 + (t >> 5)] = bal;
     changed |= chg;
     cur ^= 1;
     if (active) ++nact;
@@ -261,9 +317,17 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
   }
   const int x = x0 + tx, y = y0 + ty;
   if (changed && x < (int)J.X && y < (int)J.Y) {
+    // write back the changed 32-byte sectors of the row
     const int nq = min(VF_BZ, (int)J.Zk - z0) / 4;
-    uint4* dst = reinterpret_cast<uint4*>(J.keys + vf_kidx(J, x, y, z0));
-    for (int q = 0; q < nq; ++q) __stcg(dst + q, make_uint4(k[4 * q], k[4 * q + 1], k[4 * q + 2], k[4 * q + 3]));
+    const size_t ki = vf_kidx(J, x, y, z0);
+    uint4* dst = reinterpret_cast<uint4*>(J.keys + ki);
+    if (ki + 4 * (size_t)nq <= (size_t)J.X * J.Y * J.Zk && (reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (q < nq && ((changed >> (8 * (q >> 1))) & 0xFFu)) __stcg(dst + q, lds4(own_row + 4 + 4 * q));
+    } else {
+      flood_anomaly(a, 5u, b, (uint32_t)ki);
+    }
   }
   if (overflow) atomicOr(&a.st[jid].err, VF_JERR_DIST_OVERFLOW);
   // neighbour bricks touched by changed boundary voxels
@@ -323,14 +387,14 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
   }
 }
 
-__global__ void __launch_bounds__(256, 2) k_relax(FloodArgs a) {
+__global__ void __launch_bounds__(256, 3) k_relax(FloodArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t* tile = reinterpret_cast<uint32_t*>(smem_raw);
   __shared__ uint32_t live27[27];
   __shared__ uint32_t dirs;
   __shared__ int reenq;
   __shared__ uint32_t item;
-  __shared__ uint8_t rflag[2 * KROWS];
+  __shared__ uint32_t rfw[16];
   for (uint32_t p = 0; p < a.max_passes; ++p) {
     const uint32_t cur = p % 3u;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -347,10 +411,18 @@ __global__ void __launch_bounds__(256, 2) k_relax(FloodArgs a) {
       const uint32_t i = item;
       if (i >= qn) break;
       const uint32_t b = a.queue[cur][i];
+      if (b >= a.nbricks) {
+        if (threadIdx.x == 0) flood_anomaly(a, 1u, b, i);
+        continue;
+      }
       const uint32_t jid = a.brick_job[b];
+      if (jid >= a.njobs) {
+        if (threadIdx.x == 0) flood_anomaly(a, 2u, b, jid);
+        continue;
+      }
       const JobDesc& J = a.jobs[jid];
-      if (J.distance == 1) relax_brick<6>(a, J, jid, b, p, tile, live27, &dirs, &reenq, rflag);
-      else relax_brick<26>(a, J, jid, b, p, tile, live27, &dirs, &reenq, rflag);
+      if (J.distance == 1) relax_brick<6>(a, J, jid, b, p, tile, live27, &dirs, &reenq, rfw);
+      else relax_brick<26>(a, J, jid, b, p, tile, live27, &dirs, &reenq, rfw);
       if (threadIdx.x == 0) atomicMax(&a.st[jid].passes, p + 1);
       ++visits;
     }
@@ -688,6 +760,8 @@ cudaError_t flood_relax(cudaStream_t st, const JobDesc* dj, JobState* ds,
   a.max_passes = fs.max_passes;
   a.max_sweeps = (fs.max_sweeps > 0 && fs.max_sweeps <= MAXIT) ? fs.max_sweeps : MAXIT;
   a.pass_sizes = fs.pass_sizes;
+  a.nbricks = fs.total_bricks;
+  a.njobs = fs.njobs;
   int blocks = relax_blocks(num_sms);
   if (fs.ctas_per_sm > 0 && fs.ctas_per_sm * num_sms < blocks) blocks = fs.ctas_per_sm * num_sms;
   if (blocks_used) *blocks_used = blocks;

@@ -89,6 +89,7 @@ struct FloodScratch {
   uint32_t* stats;       // [4] brick visits, passes, overflow, timeout
   uint32_t max_passes;
   uint32_t total_bricks;
+  uint32_t njobs = 1;    // job descriptors in the table
   int max_sweeps = 0;    // tuning: sweeps per brick visit (0: default cap)
   int ctas_per_sm = 0;   // tuning: resident CTAs per SM (0: as many as fit)
   uint32_t* pass_sizes = nullptr;  // statistics: bricks queued per pass (256)

@@ -153,6 +153,7 @@ extern "C" vf_status vf_flood_noalloc(const uint16_t* d_grid, uint16_t* d_labels
   fs.epoch = reinterpret_cast<uint32_t*>(S + o_epoch);
   fs.max_passes = 1u << 20;
   fs.total_bricks = (uint32_t)nb;
+  fs.njobs = 1;
   vfk::flood_seed_bricks(st, ddesc, dstate, 1, live, list, lcount);
   vfk::flood_init_keys(st, ddesc, list, lcount, (uint32_t)nb, bj, live);
   vfk::flood_seed(st, ddesc, dstate, 1, fs, live);

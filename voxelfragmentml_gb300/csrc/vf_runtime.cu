@@ -592,11 +592,13 @@ static vfk::FloodScratch flood_scratch(Batch& B) {
   fs.qhead = sc + 4;     // [3]
   fs.barrier = sc + 8;   // [2]
   fs.err = sc + 12;      // [1]
-  fs.stats = sc + 16;    // [8]: visits, passes, busy warp-sweeps, timeouts, sweeps,
-                         // sweep-cap hits, active row-sweeps, changed voxels
+  fs.stats = sc + 16;    // [11]: visits, passes, busy warp-sweeps, timeouts, sweeps,
+                         // sweep-cap hits, active row-sweeps, changed voxels, and the
+                         // first out-of-range access (code, two values)
   fs.epoch = static_cast<uint32_t*>(B.epoch.p);
   fs.max_passes = 1u << 20;
   fs.total_bricks = B.sz.bricks;
+  fs.njobs = (uint32_t)B.jobs.size();
   fs.max_sweeps = B.ctx->tune.flood_sweeps;
   fs.ctas_per_sm = B.ctx->tune.flood_ctas;
   fs.pass_sizes = sc + 128;  // [256]
@@ -759,7 +761,8 @@ vf_status Batch::finish(vf_job_result* res) {
       first = st;
       set_error("job " + std::to_string(i) + ": " +
                 (st == VF_ERR_SEED_SEARCH ? "seed search exceeded 1e6 tries"
-                 : st == VF_ERR_TIMEOUT   ? "flood did not converge (bounded wait expired)"
+                 : st == VF_ERR_TIMEOUT   ? ((ferr & 8u) ? "flood relaxation skipped an out-of-range brick or key access"
+                                                        : "flood did not converge (bounded wait expired)")
                  : st == VF_ERR_RANGE     ? "value out of range (prefix, distance or count)"
                                           : "invalid seeds or parameters"));
     }
@@ -784,10 +787,10 @@ vf_status Batch::finish(vf_job_result* res) {
     ctx->last_flood_passes = h_scal[17];
     ctx->last_flood_sweeps = h_scal[20];
     ctx->last_flood_maxit = h_scal[21];
-    for (int i = 0; i < 8; ++i) ctx->last_flood_counters[i] = h_scal[16 + i];
+    for (int i = 0; i < 11; ++i) ctx->last_flood_counters[i] = h_scal[16 + i];
     for (int i = 0; i < 256; ++i) ctx->last_pass_sizes[i] = h_scal[128 + i];
   } else {
-    for (int i = 0; i < 8; ++i) ctx->last_flood_counters[i] = 0;
+    for (int i = 0; i < 11; ++i) ctx->last_flood_counters[i] = 0;
     ctx->last_flood_ms = 0.f;
     ctx->last_flood_visits = 0;
     ctx->last_flood_passes = 0;
