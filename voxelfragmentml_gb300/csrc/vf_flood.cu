@@ -32,10 +32,10 @@
 
 namespace {
 
-constexpr int KP = 44;                 // smem row pitch (u32): conflict-free 16 B loads
+constexpr int KP = 36;                 // smem row pitch (u32): conflict-free 16 B loads
 constexpr int KNX = VF_BX + 2, KNY = VF_BY + 2;
 constexpr int KROWS = KNX * KNY;
-constexpr int KZW = 10;                // 16-byte chunks per staged row: z in [z0-4, z0+36)
+constexpr int KZW = 10;                // staging items per row: 8 chunks of 4 keys, 2 halo keys
 constexpr int TILE_BYTES = KROWS * KP * 4;
 constexpr int MAXIT = 96;              // default cap of relaxation sweeps per brick visit
 
@@ -172,32 +172,47 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
   __shared__ uint32_t scnt[3];
   if (t == 0) { *dirs = 0; *reenq = 0; scnt[0] = 0; scnt[1] = 0; scnt[2] = 0; }
   __syncthreads();
-  // stage keys: rows [x0-1, x0+17) x [y0-1, y0+17), z [z0-4, z0+36)
+  // stage keys: rows [x0-1, x0+17) x [y0-1, y0+17), keys z0 .. z0+31 and z0-1, z0+32
   for (int q = t; q < KROWS * KZW; q += blockDim.x) {
     const int row = q / KZW, part = q % KZW;
-    const int lx = row / KNY - 1, ly = row % KNY - 1, lz = part * 4 - 4;
-    const int x = x0 + lx, y = y0 + ly, z = z0 + lz;
-    uint4 v = make_uint4(0, 0, 0, 0);
+    // part 0..7: keys z0 + 4 part .. +3 -> [4 + 4 part]; 8: key z0-1 -> [3];
+    // 9: key z0+32 -> [0]
+    const int lx = row / KNY - 1, ly = row % KNY - 1;
+    const int z = part < 8 ? z0 + 4 * part : (part == 8 ? z0 - 1 : z0 + VF_BZ);
+    const int x = x0 + lx, y = y0 + ly;
+    bool load = false;
     if (x >= 0 && y >= 0 && z >= 0 && x < (int)J.X && y < (int)J.Y && z < (int)J.Zk) {
       const int dx = lx < 0 ? 0 : (lx >= VF_BX ? 2 : 1);
       const int dy = ly < 0 ? 0 : (ly >= VF_BY ? 2 : 1);
-      const int dz = lz < 0 ? 0 : (lz >= VF_BZ ? 2 : 1);
-      if (live27[dx * 9 + dy * 3 + dz]) {
-        const size_t ki = vf_kidx(J, x, y, z);
+      const int dz = part < 8 ? 1 : (part == 8 ? 0 : 2);
+      load = live27[dx * 9 + dy * 3 + dz] != 0;
+    }
+    const size_t ki = load ? vf_kidx(J, x, y, z) : 0;
+    const size_t nk = (size_t)J.X * J.Y * J.Zk;
+    if (part < 8) {
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (load) {
         const uint32_t* src = J.keys + ki;
-        if (ki + 4 <= (size_t)J.X * J.Y * J.Zk && (reinterpret_cast<uintptr_t>(src) & 15u) == 0)
+        if (ki + 4 <= nk && (reinterpret_cast<uintptr_t>(src) & 15u) == 0)
           v = __ldcg(reinterpret_cast<const uint4*>(src));
         else
           flood_anomaly(a, 3u, b, (uint32_t)ki);
       }
+      *reinterpret_cast<uint4*>(tile + row * KP + 4 + 4 * part) = v;
+    } else {
+      uint32_t v = 0;
+      if (load) {
+        if (ki < nk) v = __ldcg(J.keys + ki);
+        else flood_anomaly(a, 3u, b, (uint32_t)ki);
+      }
+      tile[row * KP + (part == 8 ? 3 : 0)] = v;
     }
-    *reinterpret_cast<uint4*>(tile + row * KP + part * 4) = v;
   }
   __syncthreads();
   const int tx = t / VF_BY, ty = t % VF_BY;
   uint32_t* own_row = tile + ((tx + 1) * KNY + (ty + 1)) * KP;
-  // Row layout (KP u32): [0..3] z0-4 .. z0-1, [4 + z] z0 + z, [36..39] z0+32 ..
-  // z0+35.  The z halo candidates are fixed for the visit (other bricks' keys).
+  // Row layout (KP u32): [0] key z0+32, [3] key z0-1, [4 + z] key z0 + z.  The
+  // z halo candidates are fixed for the visit (other bricks' keys).
   uint32_t hlo, hhi;
   if (CONN == 26) {
     hlo = 0; hhi = 0;
@@ -205,11 +220,11 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     for (int r = 0; r < 9; ++r) {
       const uint32_t* rp = own_row + ((r / 3 - 1) * KNY + (r % 3 - 1)) * KP;
       hlo = max(hlo, rp[3]);
-      hhi = max(hhi, rp[4 + VF_BZ]);
+      hhi = max(hhi, rp[0]);
     }
   } else {
     hlo = own_row[3];
-    hhi = own_row[4 + VF_BZ];
+    hhi = own_row[0];
   }
   uint32_t changed = 0, overflow = 0, nact = 0, nchg = 0, nwarp = 0;
   // rfw[s][w]: ballot of warp w over "my row changed in sweep s-1" (bit
@@ -387,7 +402,7 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
   }
 }
 
-__global__ void __launch_bounds__(256, 3) k_relax(FloodArgs a) {
+__global__ void __launch_bounds__(256, 4) k_relax(FloodArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t* tile = reinterpret_cast<uint32_t*>(smem_raw);
   __shared__ uint32_t live27[27];
