@@ -35,7 +35,6 @@ namespace {
 constexpr int KP = 36;                 // smem row pitch (u32): conflict-free 16 B loads
 constexpr int KNX = VF_BX + 2, KNY = VF_BY + 2;
 constexpr int KROWS = KNX * KNY;
-constexpr int KZW = 10;                // staging items per row: 8 chunks of 4 keys, 2 halo keys
 constexpr int TILE_BYTES = KROWS * KP * 4;
 constexpr int MAXIT = 96;              // default cap of relaxation sweeps per brick visit
 
@@ -172,41 +171,71 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
   __shared__ uint32_t scnt[3];
   if (t == 0) { *dirs = 0; *reenq = 0; scnt[0] = 0; scnt[1] = 0; scnt[2] = 0; }
   __syncthreads();
-  // stage keys: rows [x0-1, x0+17) x [y0-1, y0+17), keys z0 .. z0+31 and z0-1, z0+32
-  for (int q = t; q < KROWS * KZW; q += blockDim.x) {
-    const int row = q / KZW, part = q % KZW;
-    // part 0..7: keys z0 + 4 part .. +3 -> [4 + 4 part]; 8: key z0-1 -> [3];
-    // 9: key z0+32 -> [0]
-    const int lx = row / KNY - 1, ly = row % KNY - 1;
-    const int z = part < 8 ? z0 + 4 * part : (part == 8 ? z0 - 1 : z0 + VF_BZ);
-    const int x = x0 + lx, y = y0 + ly;
-    bool load = false;
-    if (x >= 0 && y >= 0 && z >= 0 && x < (int)J.X && y < (int)J.Y && z < (int)J.Zk) {
-      const int dx = lx < 0 ? 0 : (lx >= VF_BX ? 2 : 1);
-      const int dy = ly < 0 ? 0 : (ly >= VF_BY ? 2 : 1);
-      const int dz = part < 8 ? 1 : (part == 8 ? 0 : 2);
-      load = live27[dx * 9 + dy * 3 + dz] != 0;
-    }
-    const size_t ki = load ? vf_kidx(J, x, y, z) : 0;
+  // stage keys: rows [x0-1, x0+17) x [y0-1, y0+17), keys z0 .. z0+31 (8 chunks
+  // of 4) and the halo keys z0-1, z0+32.  Each thread keeps SU 16-byte loads in
+  // flight before it stores them.  Keys outside the grid or in a brick without
+  // occupied voxels are zero (EMPTY).
+  {
+    constexpr int SU = 6;
     const size_t nk = (size_t)J.X * J.Y * J.Zk;
-    if (part < 8) {
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (load) {
-        const uint32_t* src = J.keys + ki;
-        if (ki + 4 <= nk && (reinterpret_cast<uintptr_t>(src) & 15u) == 0)
-          v = __ldcg(reinterpret_cast<const uint4*>(src));
-        else
-          flood_anomaly(a, 3u, b, (uint32_t)ki);
+    bool bad = false;
+#pragma unroll 1
+    for (int base = t; base < KROWS * 8; base += SU * 256) {
+      uint4 v[SU];
+#pragma unroll
+      for (int u = 0; u < SU; ++u) {
+        const int q = base + u * 256;
+        v[u] = make_uint4(0, 0, 0, 0);
+        if (q < KROWS * 8) {
+          const int row = q >> 3, part = q & 7;
+          const int lx = row / KNY - 1, ly = row % KNY - 1;
+          const int x = x0 + lx, y = y0 + ly, z = z0 + 4 * part;
+          if (x >= 0 && y >= 0 && x < (int)J.X && y < (int)J.Y && z < (int)J.Zk) {
+            const int dx = lx < 0 ? 0 : (lx >= VF_BX ? 2 : 1);
+            const int dy = ly < 0 ? 0 : (ly >= VF_BY ? 2 : 1);
+            if (live27[dx * 9 + dy * 3 + 1]) {
+              const size_t ki = vf_kidx(J, x, y, z);
+              const uint32_t* src = J.keys + ki;
+              if (ki + 4 <= nk && (reinterpret_cast<uintptr_t>(src) & 15u) == 0)
+                v[u] = __ldcg(reinterpret_cast<const uint4*>(src));
+              else
+                bad = true;
+            }
+          }
+        }
       }
-      *reinterpret_cast<uint4*>(tile + row * KP + 4 + 4 * part) = v;
-    } else {
-      uint32_t v = 0;
-      if (load) {
-        if (ki < nk) v = __ldcg(J.keys + ki);
-        else flood_anomaly(a, 3u, b, (uint32_t)ki);
+#pragma unroll
+      for (int u = 0; u < SU; ++u) {
+        const int q = base + u * 256;
+        if (q < KROWS * 8) *reinterpret_cast<uint4*>(tile + (q >> 3) * KP + 4 + 4 * (q & 7)) = v[u];
       }
-      tile[row * KP + (part == 8 ? 3 : 0)] = v;
     }
+    uint32_t h[3];
+#pragma unroll
+    for (int u = 0; u < 3; ++u) {
+      const int q = t + u * 256;  // row q >> 1; side 0: key z0-1 -> [3], 1: key z0+32 -> [0]
+      h[u] = 0;
+      if (q < KROWS * 2) {
+        const int row = q >> 1, side = q & 1;
+        const int lx = row / KNY - 1, ly = row % KNY - 1;
+        const int x = x0 + lx, y = y0 + ly, z = side ? z0 + VF_BZ : z0 - 1;
+        if (x >= 0 && y >= 0 && z >= 0 && x < (int)J.X && y < (int)J.Y && z < (int)J.Zk) {
+          const int dx = lx < 0 ? 0 : (lx >= VF_BX ? 2 : 1);
+          const int dy = ly < 0 ? 0 : (ly >= VF_BY ? 2 : 1);
+          if (live27[dx * 9 + dy * 3 + (side ? 2 : 0)]) {
+            const size_t ki = vf_kidx(J, x, y, z);
+            if (ki < nk) h[u] = __ldcg(J.keys + ki);
+            else bad = true;
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 3; ++u) {
+      const int q = t + u * 256;
+      if (q < KROWS * 2) tile[(q >> 1) * KP + ((q & 1) ? 0 : 3)] = h[u];
+    }
+    if (bad) flood_anomaly(a, 3u, b, (uint32_t)t);
   }
   __syncthreads();
   const int tx = t / VF_BY, ty = t % VF_BY;
