@@ -244,6 +244,7 @@ def main():
     L.vf_ctx_event_record(ctx.h, 0)
     launches, flood_ms, flood_bytes, visits, passes, sweeps, maxit = 0, 0.0, 0, 0, 0, 0, 0
     act_rows, key_changes, busy_warps = 0, 0, 0
+    phase = {}
     stage_tot = {}
     for _ in range(args.steps):
         rb.execute(download=False)
@@ -259,6 +260,8 @@ def main():
         key_changes += st["flood_key_changes"]
         busy_warps += st["flood_busy_warp_sweeps"]
         pass_sizes = ctx.flood_pass_sizes()
+        for k, v in st["flood_phase_cycles"].items():
+            phase[k] = phase.get(k, 0) + v
         for k, v in ctx.stage_ms().items():
             stage_tot[k] = stage_tot.get(k, 0.0) + v
     L.vf_ctx_event_record(ctx.h, 1)
@@ -342,6 +345,8 @@ def main():
             "busy_warps_per_sweep": busy_warps / max(sweeps, 1),
             "key_changes_per_visit": key_changes / max(visits, 1),
             "bricks_per_pass_last_step": pass_sizes,
+            "phase_share": {k: round(v / max(sum(phase.values()), 1), 4) for k, v in phase.items()},
+            "phase_kcycles_per_visit": {k: round(v / max(visits, 1) / 1000.0, 2) for k, v in phase.items()},
             "launch_ms": flood_launch_ms,
             "traffic": K_RELAX_DRAM_BYTES_PER_VISIT * visits / args.steps,
             "traffic_source": "ncu DRAM bytes per brick visit (48-job capture) x visits of this launch"}

@@ -672,8 +672,8 @@ vf_status vf_ctx_last_graph(vf_ctx* ctx, int* replayed) {
 
 vf_status vf_ctx_flood_counters(vf_ctx* ctx, uint64_t* out, uint32_t n) {
   if (!ctx || (n && !out)) return fail(VF_ERR_INVALID, "NULL argument");
-  for (uint32_t i = 0; i < n && i < 11; ++i) out[i] = ctx->c.last_flood_counters[i];
-  for (uint32_t i = 11; i < n; ++i) out[i] = 0;
+  for (uint32_t i = 0; i < n && i < 16; ++i) out[i] = ctx->c.last_flood_counters[i];
+  for (uint32_t i = 16; i < n; ++i) out[i] = 0;
   return VF_OK;
 }
 

@@ -51,7 +51,8 @@ struct FloodArgs {
   uint32_t* err;
   uint32_t* stats;   // [0] visits, [1] passes, [2] busy warp-sweeps, [3] timeout, [4] sweeps,
                      // [5] visits at the sweep cap, [6] active row-sweeps, [7] key changes,
-                     // [8..10] first out-of-range access (code, two values)
+                     // [8..10] first out-of-range access (code, two values),
+                     // [11..15] SM cycles / 256 per phase of the CTAs' work
   uint32_t max_passes;
   int max_sweeps;    // sweeps per brick visit before the brick re-queues itself
   uint32_t* pass_sizes;  // bricks queued for each of the first 256 passes (or null)
@@ -155,7 +156,10 @@ __device__ __forceinline__ uint4 lds4(const uint32_t* p) {
 template <int CONN>
 __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, uint32_t b,
                             uint32_t pass, uint32_t* tile, uint32_t* live27, uint32_t* dirs,
-                            int* reenq, uint32_t* rfw) {
+                            int* reenq, uint32_t* rfw, unsigned long long* ph) {
+  // ph (thread 0): SM cycles of [1] live map + staging, [2] sweeps, [3] write-back + enqueue
+  long long c0 = 0;
+  if (threadIdx.x == 0) c0 = clock64();
   const uint32_t lb = b - J.brick_base;
   const int bz = lb % J.nbz, by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
   const int x0 = bx * VF_BX, y0 = by * VF_BY, z0 = bz * VF_BZ;
@@ -238,6 +242,8 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     if (bad) flood_anomaly(a, 3u, b, (uint32_t)t);
   }
   __syncthreads();
+  long long c1 = 0;
+  if (t == 0) { c1 = clock64(); ph[1] += c1 - c0; }
   const int tx = t / VF_BY, ty = t % VF_BY;
   uint32_t* own_row = tile + ((tx + 1) * KNY + (ty + 1)) * KP;
   // Row layout (KP u32): [0] key z0+32, [3] key z0-1, [4 + z] key z0 + z.  The
@@ -359,6 +365,8 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     nchg += __popc(chg);
     if (!__syncthreads_or(chg != 0)) break;
   }
+  long long c2 = 0;
+  if (t == 0) { c2 = clock64(); ph[2] += c2 - c1; }
   const int x = x0 + tx, y = y0 + ty;
   if (changed && x < (int)J.X && y < (int)J.Y) {
     // write back the changed 32-byte sectors of the row
@@ -429,6 +437,7 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     if (t == 27 && *reenq) { want = true; nb = b; }
     enqueue(a, nb, pass + 1, want);
   }
+  if (t == 0) ph[3] += clock64() - c2;
 }
 
 __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs a) {
@@ -439,6 +448,8 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs a) {
   __shared__ int reenq;
   __shared__ uint32_t item;
   __shared__ uint32_t rfw[16];
+  __shared__ unsigned long long ph[5];  // thread 0: SM cycles per phase (see flush below)
+  if (threadIdx.x < 5) ph[threadIdx.x] = 0;
   for (uint32_t p = 0; p < a.max_passes; ++p) {
     const uint32_t cur = p % 3u;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -448,9 +459,13 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs a) {
     const uint32_t qn = ld_acquire(&a.qcount[cur]);
     if (a.pass_sizes && blockIdx.x == 0 && threadIdx.x == 0 && p < 256) a.pass_sizes[p] = qn;
     uint32_t visits = 0;
+    long long c_claim = 0;
     for (;;) {
       __syncthreads();
-      if (threadIdx.x == 0) item = atomicAdd(&a.qhead[cur], 1u);
+      if (threadIdx.x == 0) {
+        c_claim = clock64();
+        item = atomicAdd(&a.qhead[cur], 1u);
+      }
       __syncthreads();
       const uint32_t i = item;
       if (i >= qn) break;
@@ -465,13 +480,27 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs a) {
         continue;
       }
       const JobDesc& J = a.jobs[jid];
-      if (J.distance == 1) relax_brick<6>(a, J, jid, b, p, tile, live27, &dirs, &reenq, rfw);
-      else relax_brick<26>(a, J, jid, b, p, tile, live27, &dirs, &reenq, rfw);
+      const int conn6 = J.distance == 1;
+      if (threadIdx.x == 0) ph[0] += clock64() - c_claim;
+      if (conn6) relax_brick<6>(a, J, jid, b, p, tile, live27, &dirs, &reenq, rfw, ph);
+      else relax_brick<26>(a, J, jid, b, p, tile, live27, &dirs, &reenq, rfw, ph);
       if (threadIdx.x == 0) atomicMax(&a.st[jid].passes, p + 1);
       ++visits;
     }
     if (threadIdx.x == 0 && visits) atomicAdd(&a.stats[0], visits);
-    if (!grid_sync(a.bar, gridDim.x, a.err, a.stats)) return;
+    const bool synced = grid_sync(a.bar, gridDim.x, a.err, a.stats);
+    if (threadIdx.x == 0) {
+      // phase cycles: [0] claim, [1] staging, [2] sweeps, [3] write-back +
+      // enqueue, [4] from the failed claim through the pass barrier; added to
+      // stats[11..15] in units of 256 cycles
+      ph[4] += clock64() - c_claim;
+      for (int i = 0; i < 5; ++i) {
+        const uint32_t c = (uint32_t)(ph[i] >> 8);
+        if (c) atomicAdd(a.stats + 11 + i, c);
+        ph[i] &= 255u;
+      }
+    }
+    if (!synced) return;
     const uint32_t nn = ld_acquire(&a.qcount[(p + 1) % 3]);
     if (nn == 0 || ld_acquire(a.err) != 0) {
       if (blockIdx.x == 0 && threadIdx.x == 0) a.stats[1] = p + 1;

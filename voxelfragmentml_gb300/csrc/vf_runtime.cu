@@ -592,9 +592,10 @@ static vfk::FloodScratch flood_scratch(Batch& B) {
   fs.qhead = sc + 4;     // [3]
   fs.barrier = sc + 8;   // [2]
   fs.err = sc + 12;      // [1]
-  fs.stats = sc + 16;    // [11]: visits, passes, busy warp-sweeps, timeouts, sweeps,
-                         // sweep-cap hits, active row-sweeps, changed voxels, and the
-                         // first out-of-range access (code, two values)
+  fs.stats = sc + 16;    // [16]: visits, passes, busy warp-sweeps, timeouts, sweeps,
+                         // sweep-cap hits, active row-sweeps, changed voxels, the
+                         // first out-of-range access (code, two values) and the
+                         // SM cycles / 256 of five phases of the relaxation CTAs
   fs.epoch = static_cast<uint32_t*>(B.epoch.p);
   fs.max_passes = 1u << 20;
   fs.total_bricks = B.sz.bricks;
@@ -787,10 +788,10 @@ vf_status Batch::finish(vf_job_result* res) {
     ctx->last_flood_passes = h_scal[17];
     ctx->last_flood_sweeps = h_scal[20];
     ctx->last_flood_maxit = h_scal[21];
-    for (int i = 0; i < 11; ++i) ctx->last_flood_counters[i] = h_scal[16 + i];
+    for (int i = 0; i < 16; ++i) ctx->last_flood_counters[i] = h_scal[16 + i];
     for (int i = 0; i < 256; ++i) ctx->last_pass_sizes[i] = h_scal[128 + i];
   } else {
-    for (int i = 0; i < 11; ++i) ctx->last_flood_counters[i] = 0;
+    for (int i = 0; i < 16; ++i) ctx->last_flood_counters[i] = 0;
     ctx->last_flood_ms = 0.f;
     ctx->last_flood_visits = 0;
     ctx->last_flood_passes = 0;

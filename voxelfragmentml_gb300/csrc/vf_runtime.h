@@ -136,7 +136,7 @@ struct Ctx {
   uint64_t last_flood_visits = 0;
   uint64_t last_flood_passes = 0;
   uint64_t last_flood_sweeps = 0;
-  uint64_t last_flood_counters[11] = {};  // raw flood counters of the last batched run
+  uint64_t last_flood_counters[16] = {};  // raw flood counters of the last batched run
   uint32_t last_pass_sizes[256] = {};    // bricks queued per flood pass (first 256)
   uint64_t last_flood_maxit = 0;
   vf_status alloc(DevBuf& b, size_t bytes);
