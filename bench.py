@@ -243,7 +243,7 @@ def main():
     ctx.synchronize()
     L.vf_ctx_event_record(ctx.h, 0)
     launches, flood_ms, flood_bytes, visits, passes, sweeps, maxit = 0, 0.0, 0, 0, 0, 0, 0
-    act_rows, key_changes, busy_warps = 0, 0, 0
+    act_rows, key_changes, busy_warps, empty = 0, 0, 0, 0
     phase = {}
     stage_tot = {}
     for _ in range(args.steps):
@@ -253,6 +253,7 @@ def main():
         flood_ms += st["flood_ms"]
         flood_bytes += st["flood_bytes"]
         visits += st["flood_visits"]
+        empty += st["flood_empty_visits"]
         passes += st["flood_passes"]
         sweeps += st["flood_sweeps"]
         maxit += st["flood_maxit_hits"]
@@ -338,6 +339,7 @@ def main():
             "algorithmic_bytes_per_launch": flood_launch_bytes,
             "bytes_rule": "4 B (u16 label read + write) per voxel of every brick visit",
             "brick_visits_per_launch": visits / args.steps,
+            "empty_visits_per_launch": empty / args.steps,
             "passes_per_launch": passes / args.steps,
             "sweeps_per_visit": sweeps / max(visits, 1),
             "visits_at_sweep_cap": maxit / args.steps,
@@ -348,7 +350,7 @@ def main():
             "phase_share": {k: round(v / max(sum(phase.values()), 1), 4) for k, v in phase.items()},
             "phase_kcycles_per_visit": {k: round(v / max(visits, 1) / 1000.0, 2) for k, v in phase.items()},
             "launch_ms": flood_launch_ms,
-            "traffic": K_RELAX_DRAM_BYTES_PER_VISIT * visits / args.steps,
+            "traffic": K_RELAX_DRAM_BYTES_PER_VISIT * (visits - empty) / args.steps,
             "traffic_source": "ncu DRAM bytes per brick visit (48-job capture) x visits of this launch"}
     line = {"metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,

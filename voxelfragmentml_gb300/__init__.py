@@ -240,8 +240,8 @@ class Context:
         _check(lib().vf_ctx_last_stats(self.h, C.byref(la), C.byref(ms), C.byref(by), C.byref(vis)))
         pa, sw, mh = C.c_uint64(), C.c_uint64(), C.c_uint64()
         _check(lib().vf_ctx_flood_stats(self.h, C.byref(pa), C.byref(sw), C.byref(mh)))
-        cn = (C.c_uint64 * 16)()
-        _check(lib().vf_ctx_flood_counters(self.h, cn, 16))
+        cn = (C.c_uint64 * 17)()
+        _check(lib().vf_ctx_flood_counters(self.h, cn, 17))
         return {"launches": la.value, "flood_ms": ms.value, "flood_bytes": by.value,
                 "flood_visits": vis.value, "flood_passes": pa.value, "flood_sweeps": sw.value,
                 "flood_maxit_hits": mh.value, "flood_active_row_sweeps": cn[6],
@@ -249,6 +249,7 @@ class Context:
                 "flood_key_changes": cn[7],
                 # first out-of-range access the relaxation skipped (0: none)
                 "flood_anomaly": (cn[8], cn[9], cn[10]),
+                "flood_empty_visits": cn[16],
                 # SM cycles summed over the relaxation CTAs, per phase of their work
                 "flood_phase_cycles": {k: 256 * cn[11 + i] for i, k in enumerate(
                     ("claim", "staging", "sweeps", "writeback_enqueue", "pass_barrier"))}}

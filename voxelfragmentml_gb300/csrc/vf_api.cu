@@ -672,8 +672,8 @@ vf_status vf_ctx_last_graph(vf_ctx* ctx, int* replayed) {
 
 vf_status vf_ctx_flood_counters(vf_ctx* ctx, uint64_t* out, uint32_t n) {
   if (!ctx || (n && !out)) return fail(VF_ERR_INVALID, "NULL argument");
-  for (uint32_t i = 0; i < n && i < 16; ++i) out[i] = ctx->c.last_flood_counters[i];
-  for (uint32_t i = 16; i < n; ++i) out[i] = 0;
+  for (uint32_t i = 0; i < n && i < 17; ++i) out[i] = ctx->c.last_flood_counters[i];
+  for (uint32_t i = 17; i < n; ++i) out[i] = 0;
   return VF_OK;
 }
 
@@ -722,7 +722,8 @@ vf_status vf_ctx_last_stats(vf_ctx* ctx, uint64_t* launches, float* flood_ms, ui
   if (launches) *launches = ctx->c.last_launches;
   if (flood_ms) *flood_ms = ctx->c.last_flood_ms;
   // algorithmic bytes of a brick visit: every voxel's label read and written
-  if (flood_bytes) *flood_bytes = ctx->c.last_flood_visits * (uint64_t)VF_BRICK_VOXELS * 4u;
+  if (flood_bytes)  // visits that staged the brick (4 B per voxel, label read + write)
+    *flood_bytes = (ctx->c.last_flood_visits - ctx->c.last_flood_counters[16]) * (uint64_t)VF_BRICK_VOXELS * 4u;
   if (flood_visits) *flood_visits = ctx->c.last_flood_visits;
   return VF_OK;
 }

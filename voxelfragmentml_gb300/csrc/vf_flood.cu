@@ -32,6 +32,8 @@
 
 namespace {
 
+using vfk::FLOOD_FDIR;
+
 constexpr int KP = 36;                 // smem row pitch (u32): conflict-free 16 B loads
 constexpr int KNX = VF_BX + 2, KNY = VF_BY + 2;
 constexpr int KROWS = KNX * KNY;
@@ -52,10 +54,12 @@ struct FloodArgs {
   uint32_t* stats;   // [0] visits, [1] passes, [2] busy warp-sweeps, [3] timeout, [4] sweeps,
                      // [5] visits at the sweep cap, [6] active row-sweeps, [7] key changes,
                      // [8..10] first out-of-range access (code, two values),
-                     // [11..15] SM cycles / 256 per phase of the CTAs' work
+                     // [11..15] SM cycles / 256 per phase of the CTAs' work,
+                     // [16] visits that found nothing new and staged nothing
   uint32_t max_passes;
   int max_sweeps;    // sweeps per brick visit before the brick re-queues itself
   uint32_t* pass_sizes;  // bricks queued for each of the first 256 passes (or null)
+  uint32_t* fdir;        // [nbricks][FLOOD_FDIR] change record (read and cleared by each visit)
   uint32_t nbricks;      // bricks of the batch (queue entries and brick ids are below)
   uint32_t njobs;        // jobs of the batch
 };
@@ -156,7 +160,8 @@ __device__ __forceinline__ uint4 lds4(const uint32_t* p) {
 template <int CONN>
 __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, uint32_t b,
                             uint32_t pass, uint32_t* tile, uint32_t* live27, uint32_t* dirs,
-                            int* reenq, uint32_t* rfw, unsigned long long* ph) {
+                            int* reenq, uint32_t* rfw, uint32_t* fbits,
+                            unsigned long long* ph) {
   // ph (thread 0): SM cycles of [1] live map + staging, [2] sweeps, [3] write-back + enqueue
   long long c0 = 0;
   if (threadIdx.x == 0) c0 = clock64();
@@ -164,6 +169,17 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
   const int bz = lb % J.nbz, by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
   const int x0 = bx * VF_BX, y0 = by * VF_BY, z0 = bz * VF_BZ;
   const int t = threadIdx.x;
+  // What changed next to the brick since its last visit (read and cleared).
+  // A flag set after the keys it covers were written (writer: fence, then
+  // flag) makes the staging loads below see those keys (reader: flag, fence,
+  // barrier, loads); a flag this visit does not see stays for the next visit,
+  // which the same writer queued.
+  uint32_t fv = 0;
+  if (t < (int)FLOOD_FDIR) {
+    fv = atomicExch(&a.fdir[(size_t)b * FLOOD_FDIR + t], 0u);
+    fbits[t] = fv;
+    __threadfence();
+  }
   if (t < 27) {
     const int dx = t / 9 - 1, dy = (t / 3) % 3 - 1, dz = t % 3 - 1;
     const int nx = bx + dx, ny = by + dy, nz = bz + dz;
@@ -174,7 +190,10 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
   }
   __shared__ uint32_t scnt[3];
   if (t == 0) { *dirs = 0; *reenq = 0; scnt[0] = 0; scnt[1] = 0; scnt[2] = 0; }
-  __syncthreads();
+  if (!__syncthreads_or(fv != 0)) {  // nothing new around the brick
+    if (t == 0) atomicAdd(a.stats + 16, 1u);
+    return;
+  }
   // stage keys: rows [x0-1, x0+17) x [y0-1, y0+17), keys z0 .. z0+31 (8 chunks
   // of 4) and the halo keys z0-1, z0+32.  Each thread keeps SU 16-byte loads in
   // flight before it stores them.  Keys outside the grid or in a brick without
@@ -267,8 +286,30 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
   // when a neighbour row changed: its own changes are already final along z
   // (forward and backward pass) against the neighbour values it read.  Sweep
   // 0 runs every row (new halo data).
-  if (t < 8) rfw[t] = 0xFFFFFFFFu;
-  __syncthreads();
+  // Sweep 0 runs the rows that read a changed key: x/y face, edge and corner
+  // neighbours mark whole faces and edges, the z neighbours the changed rows
+  // (26: widened by one row in x and y); bit 13 marks every row.
+  bool act0;
+  {
+    const uint32_t d = fbits[0];
+    const uint32_t dxm = 2u | (tx == 0 ? 1u : 0u) | (tx == VF_BX - 1 ? 4u : 0u);
+    const uint32_t dym = 2u | (ty == 0 ? 1u : 0u) | (ty == VF_BY - 1 ? 4u : 0u);
+    uint32_t hit = 0;
+#pragma unroll
+    for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+      for (int dy = 0; dy < 3; ++dy)
+        if ((dxm >> dx) & (dym >> dy) & 1u) hit |= (d >> (dx * 9 + dy * 3)) & 7u;
+    const uint32_t zc = (((fbits[1 + (tx >> 1)] | fbits[9 + (tx >> 1)]) >> ((tx & 1) * 16)) & 0xFFFFu);
+    if (CONN == 26) {
+      const uint32_t zl = tx > 0 ? (((fbits[1 + ((tx - 1) >> 1)] | fbits[9 + ((tx - 1) >> 1)]) >> (((tx - 1) & 1) * 16)) & 0xFFFFu) : 0u;
+      const uint32_t zr = tx < VF_BX - 1 ? (((fbits[1 + ((tx + 1) >> 1)] | fbits[9 + ((tx + 1) >> 1)]) >> (((tx + 1) & 1) * 16)) & 0xFFFFu) : 0u;
+      hit |= (((zl | zc | zr) << 1) >> ty) & 7u;
+    } else {
+      hit |= (zc >> ty) & 1u;
+    }
+    act0 = hit != 0;
+  }
   int it = 0, cur = 0;
   for (; it < a.max_sweeps; ++it) {
     const uint32_t* pw = rfw + cur * 8;
@@ -276,7 +317,9 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     const uint32_t m1 = (pw[tx >> 1] >> ((tx & 1) * 16)) & 0xFFFFu;
     const uint32_t m2 = tx < VF_BX - 1 ? (pw[(tx + 1) >> 1] >> (((tx + 1) & 1) * 16)) & 0xFFFFu : 0u;
     bool active;
-    if (CONN == 26)
+    if (it == 0)
+      active = act0;
+    else if (CONN == 26)
       active = ((((m0 | m2) << 1) & (7u << ty)) | ((m1 << 1) & (5u << ty))) != 0;
     else
       active = ((((m0 | m2) >> ty) & 1u) | ((m1 << 1) & (5u << ty))) != 0;
@@ -411,6 +454,10 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     dm &= ~(1u << 13);  // self
     if (dm) atomicOr(dirs, dm);
   }
+  // rows whose bottom / top key layer changed (the z neighbours' halo keys)
+  const int lastz_all = min(VF_BZ, (int)J.Z - z0) - 1;
+  const unsigned zlo = __ballot_sync(0xFFFFFFFFu, (changed & 1u) != 0);
+  const unsigned zhi = __ballot_sync(0xFFFFFFFFu, lastz_all >= 0 && ((changed >> lastz_all) & 1u));
   // statistics: active row-sweeps and key changes (block sums in shared memory)
   if (nact) atomicAdd(&scnt[0], nact);
   if (nchg) atomicAdd(&scnt[1], nchg);
@@ -426,6 +473,20 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     atomicAdd(a.stats + 7, scnt[1]);
     atomicAdd(a.stats + 2, scnt[2]);
   }
+  // change records of the neighbours, after the key writes above (fence), then
+  // the neighbours go on the next pass's queue
+  if (t < 32 || (t & 31) == 0) __threadfence();
+  if ((t & 31) == 0) {
+    const int w = t >> 5;
+    if (zlo && live27[1 * 9 + 1 * 3 + 0]) {  // below: its keys at z0'+32 are our bottom layer
+      const uint32_t nb = brick_id(J, bx, by, bz - 1);
+      if (nb < a.nbricks) atomicOr(&a.fdir[(size_t)nb * FLOOD_FDIR + 9 + w], zlo);
+    }
+    if (zhi && live27[1 * 9 + 1 * 3 + 2]) {  // above: its keys at z0'-1 are our top layer
+      const uint32_t nb = brick_id(J, bx, by, bz + 1);
+      if (nb < a.nbricks) atomicOr(&a.fdir[(size_t)nb * FLOOD_FDIR + 1 + w], zhi);
+    }
+  }
   if (t < 32) {
     const uint32_t dm = *dirs;
     bool want = false;
@@ -433,14 +494,27 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     if (t < 27 && ((dm >> t) & 1u) && live27[t]) {
       want = true;
       nb = brick_id(J, bx + t / 9 - 1, by + (t / 3) % 3 - 1, bz + t % 3 - 1);
+      // seen from nb this brick is in direction 26 - t; z faces use the row masks
+      if (t != 1 * 9 + 1 * 3 + 0 && t != 1 * 9 + 1 * 3 + 2 && nb < a.nbricks)
+        atomicOr(&a.fdir[(size_t)nb * FLOOD_FDIR], 1u << (26 - t));
     }
-    if (t == 27 && *reenq) { want = true; nb = b; }
+    if (t == 27 && *reenq) {  // sweep cap: the brick comes back with every row
+      want = true;
+      nb = b;
+      atomicOr(&a.fdir[(size_t)b * FLOOD_FDIR], 1u << 13);
+    }
     enqueue(a, nb, pass + 1, want);
   }
   if (t == 0) ph[3] += clock64() - c2;
 }
 
-__global__ void __launch_bounds__(256, 4) k_relax(FloodArgs a) {
+__global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
+  // The arguments are read from a shared copy: the kernel and the functions
+  // it calls take them by reference, and a shared-memory struct is an
+  // ordinary addressable object (no address of the parameter space is taken).
+  __shared__ FloodArgs a;
+  if (threadIdx.x == 0) a = args;
+  __syncthreads();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t* tile = reinterpret_cast<uint32_t*>(smem_raw);
   __shared__ uint32_t live27[27];
@@ -448,6 +522,7 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs a) {
   __shared__ int reenq;
   __shared__ uint32_t item;
   __shared__ uint32_t rfw[16];
+  __shared__ uint32_t fbits[FLOOD_FDIR];
   __shared__ unsigned long long ph[5];  // thread 0: SM cycles per phase (see flush below)
   if (threadIdx.x < 5) ph[threadIdx.x] = 0;
   for (uint32_t p = 0; p < a.max_passes; ++p) {
@@ -482,8 +557,8 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs a) {
       const JobDesc& J = a.jobs[jid];
       const int conn6 = J.distance == 1;
       if (threadIdx.x == 0) ph[0] += clock64() - c_claim;
-      if (conn6) relax_brick<6>(a, J, jid, b, p, tile, live27, &dirs, &reenq, rfw, ph);
-      else relax_brick<26>(a, J, jid, b, p, tile, live27, &dirs, &reenq, rfw, ph);
+      if (conn6) relax_brick<6>(a, J, jid, b, p, tile, live27, &dirs, &reenq, rfw, fbits, ph);
+      else relax_brick<26>(a, J, jid, b, p, tile, live27, &dirs, &reenq, rfw, fbits, ph);
       if (threadIdx.x == 0) atomicMax(&a.st[jid].passes, p + 1);
       ++visits;
     }
@@ -575,7 +650,7 @@ __global__ void k_seed_bricks(const JobDesc* jobs, JobState* st, int njobs, uint
 // seeds into the keys (later seeds win a shared voxel, as grid.set in list
 // order does, FloodFracturer.cpp:101-103) and their bricks onto queue 0
 __global__ void k_seed_keys(const JobDesc* jobs, JobState* st, int njobs, uint32_t* epoch,
-                            uint32_t* queue0, uint32_t* qcount) {
+                            uint32_t* queue0, uint32_t* qcount, uint32_t* fdir) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= njobs) return;
   const JobDesc& J = jobs[j];
@@ -587,6 +662,7 @@ __global__ void k_seed_keys(const JobDesc* jobs, JobState* st, int njobs, uint32
     const uint32_t x = J.seeds[4 * i], y = J.seeds[4 * i + 1], z = J.seeds[4 * i + 2];
     J.keys[vf_kidx(J, x, y, z)] = ~i;
     const uint32_t b = J.brick_base + ((x / VF_BX) * J.nby + y / VF_BY) * J.nbz + z / VF_BZ;
+    atomicOr(&fdir[(size_t)b * FLOOD_FDIR], 1u << 13);  // first visit: every row
     if (atomicMax(&epoch[b], 1u) < 1u) queue0[atomicAdd(qcount, 1u)] = b;
   }
 }
@@ -760,12 +836,14 @@ __global__ void __launch_bounds__(256) k_disjoint_reset(const JobDesc* jobs, Job
 
 __global__ void k_enqueue_pass2(const JobDesc* jobs, const JobState* st, const uint32_t* list,
                                 const uint32_t* count, const uint32_t* brick_job,
-                                uint32_t* epoch, uint32_t* queue0, uint32_t* qcount) {
+                                uint32_t* epoch, uint32_t* queue0, uint32_t* qcount,
+                                uint32_t* fdir) {
   const uint32_t n = *count;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const uint32_t b = list[i];
     const uint32_t j = brick_job[b];
     if (!jobs[j].active || !st[j].has_prefix || !st[j].disjoint) continue;
+    fdir[(size_t)b * FLOOD_FDIR] = 1u << 13;  // keys were reset: every row
     if (atomicMax(&epoch[b], 1u) < 1u) queue0[atomicAdd(qcount, 1u)] = b;
   }
 }
@@ -796,8 +874,10 @@ void flood_seed(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs,
   cudaMemsetAsync(fs.qcount, 0, sizeof(uint32_t) * 3, st);
   cudaMemsetAsync(fs.qhead, 0, sizeof(uint32_t) * 3, st);
   cudaMemsetAsync(fs.barrier, 0, sizeof(uint32_t) * 2, st);
+  cudaMemsetAsync(fs.fdir, 0, sizeof(uint32_t) * FLOOD_FDIR * fs.total_bricks, st);
   if (njobs > 0)
-    k_seed_keys<<<(njobs + 127) / 128, 128, 0, st>>>(dj, ds, njobs, fs.epoch, fs.queue[0], fs.qcount);
+    k_seed_keys<<<(njobs + 127) / 128, 128, 0, st>>>(dj, ds, njobs, fs.epoch, fs.queue[0], fs.qcount,
+                                                      fs.fdir);
 }
 
 static int relax_blocks(int num_sms) {
@@ -833,6 +913,7 @@ cudaError_t flood_relax(cudaStream_t st, const JobDesc* dj, JobState* ds,
   a.max_passes = fs.max_passes;
   a.max_sweeps = (fs.max_sweeps > 0 && fs.max_sweeps <= MAXIT) ? fs.max_sweeps : MAXIT;
   a.pass_sizes = fs.pass_sizes;
+  a.fdir = fs.fdir;
   a.nbricks = fs.total_bricks;
   a.njobs = fs.njobs;
   int blocks = relax_blocks(num_sms);
@@ -865,8 +946,9 @@ void flood_disjoint(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs,
   cudaMemsetAsync(fs.qcount, 0, sizeof(uint32_t) * 3, st);
   cudaMemsetAsync(fs.qhead, 0, sizeof(uint32_t) * 3, st);
   cudaMemsetAsync(fs.barrier, 0, sizeof(uint32_t) * 2, st);
+  cudaMemsetAsync(fs.fdir, 0, sizeof(uint32_t) * FLOOD_FDIR * fs.total_bricks, st);
   k_enqueue_pass2<<<brick_grid((max_count + 255) / 256), 256, 0, st>>>(
-      dj, ds, list, count, brick_job, fs.epoch, fs.queue[0], fs.qcount);
+      dj, ds, list, count, brick_job, fs.epoch, fs.queue[0], fs.qcount, fs.fdir);
 }
 
 }  // namespace vfk

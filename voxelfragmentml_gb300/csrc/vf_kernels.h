@@ -79,11 +79,18 @@ void count_values(cudaStream_t st, const JobDesc* dj, JobState* ds, const uint32
                   const uint32_t* count, uint32_t max_count, const uint32_t* brick_job);
 
 // ---- flood (vf_flood.cu) ----
+// Words per brick of the flood's change record: [0] neighbour directions
+// (bit dx*9 + dy*3 + dz: the brick at offset (dx-1, dy-1, dz-1) changed keys
+// this brick reads; bit 13: every row), [1..8] rows whose key at z0-1 changed,
+// [9..16] rows whose key at z0+32 changed (bit t & 31 of word t >> 5, row
+// t = x * 16 + y within the brick).
+constexpr uint32_t FLOOD_FDIR = 17;
 struct FloodScratch {
   uint32_t* queue[3];    // brick ids, capacity total_bricks each (rotating)
   uint32_t* qcount;      // [3]
   uint32_t* qhead;       // [3]
   uint32_t* epoch;       // [total_bricks]
+  uint32_t* fdir;        // [total_bricks][FLOOD_FDIR] change record, zero between floods
   uint32_t* barrier;     // [2] count, generation
   uint32_t* err;         // [1] global error word
   uint32_t* stats;       // [4] brick visits, passes, overflow, timeout

@@ -90,6 +90,7 @@ extern "C" vf_status vf_flood_noalloc(const uint16_t* d_grid, uint16_t* d_labels
   const size_t o_q1 = off; off += up(nb * 4);
   const size_t o_q2 = off; off += up(nb * 4);
   const size_t o_epoch = off; off += up(nb * 4);
+  const size_t o_fdir = off; off += up(nb * 4 * vfk::FLOOD_FDIR);
   const size_t o_grid = off; off += up((size_t)X * Y * Zp * 2);
   const size_t o_keys = off; off += up((size_t)X * Y * Zk * 4);
   if (off > VF_NOALLOC_SCRATCH_BYTES)
@@ -151,6 +152,7 @@ extern "C" vf_status vf_flood_noalloc(const uint16_t* d_grid, uint16_t* d_labels
   fs.err = scal + 12;
   fs.stats = scal + 16;
   fs.epoch = reinterpret_cast<uint32_t*>(S + o_epoch);
+  fs.fdir = reinterpret_cast<uint32_t*>(S + o_fdir);
   fs.max_passes = 1u << 20;
   fs.total_bricks = (uint32_t)nb;
   fs.njobs = 1;

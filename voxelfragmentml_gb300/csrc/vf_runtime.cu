@@ -135,7 +135,7 @@ void Batch::release() {
   if (!ctx) return;
   for (DevBuf* b : {&grid0, &grid1, &keys, &par, &tets, &range, &ys, &seeds, &counts, &lat,
                     &verts, &faces, &emask, &etab, &tables, &state, &brick_job, &live, &list, &lcount,
-                    &q[0], &q[1], &q[2], &scal, &epoch, &front[0], &front[1], &pcnt, &pbase,
+                    &q[0], &q[1], &q[2], &scal, &epoch, &fdir, &front[0], &front[1], &pcnt, &pbase,
                     &psums, &srec, &rle_cnt, &rle_base, &rle_sums, &rle_tot, &rle_starts,
                     &rle_rec})
     ctx->free_buf(*b);
@@ -264,6 +264,9 @@ size_t job_footprint(const vf_job& j) {
   size_t b = X * Y * Zp * 2 * 2 + X * Y * Zw * 4 * 2 + (size_t)j.nfaces * (48 + 4 + 12) +
              (size_t)edge_slots(j.nfaces) * 8 + (size_t)j.nverts * 12 + 65536;
   if (j.params.algorithm == VF_FLOOD) b += X * Y * Zk * 4;
+  // per brick: owner, live flag, list, 3 queues, epoch, change record
+  b += ((X + VF_BX - 1) / VF_BX) * ((Y + VF_BY - 1) / VF_BY) * ((Z + VF_BZ - 1) / VF_BZ) *
+       (4 + 1 + 4 + 12 + 4 + 4 * vfk::FLOOD_FDIR);
   return b;
 }
 
@@ -365,6 +368,7 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
   ALLOC(lcount, 256);
   for (int i = 0; i < 3; ++i) ALLOC(q[i], nb * 4);
   ALLOC(epoch, nb * 4);
+  ALLOC(fdir, nb * vfk::FLOOD_FDIR * 4);
   ALLOC(scal, 4096);
   const size_t nf = std::max<uint32_t>(sz.faces_total, 1);
   ALLOC(pcnt, nf * 4);
@@ -592,11 +596,13 @@ static vfk::FloodScratch flood_scratch(Batch& B) {
   fs.qhead = sc + 4;     // [3]
   fs.barrier = sc + 8;   // [2]
   fs.err = sc + 12;      // [1]
-  fs.stats = sc + 16;    // [16]: visits, passes, busy warp-sweeps, timeouts, sweeps,
+  fs.stats = sc + 16;    // [17]: visits, passes, busy warp-sweeps, timeouts, sweeps,
                          // sweep-cap hits, active row-sweeps, changed voxels, the
-                         // first out-of-range access (code, two values) and the
-                         // SM cycles / 256 of five phases of the relaxation CTAs
+                         // first out-of-range access (code, two values), the SM
+                         // cycles / 256 of five phases of the relaxation CTAs and
+                         // the visits that found nothing new
   fs.epoch = static_cast<uint32_t*>(B.epoch.p);
+  fs.fdir = static_cast<uint32_t*>(B.fdir.p);
   fs.max_passes = 1u << 20;
   fs.total_bricks = B.sz.bricks;
   fs.njobs = (uint32_t)B.jobs.size();
@@ -788,10 +794,10 @@ vf_status Batch::finish(vf_job_result* res) {
     ctx->last_flood_passes = h_scal[17];
     ctx->last_flood_sweeps = h_scal[20];
     ctx->last_flood_maxit = h_scal[21];
-    for (int i = 0; i < 16; ++i) ctx->last_flood_counters[i] = h_scal[16 + i];
+    for (int i = 0; i < 17; ++i) ctx->last_flood_counters[i] = h_scal[16 + i];
     for (int i = 0; i < 256; ++i) ctx->last_pass_sizes[i] = h_scal[128 + i];
   } else {
-    for (int i = 0; i < 16; ++i) ctx->last_flood_counters[i] = 0;
+    for (int i = 0; i < 17; ++i) ctx->last_flood_counters[i] = 0;
     ctx->last_flood_ms = 0.f;
     ctx->last_flood_visits = 0;
     ctx->last_flood_passes = 0;
@@ -835,7 +841,7 @@ vf_status Batch::enqueue_plain_and_wait(vf_job_result* res, bool skip_vox) {
     if ((s = ctx->alloc(front[1], (N + VF_MAX_SEEDS) * 4 + 256))) return s;
     uint32_t* f0 = static_cast<uint32_t*>(front[0].p);
     uint32_t* f1 = static_cast<uint32_t*>(front[1].p);
-    uint32_t* cnt = static_cast<uint32_t*>(scal.p) + 32;
+    uint32_t* cnt = static_cast<uint32_t*>(scal.p) + 48;  // after the flood counters (16 .. 32)
     const JobDesc* tf = dtable(T_FLOOD);
     vfk::plain_init_keys(st, tf, hj);
     vfk::plain_seed(st, tf, ds, f0, cnt);

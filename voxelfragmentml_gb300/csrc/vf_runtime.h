@@ -60,7 +60,7 @@ struct Batch {
   DevBuf grid0, grid1, keys, par, tets, range, ys, seeds, counts, lat, verts, faces, emask;
   DevBuf etab;  // mesh edge parity tables (voxelizer)
   DevBuf rle_cnt, rle_base, rle_sums, rle_tot, rle_starts, rle_rec;  // RLE export scratch
-  DevBuf tables, state, brick_job, live, list, lcount, q[3], scal, epoch, front[2];
+  DevBuf tables, state, brick_job, live, list, lcount, q[3], scal, epoch, fdir, front[2];
   DevBuf pcnt, pbase, psums, srec;  // flattened per-face work lists, shell setup
   void* h_tables = nullptr;  // pinned staging
   size_t h_tables_cap = 0;
@@ -136,7 +136,7 @@ struct Ctx {
   uint64_t last_flood_visits = 0;
   uint64_t last_flood_passes = 0;
   uint64_t last_flood_sweeps = 0;
-  uint64_t last_flood_counters[16] = {};  // raw flood counters of the last batched run
+  uint64_t last_flood_counters[17] = {};  // raw flood counters of the last batched run
   uint32_t last_pass_sizes[256] = {};    // bricks queued per flood pass (first 256)
   uint64_t last_flood_maxit = 0;
   vf_status alloc(DevBuf& b, size_t bytes);
