@@ -142,13 +142,16 @@ __device__ __forceinline__ void enqueue(const FloodArgs& a, uint32_t b, uint32_t
 __device__ __forceinline__ uint32_t step_from(uint32_t m) {
   return m >= 2u * VF_KEY_STEP ? m - VF_KEY_STEP : 0u;
 }
-// an unreached voxel next to a key one step from the distance limit
-__device__ __forceinline__ bool at_limit(uint32_t kk, uint32_t m) {
-  return kk == VF_KEY_UNREACHED && m >= VF_KEY_MIN_REACHED && m < 2u * VF_KEY_STEP;
-}
-__device__ __forceinline__ uint32_t relax1(uint32_t kk, uint32_t m, uint32_t& overflow) {
-  if (at_limit(kk, m)) overflow = 1;
+// key of a voxel (kk) relaxed by the best neighbour key m; EMPTY stays EMPTY.
+// step_from is monotone, so relaxing by max(m1, m2) equals relaxing by m1
+// and then by m2.
+__device__ __forceinline__ uint32_t relax(uint32_t kk, uint32_t m) {
   return kk ? max(kk, step_from(m)) : 0u;
+}
+// a key at the largest distance the key format holds (its neighbours would
+// overflow the distance field)
+__device__ __forceinline__ bool at_limit(uint32_t m) {
+  return m - VF_KEY_MIN_REACHED < VF_KEY_STEP;
 }
 __device__ __forceinline__ uint4 max4(uint4 a, uint4 b) {
   return make_uint4(max(a.x, b.x), max(a.y, b.y), max(a.z, b.z), max(a.w, b.w));
@@ -350,8 +353,7 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
           uint32_t f[4];
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
-            const uint32_t k1 = relax1(kk[j], w[j], overflow);
-            f[j] = relax1(k1, prev, overflow);
+            f[j] = relax(kk[j], max(w[j], prev));
             prev = f[j];
             if (f[j] != kk[j]) chg |= 1u << (4 * q + j);
           }
@@ -370,8 +372,7 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
           uint32_t f[4];
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
-            const uint32_t k1 = relax1(kk[j], w[j], overflow);
-            f[j] = relax1(k1, prev, overflow);
+            f[j] = relax(kk[j], max(w[j], prev));
             prev = f[j];
             if (f[j] != kk[j]) chg |= 1u << (4 * q + j);
           }
@@ -389,7 +390,7 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
         uint32_t cq = 0;
 #pragma unroll
         for (int j = 3; j >= 0; --j) {
-          f[j] = relax1(kk[j], prev, overflow);
+          f[j] = relax(kk[j], prev);
           prev = f[j];
           if (f[j] != kk[j]) cq |= 1u << j;
         }
@@ -407,6 +408,47 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     nwarp += __any_sync(0xFFFFFFFFu, active) ? 1u : 0u;  // warps with work in this sweep
     nchg += __popc(chg);
     if (!__syncthreads_or(chg != 0)) break;
+  }
+  // Distance limit: an unreached voxel next to a key at the largest distance
+  // the key format holds.  Checked on the converged tile, and only when some
+  // key of the tile (row or halo) is at that distance.
+  {
+    bool lim = false;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const uint4 v = lds4(own_row + 4 + 4 * q);
+      lim |= at_limit(v.x) | at_limit(v.y) | at_limit(v.z) | at_limit(v.w);
+    }
+    lim |= at_limit(own_row[0]) | at_limit(own_row[3]);
+    if (t < 2 * KNY + 2 * VF_BX) {  // the 68 halo rows of the 18 x 18 tile
+      const int lx = t < KNY ? 0 : t < 2 * KNY ? KNX - 1 : 1 + (t - 2 * KNY) % VF_BX;
+      const int ly = t < KNY ? t : t < 2 * KNY ? t - KNY : (t < 2 * KNY + VF_BX ? 0 : KNY - 1);
+      const uint32_t* hr = tile + (lx * KNY + ly) * KP;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const uint4 v = lds4(hr + 4 + 4 * q);
+        lim |= at_limit(v.x) | at_limit(v.y) | at_limit(v.z) | at_limit(v.w);
+      }
+      lim |= at_limit(hr[0]) | at_limit(hr[3]);
+    }
+    if (__syncthreads_or(lim)) {
+      // key at z (-1 .. 32) of a row: [3] z0-1, [4 + z], [0] z0+32
+      auto at = [](const uint32_t* r, int z) { return r[z < 0 ? 3 : (z >= VF_BZ ? 0 : 4 + z)]; };
+      for (int z = 0; z < VF_BZ; ++z) {
+        if (own_row[4 + z] != VF_KEY_UNREACHED) continue;
+        uint32_t m = max(at(own_row, z - 1), at(own_row, z + 1));
+        if (CONN == 26) {
+          for (int r = 0; r < 9; ++r) {
+            const uint32_t* rp = own_row + ((r / 3 - 1) * KNY + (r % 3 - 1)) * KP;
+            m = max(m, max(at(rp, z - 1), max(at(rp, z), at(rp, z + 1))));
+          }
+        } else {
+          m = max(m, max(max(own_row[-KNY * KP + 4 + z], own_row[KNY * KP + 4 + z]),
+                         max(own_row[-KP + 4 + z], own_row[KP + 4 + z])));
+        }
+        if (at_limit(m)) overflow = 1;
+      }
+    }
   }
   long long c2 = 0;
   if (t == 0) { c2 = clock64(); ph[2] += c2 - c1; }
