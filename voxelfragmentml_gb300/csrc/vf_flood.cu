@@ -160,10 +160,101 @@ __device__ __forceinline__ uint4 lds4(const uint32_t* p) {
   return *reinterpret_cast<const uint4*>(p);
 }
 
+// Shared state of the sweeps of one brick visit.
+struct SweepShared {
+  uint32_t rfw[16];      // [2][8] rows that changed in the previous sweep (bit per row)
+  uint32_t wcnt[8];      // active rows per warp in this sweep
+  uint32_t hl[256];      // per row: z halo candidate below the brick (z0-1)
+  uint32_t hh[256];      //          z halo candidate above the brick (z0+32)
+  uint32_t rowchg[256];  // per row: z positions changed during the visit
+  uint16_t rlist[256];   // rows to run in this sweep
+};
+
+// Relaxes one row of the staged tile (own_row) in place: the forward pass
+// (cross-row candidates fused with the increasing-z pass) and the backward
+// pass, both starting from the row's z halo candidates hlo / hhi.  Returns the
+// z positions whose key changed.
+template <int CONN>
+__device__ __forceinline__ uint32_t relax_row(uint32_t* own_row, uint32_t hlo, uint32_t hhi) {
+  uint32_t chg = 0;
+  // forward: cross-row candidates fused with the increasing-z pass
+  uint32_t prev = hlo;
+  if (CONN == 26) {
+    uint4 C = make_uint4(0, 0, 0, 0);
+#pragma unroll
+    for (int r = 0; r < 9; ++r)
+      C = max4(C, lds4(own_row + ((r / 3 - 1) * KNY + (r % 3 - 1)) * KP + 4));
+    uint4 kv = lds4(own_row + 4);
+    uint32_t cp = hlo;  // window maximum at z-1 of the chunk
+#pragma unroll 1
+    for (int q = 0; q < 8; ++q) {
+      uint4 Cn = make_uint4(hhi, 0, 0, 0), kn = make_uint4(0, 0, 0, 0);
+      if (q + 1 < 8) {
+        Cn = make_uint4(0, 0, 0, 0);
+#pragma unroll
+        for (int r = 0; r < 9; ++r)
+          Cn = max4(Cn, lds4(own_row + ((r / 3 - 1) * KNY + (r % 3 - 1)) * KP + 8 + 4 * q));
+        kn = lds4(own_row + 8 + 4 * q);
+      }
+      const uint32_t w[4] = {max(cp, max(C.x, C.y)), max(C.x, max(C.y, C.z)),
+                             max(C.y, max(C.z, C.w)), max(C.z, max(C.w, Cn.x))};
+      const uint32_t kk[4] = {kv.x, kv.y, kv.z, kv.w};
+      uint32_t f[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        f[j] = relax(kk[j], max(w[j], prev));
+        prev = f[j];
+        if (f[j] != kk[j]) chg |= 1u << (4 * q + j);
+      }
+      if ((chg >> (4 * q)) & 0xFu)
+        *reinterpret_cast<uint4*>(own_row + 4 + 4 * q) = make_uint4(f[0], f[1], f[2], f[3]);
+      cp = C.w; C = Cn; kv = kn;
+    }
+  } else {
+#pragma unroll 1
+    for (int q = 0; q < 8; ++q) {
+      const uint4 M = max4(max4(lds4(own_row - KNY * KP + 4 + 4 * q), lds4(own_row + KNY * KP + 4 + 4 * q)),
+                           max4(lds4(own_row - KP + 4 + 4 * q), lds4(own_row + KP + 4 + 4 * q)));
+      const uint4 kv = lds4(own_row + 4 + 4 * q);
+      const uint32_t w[4] = {M.x, M.y, M.z, M.w};
+      const uint32_t kk[4] = {kv.x, kv.y, kv.z, kv.w};
+      uint32_t f[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        f[j] = relax(kk[j], max(w[j], prev));
+        prev = f[j];
+        if (f[j] != kk[j]) chg |= 1u << (4 * q + j);
+      }
+      if ((chg >> (4 * q)) & 0xFu)
+        *reinterpret_cast<uint4*>(own_row + 4 + 4 * q) = make_uint4(f[0], f[1], f[2], f[3]);
+    }
+  }
+  // backward in-row pass
+  prev = hhi;
+#pragma unroll 1
+  for (int q = 7; q >= 0; --q) {
+    const uint4 kv = lds4(own_row + 4 + 4 * q);
+    const uint32_t kk[4] = {kv.x, kv.y, kv.z, kv.w};
+    uint32_t f[4];
+    uint32_t cq = 0;
+#pragma unroll
+    for (int j = 3; j >= 0; --j) {
+      f[j] = relax(kk[j], prev);
+      prev = f[j];
+      if (f[j] != kk[j]) cq |= 1u << j;
+    }
+    if (cq) {
+      *reinterpret_cast<uint4*>(own_row + 4 + 4 * q) = make_uint4(f[0], f[1], f[2], f[3]);
+      chg |= cq << (4 * q);
+    }
+  }
+  return chg;
+}
+
 template <int CONN>
 __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, uint32_t b,
                             uint32_t pass, uint32_t* tile, uint32_t* live27, uint32_t* dirs,
-                            int* reenq, uint32_t* rfw, uint32_t* fbits,
+                            int* reenq, SweepShared& sw, uint32_t* fbits,
                             unsigned long long* ph) {
   // ph (thread 0): SM cycles of [1] live map + staging, [2] sweeps, [3] write-back + enqueue
   long long c0 = 0;
@@ -283,12 +374,10 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     hlo = own_row[3];
     hhi = own_row[0];
   }
-  uint32_t changed = 0, overflow = 0, nact = 0, nchg = 0, nwarp = 0;
-  // rfw[s][w]: ballot of warp w over "my row changed in sweep s-1" (bit
-  // t & 31; warp w holds x-rows 2w and 2w+1, 16 y-rows each).  A row runs
-  // when a neighbour row changed: its own changes are already final along z
-  // (forward and backward pass) against the neighbour values it read.  Sweep
-  // 0 runs every row (new halo data).
+  uint32_t overflow = 0, nact = 0, nchg = 0, nwarp = 0;
+  sw.hl[t] = hlo;
+  sw.hh[t] = hhi;
+  sw.rowchg[t] = 0;
   // Sweep 0 runs the rows that read a changed key: x/y face, edge and corner
   // neighbours mark whole faces and edges, the z neighbours the changed rows
   // (26: widened by one row in x and y); bit 13 marks every row.
@@ -313,102 +402,58 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     }
     act0 = hit != 0;
   }
+  // Sweeps.  The rows to run are compacted onto the lowest threads (one list
+  // per sweep), so a sweep with n active rows keeps ceil(n / 32) warps busy.
+  // A row runs when a neighbour row changed in the previous sweep (its own
+  // changes are already final along z against the neighbour values it read);
+  // sweep 0 runs the rows next to new halo data (act0).  sw.rfw[s & 1] holds
+  // the rows that changed in sweep s - 1 (bit row & 31 of word row >> 5, row
+  // t = x * 16 + y, so word w holds x-rows 2w and 2w + 1).
+  const int lane = t & 31, wid = t >> 5;
   int it = 0, cur = 0;
   for (; it < a.max_sweeps; ++it) {
-    const uint32_t* pw = rfw + cur * 8;
-    const uint32_t m0 = tx > 0 ? (pw[(tx - 1) >> 1] >> (((tx - 1) & 1) * 16)) & 0xFFFFu : 0u;
-    const uint32_t m1 = (pw[tx >> 1] >> ((tx & 1) * 16)) & 0xFFFFu;
-    const uint32_t m2 = tx < VF_BX - 1 ? (pw[(tx + 1) >> 1] >> (((tx + 1) & 1) * 16)) & 0xFFFFu : 0u;
+    const uint32_t* pw = sw.rfw + cur * 8;
     bool active;
-    if (it == 0)
+    if (it == 0) {
       active = act0;
-    else if (CONN == 26)
-      active = ((((m0 | m2) << 1) & (7u << ty)) | ((m1 << 1) & (5u << ty))) != 0;
-    else
-      active = ((((m0 | m2) >> ty) & 1u) | ((m1 << 1) & (5u << ty))) != 0;
+    } else {
+      const uint32_t m0 = tx > 0 ? (pw[(tx - 1) >> 1] >> (((tx - 1) & 1) * 16)) & 0xFFFFu : 0u;
+      const uint32_t m1 = (pw[tx >> 1] >> ((tx & 1) * 16)) & 0xFFFFu;
+      const uint32_t m2 = tx < VF_BX - 1 ? (pw[(tx + 1) >> 1] >> (((tx + 1) & 1) * 16)) & 0xFFFFu : 0u;
+      if (CONN == 26)
+        active = ((((m0 | m2) << 1) & (7u << ty)) | ((m1 << 1) & (5u << ty))) != 0;
+      else
+        active = ((((m0 | m2) >> ty) & 1u) | ((m1 << 1) & (5u << ty))) != 0;
+    }
+    const unsigned bal = __ballot_sync(0xFFFFFFFFu, active);
+    if (lane == 0) sw.wcnt[wid] = (uint32_t)__popc(bal);
+    if (t < 8) sw.rfw[(cur ^ 1) * 8 + t] = 0u;  // filled by this sweep's changes
+    __syncthreads();
+    uint32_t base = 0, n = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const uint32_t c = sw.wcnt[i];
+      base += i < wid ? c : 0u;
+      n += c;
+    }
+    if (active) sw.rlist[base + __popc(bal & ((1u << lane) - 1u))] = (uint16_t)t;
+    __syncthreads();
     uint32_t chg = 0;
-    if (active) {
-      // forward: cross-row candidates fused with the increasing-z pass
-      uint32_t prev = hlo;
-      if (CONN == 26) {
-        uint4 C = make_uint4(0, 0, 0, 0);
-#pragma unroll
-        for (int r = 0; r < 9; ++r)
-          C = max4(C, lds4(own_row + ((r / 3 - 1) * KNY + (r % 3 - 1)) * KP + 4));
-        uint4 kv = lds4(own_row + 4);
-        uint32_t cp = hlo;  // window maximum at z-1 of the chunk
-#pragma unroll 1
-        for (int q = 0; q < 8; ++q) {
-          uint4 Cn = make_uint4(hhi, 0, 0, 0), kn = make_uint4(0, 0, 0, 0);
-          if (q + 1 < 8) {
-            Cn = make_uint4(0, 0, 0, 0);
-#pragma unroll
-            for (int r = 0; r < 9; ++r)
-              Cn = max4(Cn, lds4(own_row + ((r / 3 - 1) * KNY + (r % 3 - 1)) * KP + 8 + 4 * q));
-            kn = lds4(own_row + 8 + 4 * q);
-          }
-          const uint32_t w[4] = {max(cp, max(C.x, C.y)), max(C.x, max(C.y, C.z)),
-                                 max(C.y, max(C.z, C.w)), max(C.z, max(C.w, Cn.x))};
-          const uint32_t kk[4] = {kv.x, kv.y, kv.z, kv.w};
-          uint32_t f[4];
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            f[j] = relax(kk[j], max(w[j], prev));
-            prev = f[j];
-            if (f[j] != kk[j]) chg |= 1u << (4 * q + j);
-          }
-          if ((chg >> (4 * q)) & 0xFu)
-            *reinterpret_cast<uint4*>(own_row + 4 + 4 * q) = make_uint4(f[0], f[1], f[2], f[3]);
-          cp = C.w; C = Cn; kv = kn;
-        }
-      } else {
-#pragma unroll 1
-        for (int q = 0; q < 8; ++q) {
-          const uint4 M = max4(max4(lds4(own_row - KNY * KP + 4 + 4 * q), lds4(own_row + KNY * KP + 4 + 4 * q)),
-                               max4(lds4(own_row - KP + 4 + 4 * q), lds4(own_row + KP + 4 + 4 * q)));
-          const uint4 kv = lds4(own_row + 4 + 4 * q);
-          const uint32_t w[4] = {M.x, M.y, M.z, M.w};
-          const uint32_t kk[4] = {kv.x, kv.y, kv.z, kv.w};
-          uint32_t f[4];
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            f[j] = relax(kk[j], max(w[j], prev));
-            prev = f[j];
-            if (f[j] != kk[j]) chg |= 1u << (4 * q + j);
-          }
-          if ((chg >> (4 * q)) & 0xFu)
-            *reinterpret_cast<uint4*>(own_row + 4 + 4 * q) = make_uint4(f[0], f[1], f[2], f[3]);
-        }
-      }
-      // backward in-row pass
-      prev = hhi;
-#pragma unroll 1
-      for (int q = 7; q >= 0; --q) {
-        const uint4 kv = lds4(own_row + 4 + 4 * q);
-        const uint32_t kk[4] = {kv.x, kv.y, kv.z, kv.w};
-        uint32_t f[4];
-        uint32_t cq = 0;
-#pragma unroll
-        for (int j = 3; j >= 0; --j) {
-          f[j] = relax(kk[j], prev);
-          prev = f[j];
-          if (f[j] != kk[j]) cq |= 1u << j;
-        }
-        if (cq) {
-          *reinterpret_cast<uint4*>(own_row + 4 + 4 * q) = make_uint4(f[0], f[1], f[2], f[3]);
-          chg |= cq << (4 * q);
-        }
+    if (t < (int)n) {
+      const int row = sw.rlist[t];
+      uint32_t* rr = tile + (((row >> 4) + 1) * KNY + ((row & 15) + 1)) * KP;
+      chg = relax_row<CONN>(rr, sw.hl[row], sw.hh[row]);
+      if (chg) {
+        atomicOr(&sw.rfw[(cur ^ 1) * 8 + (row >> 5)], 1u << (row & 31));
+        sw.rowchg[row] |= chg;
       }
     }
-    const unsigned bal = __ballot_sync(0xFFFFFFFFu, chg != 0);
-    if ((t & 31) == 0) rfw[(cur ^ 1) * 8 + (t >> 5)] = bal;
-    changed |= chg;
     cur ^= 1;
-    if (active) ++nact;
-    nwarp += __any_sync(0xFFFFFFFFu, active) ? 1u : 0u;  // warps with work in this sweep
+    if (t == 0) { nact += n; nwarp += (n + 31) / 32; }
     nchg += __popc(chg);
     if (!__syncthreads_or(chg != 0)) break;
   }
+  const uint32_t changed = sw.rowchg[t];
   // Distance limit: an unreached voxel next to a key at the largest distance
   // the key format holds.  Checked on the converged tile, and only when some
   // key of the tile (row or halo) is at that distance.
@@ -563,7 +608,7 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
   __shared__ uint32_t dirs;
   __shared__ int reenq;
   __shared__ uint32_t item;
-  __shared__ uint32_t rfw[16];
+  __shared__ SweepShared sw;
   __shared__ uint32_t fbits[FLOOD_FDIR];
   __shared__ unsigned long long ph[5];  // thread 0: SM cycles per phase (see flush below)
   if (threadIdx.x < 5) ph[threadIdx.x] = 0;
@@ -599,8 +644,8 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
       const JobDesc& J = a.jobs[jid];
       const int conn6 = J.distance == 1;
       if (threadIdx.x == 0) ph[0] += clock64() - c_claim;
-      if (conn6) relax_brick<6>(a, J, jid, b, p, tile, live27, &dirs, &reenq, rfw, fbits, ph);
-      else relax_brick<26>(a, J, jid, b, p, tile, live27, &dirs, &reenq, rfw, fbits, ph);
+      if (conn6) relax_brick<6>(a, J, jid, b, p, tile, live27, &dirs, &reenq, sw, fbits, ph);
+      else relax_brick<26>(a, J, jid, b, p, tile, live27, &dirs, &reenq, sw, fbits, ph);
       if (threadIdx.x == 0) atomicMax(&a.st[jid].passes, p + 1);
       ++visits;
     }
