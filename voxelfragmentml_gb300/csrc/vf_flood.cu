@@ -269,18 +269,19 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
   // barrier, loads); a flag this visit does not see stays for the next visit,
   // which the same writer queued.
   uint32_t fv = 0;
-  if (t < (int)FLOOD_FDIR) {
-    fv = atomicExch(&a.fdir[(size_t)b * FLOOD_FDIR + t], 0u);
+  if (t < (int)FLOOD_FDIR) {  // exchange with acquire semantics
+    asm volatile("atom.acquire.gpu.global.exch.b32 %0, [%1], %2;"
+                 : "=r"(fv) : "l"(a.fdir + (size_t)b * FLOOD_FDIR + t), "r"(0u) : "memory");
     fbits[t] = fv;
-    __threadfence();
   }
-  if (t < 27) {
-    const int dx = t / 9 - 1, dy = (t / 3) % 3 - 1, dz = t % 3 - 1;
+  if (t >= 32 && t < 32 + 27) {  // live map of the 27 bricks around (warp 1)
+    const int n = t - 32;
+    const int dx = n / 9 - 1, dy = (n / 3) % 3 - 1, dz = n % 3 - 1;
     const int nx = bx + dx, ny = by + dy, nz = bz + dz;
     uint32_t l = 0;
     if (nx >= 0 && ny >= 0 && nz >= 0 && nx < (int)J.nbx && ny < (int)J.nby && nz < (int)J.nbz)
       l = a.live[brick_id(J, nx, ny, nz)];
-    live27[t] = l;
+    live27[n] = l;
   }
   __shared__ uint32_t scnt[3];
   if (t == 0) { *dirs = 0; *reenq = 0; scnt[0] = 0; scnt[1] = 0; scnt[2] = 0; }
@@ -296,6 +297,28 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     constexpr int SU = 6;
     const size_t nk = (size_t)J.X * J.Y * J.Zk;
     bool bad = false;
+    // halo keys first (their loads overlap the chunk loads): row q >> 1;
+    // side 0: key z0-1 -> [3], 1: key z0+32 -> [0]
+    uint32_t h[3];
+#pragma unroll
+    for (int u = 0; u < 3; ++u) {
+      const int q = t + u * 256;
+      h[u] = 0;
+      if (q < KROWS * 2) {
+        const int row = q >> 1, side = q & 1;
+        const int lx = row / KNY - 1, ly = row % KNY - 1;
+        const int x = x0 + lx, y = y0 + ly, z = side ? z0 + VF_BZ : z0 - 1;
+        if (x >= 0 && y >= 0 && z >= 0 && x < (int)J.X && y < (int)J.Y && z < (int)J.Zk) {
+          const int dx = lx < 0 ? 0 : (lx >= VF_BX ? 2 : 1);
+          const int dy = ly < 0 ? 0 : (ly >= VF_BY ? 2 : 1);
+          if (live27[dx * 9 + dy * 3 + (side ? 2 : 0)]) {
+            const size_t ki = vf_kidx(J, x, y, z);
+            if (ki < nk) h[u] = __ldcg(J.keys + ki);
+            else bad = true;
+          }
+        }
+      }
+    }
 #pragma unroll 1
     for (int base = t; base < KROWS * 8; base += SU * 256) {
       uint4 v[SU];
@@ -325,26 +348,6 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
       for (int u = 0; u < SU; ++u) {
         const int q = base + u * 256;
         if (q < KROWS * 8) *reinterpret_cast<uint4*>(tile + (q >> 3) * KP + 4 + 4 * (q & 7)) = v[u];
-      }
-    }
-    uint32_t h[3];
-#pragma unroll
-    for (int u = 0; u < 3; ++u) {
-      const int q = t + u * 256;  // row q >> 1; side 0: key z0-1 -> [3], 1: key z0+32 -> [0]
-      h[u] = 0;
-      if (q < KROWS * 2) {
-        const int row = q >> 1, side = q & 1;
-        const int lx = row / KNY - 1, ly = row % KNY - 1;
-        const int x = x0 + lx, y = y0 + ly, z = side ? z0 + VF_BZ : z0 - 1;
-        if (x >= 0 && y >= 0 && z >= 0 && x < (int)J.X && y < (int)J.Y && z < (int)J.Zk) {
-          const int dx = lx < 0 ? 0 : (lx >= VF_BX ? 2 : 1);
-          const int dy = ly < 0 ? 0 : (ly >= VF_BY ? 2 : 1);
-          if (live27[dx * 9 + dy * 3 + (side ? 2 : 0)]) {
-            const size_t ki = vf_kidx(J, x, y, z);
-            if (ki < nk) h[u] = __ldcg(J.keys + ki);
-            else bad = true;
-          }
-        }
       }
     }
 #pragma unroll
@@ -562,7 +565,7 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
   }
   // change records of the neighbours, after the key writes above (fence), then
   // the neighbours go on the next pass's queue
-  if (t < 32 || (t & 31) == 0) __threadfence();
+  if (t < 32 || (t & 31) == 0) asm volatile("fence.acq_rel.gpu;" ::: "memory");
   if ((t & 31) == 0) {
     const int w = t >> 5;
     if (zlo && live27[1 * 9 + 1 * 3 + 0]) {  // below: its keys at z0'+32 are our bottom layer
