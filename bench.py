@@ -174,11 +174,13 @@ def reference_arm(args):
     return 0
 
 
-# DRAM bytes per flood brick visit: dram__bytes_read.sum + dram__bytes_write.sum of
-# one k_relax launch over the first 48 jobs of mixed-256 (ncu, one GB300), divided
-# by that launch's 52557 brick visits.  The roofline's `traffic` is this figure
-# times the visits the timed launch made.
-K_RELAX_DRAM_BYTES_PER_VISIT = 2783539456 / 52557
+# DRAM bytes per staged flood brick visit: dram__bytes_read.sum +
+# dram__bytes_write.sum of one k_relax launch over the first 48 jobs of
+# mixed-256 (ncu, one GB300: 2298511616 + 207979008 B), divided by the 50965
+# visits of that launch that staged their brick (52963 visits, 1998 found
+# nothing new).  The roofline's `traffic` is this figure times the staged
+# visits of the timed launch.
+K_RELAX_DRAM_BYTES_PER_VISIT = (2298511616 + 207979008) / 50965
 
 
 def main():

@@ -463,6 +463,9 @@ __global__ void __launch_bounds__(256) k_detect(const JobDesc* jobs, const uint3
 constexpr int D1_ROWS = (VF_BX + 2) * (VF_BY + 2);
 constexpr int D1_W = VF_BZ / 2;  // u16 pairs per row
 constexpr int D1_BYTES = Tile<1>::BYTES + 2 * D1_ROWS * D1_W * 4;
+// 16-byte chunk c of window row r is stored at chunk c ^ ((r >> 1) & 3): the
+// chunk-q loads of any 8 consecutive rows then fall on 8 distinct bank groups
+__device__ __forceinline__ int d1_swz(int r, int c) { return c ^ ((r >> 1) & 3); }
 
 __global__ void __launch_bounds__(256, 3) k_detect1(const JobDesc* jobs, const uint32_t* list,
                                                  const uint32_t* count, const uint32_t* brick_job) {
@@ -482,30 +485,26 @@ __global__ void __launch_bounds__(256, 3) k_detect1(const JobDesc* jobs, const u
     __syncthreads();
     const bool self_only = J.boundary_size <= 0;  // uniform across the CTA
     if (!self_only) {
-      // phase 1: z-window extrema of every staged row
-      for (int r = threadIdx.x; r < D1_ROWS; r += blockDim.x) {
-        const uint16_t* row = tile + r * ZW + 8;  // z = z0 + 0
-        uint32_t lo_prev, hi_prev, lo_cur, hi_cur;
-        auto lab = [](uint16_t w, uint32_t& lo, uint32_t& hi) {
-          const uint32_t u = w & 0x7FFFu;
-          lo = u > VOXEL_FREE ? u : 0xFFFFu;
-          hi = u > VOXEL_FREE ? u : 0u;
+      // phase 1: z-window extrema of every staged row, one u16 pair (z = 2p,
+      // 2p + 1) per thread: the window of the pair is (2p-1, 2p), (2p, 2p+1)
+      // and (2p+1, 2p+2), taken from three aligned u32 words by byte permutes
+      for (int i = threadIdx.x; i < D1_ROWS * D1_W; i += blockDim.x) {
+        const int r = i >> 4, p = i & (D1_W - 1);
+        const uint32_t* rw = reinterpret_cast<const uint32_t*>(tile + r * ZW + 8) + p;
+        const uint32_t w1 = rw[0];
+        const uint32_t wa = __byte_perm(rw[-1], w1, 0x5432), wc = __byte_perm(w1, rw[1], 0x5432);
+        // labelled halves keep u = w & 0x7FFF, the others become 0xFFFF (min) / 0 (max)
+        auto lo = [](uint32_t w) {
+          const uint32_t u = w & 0x7FFF7FFFu;
+          return u | ~__vcmpgtu2(u, 0x00010001u);
         };
-        lab(row[-1], lo_prev, hi_prev);
-        lab(row[0], lo_cur, hi_cur);
-        uint32_t* mnr = zmin + r * D1_W;
-        uint32_t* mxr = zmax + r * D1_W;
-        for (int p = 0; p < D1_W; ++p) {
-          uint32_t lo1, hi1, lo2, hi2;
-          lab(row[2 * p + 1], lo1, hi1);
-          lab(row[2 * p + 2], lo2, hi2);
-          const uint32_t mn0 = min(lo_prev, min(lo_cur, lo1)), mx0 = max(hi_prev, max(hi_cur, hi1));
-          const uint32_t mn1 = min(lo_cur, min(lo1, lo2)), mx1 = max(hi_cur, max(hi1, hi2));
-          mnr[p] = mn0 | (mn1 << 16);
-          mxr[p] = mx0 | (mx1 << 16);
-          lo_prev = lo1; hi_prev = hi1;
-          lo_cur = lo2; hi_cur = hi2;
-        }
+        auto hi = [](uint32_t w) {
+          const uint32_t u = w & 0x7FFF7FFFu;
+          return u & __vcmpgtu2(u, 0x00010001u);
+        };
+        const int o = r * D1_W + (d1_swz(r, p >> 2) << 2) + (p & 3);
+        zmin[o] = __vminu2(__vminu2(lo(wa), lo(w1)), lo(wc));
+        zmax[o] = __vmaxu2(__vmaxu2(hi(wa), hi(w1)), hi(wc));
       }
       __syncthreads();
     }
@@ -521,12 +520,15 @@ __global__ void __launch_bounds__(256, 3) k_detect1(const JobDesc* jobs, const u
     for (uint32_t q = 0; q < nq; ++q) {
       uint32_t out[4];
       bool any = false;
+      // the row's 8 voxels of this chunk, one 16-byte load
+      const uint4 gq = *reinterpret_cast<const uint4*>(own + 8 * q);
+      const uint32_t gw[4] = {gq.x, gq.y, gq.z, gq.w};
       if (self_only) {
         // the window is the voxel itself: only a marked voxel can differ from
         // its own masked value
 #pragma unroll
         for (int h = 0; h < 8; ++h) {
-          const uint16_t g = own[8 * q + h];
+          const uint16_t g = (uint16_t)(gw[h >> 1] >> (16 * (h & 1)));
           const uint32_t u = g & 0x7FFFu;
           const bool bd = g > VOXEL_FREE && u > VOXEL_FREE && u != g;
           const uint32_t o = bd ? (uint32_t)(g | 0x8000u) : (uint32_t)g;
@@ -540,8 +542,8 @@ __global__ void __launch_bounds__(256, 3) k_detect1(const JobDesc* jobs, const u
 #pragma unroll 3
         for (int r = 0; r < 9; ++r) {
           const int row = (lx + r / 3) * Tile<1>::NY + (ly + r % 3);
-          const uint4 a = reinterpret_cast<const uint4*>(zmin + row * D1_W)[q];
-          const uint4 c = reinterpret_cast<const uint4*>(zmax + row * D1_W)[q];
+          const uint4 a = reinterpret_cast<const uint4*>(zmin + row * D1_W)[d1_swz(row, q)];
+          const uint4 c = reinterpret_cast<const uint4*>(zmax + row * D1_W)[d1_swz(row, q)];
           mn.x = __vminu2(mn.x, a.x); mn.y = __vminu2(mn.y, a.y);
           mn.z = __vminu2(mn.z, a.z); mn.w = __vminu2(mn.w, a.w);
           mx.x = __vmaxu2(mx.x, c.x); mx.y = __vmaxu2(mx.y, c.y);
@@ -552,7 +554,7 @@ __global__ void __launch_bounds__(256, 3) k_detect1(const JobDesc* jobs, const u
         for (int h = 0; h < 8; ++h) {
           const uint32_t lo = (mns[h >> 1] >> (16 * (h & 1))) & 0xFFFFu;
           const uint32_t hi = (mxs[h >> 1] >> (16 * (h & 1))) & 0xFFFFu;
-          const uint16_t g = own[8 * q + h];
+          const uint16_t g = (uint16_t)(gw[h >> 1] >> (16 * (h & 1)));
           const bool bd = g > VOXEL_FREE && lo != 0xFFFFu && (lo != g || hi != g);
           const uint32_t o = bd ? (uint32_t)(g | 0x8000u) : (uint32_t)g;
           if (h & 1) out[h >> 1] |= o << 16; else out[h >> 1] = o;
