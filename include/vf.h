@@ -69,6 +69,7 @@ typedef int vf_status;
 typedef struct vf_ctx vf_ctx;
 typedef struct vf_grid vf_grid;
 typedef struct vf_server vf_server;
+typedef struct vf_pipeline vf_pipeline;
 
 /* Fracture parameters: the hot-path fields of FractureParameters
  * (FractureParameters.h:43-85, defaults :91-145). */
@@ -254,6 +255,26 @@ vf_status vf_server_submit(vf_server* s, const vf_job* job, uint64_t* ticket);
 vf_status vf_server_poll(vf_server* s, vf_job_result* out, uint32_t max,
                          uint32_t* n, int wait_ms);
 vf_status vf_server_destroy(vf_server* s);
+
+/* ---- pipelined batches ---------------------------------------------------
+ * No counterpart in the reference.  A caller with a stream of batches keeps
+ * up to `depth` (1..4) of them in flight, each with its own stream and device
+ * memory: vf_pipeline_submit plans a batch, issues its uploads, stages and
+ * downloads, and returns; vf_pipeline_collect waits for the oldest batch and
+ * writes its results (vf_batch_run semantics per batch).  Labels are packed
+ * on the device and copied to out_labels by the copy engine, so the download
+ * of one batch runs while the next batch computes.  The jobs' host buffers
+ * must stay valid until their batch is collected. */
+vf_status vf_pipeline_create(vf_ctx* ctx, uint32_t depth, vf_pipeline** out);
+/* VF_ERR_BUSY when `depth` batches are in flight: collect one first */
+vf_status vf_pipeline_submit(vf_pipeline* p, const vf_job* jobs, uint32_t njobs);
+/* results of the oldest batch, in job order; *njobs = its job count.
+ * VF_ERR_INVALID when no batch is in flight or max < its job count (the
+ * batch then stays in flight). */
+vf_status vf_pipeline_collect(vf_pipeline* p, vf_job_result* results, uint32_t max,
+                              uint32_t* njobs);
+/* waits for the batches in flight (their results are dropped) */
+vf_status vf_pipeline_destroy(vf_pipeline* p);
 
 /* ---- flood without device allocation ------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device

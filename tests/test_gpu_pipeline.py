@@ -263,3 +263,34 @@ def test_large_batch_matches_small_batches(vf, ctx):
         assert r.status == 0 and r.user_tag == a.tag
         assert np.array_equal(a.labels, b.labels), f"job {a.tag}"
         assert np.array_equal(a.counts, b.counts)
+
+
+def test_pipeline_overlapped_batches_match_batch_run(vf, ctx):
+    """vf_pipeline_*: batches in flight (pinned and pageable outputs, odd
+    dims) give the bits of vf_batch_run, collected in submission order; a
+    full pipeline refuses another batch; collect with nothing in flight is an
+    error."""
+    ref = {}
+    for i in range(12):
+        s = _job(vf, i)
+        vf.batch_run([s], ctx)
+        ref[i] = (s.labels.copy(), s.counts.copy())
+    pipe = vf.Pipeline(ctx, depth=2)
+    batches = [[_job(vf, i, pinned=bool(i % 2)) for i in range(k, k + 4)] for k in (0, 4, 8)]
+    pipe.submit(batches[0])
+    pipe.submit(batches[1])
+    with pytest.raises(vf.VFError) as e:
+        pipe.submit(batches[2])
+    assert e.value.status == vf.ERR_BUSY
+    done = [pipe.collect()]
+    pipe.submit(batches[2])
+    done += [pipe.collect(), pipe.collect()]
+    for b, res in zip(batches, done):
+        assert len(res) == len(b)
+        for s, r in zip(b, res):
+            assert r.status == 0
+            assert np.array_equal(s.labels, ref[s.tag][0]), f"job {s.tag}"
+            assert np.array_equal(s.counts, ref[s.tag][1])
+    with pytest.raises(vf.VFError):
+        pipe.collect()
+    pipe.close()

@@ -135,6 +135,10 @@ EXPORTS = {
     "vf_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "vf_server_poll": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int]),
     "vf_server_destroy": (C.c_int, [C.c_void_p]),
+    "vf_pipeline_create": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
+    "vf_pipeline_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "vf_pipeline_collect": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "vf_pipeline_destroy": (C.c_int, [C.c_void_p]),
     "vf_flood_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
                                    C.c_void_p, C.c_uint32, C.c_int, C.c_void_p]),
     "vf_ctx_event_record": (C.c_int, [C.c_void_p, C.c_int]),
@@ -481,6 +485,51 @@ def _run(fn, specs, ctx):
 def batch_run(specs, ctx: Context | None = None):
     """Batched path: every stage once over all jobs (vf_batch_run)."""
     return _run(lib().vf_batch_run, specs, ctx)
+
+
+class Pipeline:
+    """vf_pipeline_*: up to `depth` batches in flight; the download of one
+    batch runs while the next one computes.  submit() returns once the batch
+    is issued; collect() waits for the oldest batch and returns its results.
+    The specs' host buffers stay referenced until their batch is collected."""
+
+    def __init__(self, ctx: Context | None = None, depth: int = 2):
+        self.ctx = ctx or default_context()
+        h = C.c_void_p()
+        _check(lib().vf_pipeline_create(self.ctx.h, depth, C.byref(h)))
+        self.h = h
+        self._inflight = []  # (specs, job array) of the batches in flight, oldest first
+
+    def submit(self, specs):
+        specs = list(specs)
+        arr = (Job * len(specs))(*[s.job() for s in specs])
+        _check(lib().vf_pipeline_submit(self.h, arr, len(specs)))
+        self._inflight.append((specs, arr))
+
+    def collect(self):
+        if not self._inflight:
+            raise VFError(ERR_INVALID, "no batch in flight")
+        specs, _ = self._inflight[0]
+        res = (JobResult * len(specs))()
+        n = C.c_uint32()
+        st = lib().vf_pipeline_collect(self.h, res, len(specs), C.byref(n))
+        if st == OK or n.value:
+            self._inflight.pop(0)
+        if st != OK and all(r.status == OK for r in res[:n.value]):
+            _check(st)
+        return list(res[:n.value])
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().vf_pipeline_destroy(self.h)
+            self.h = None
+            self._inflight = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class ResidentBatch:

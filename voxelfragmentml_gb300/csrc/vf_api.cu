@@ -107,6 +107,8 @@ vf_status vf_ctx_create(int device, size_t hbm_budget, vf_ctx** out) {
     return fail(VF_ERR_CUDA, "stream creation failed");
   }
   for (int i = 0; i < 16; ++i) cudaEventCreate(&c->c.ev[i]);
+  cudaEventCreateWithFlags(&c->c.ev_relax, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&c->c.ev_compute, cudaEventDisableTiming);
   vf_status s = c->c.batch.init(&c->c, false);
   if (s) {
     delete c;
@@ -122,6 +124,8 @@ vf_status vf_ctx_destroy(vf_ctx* ctx) {
   cudaStreamSynchronize(ctx->c.stream);
   ctx->c.batch.release();
   for (int i = 0; i < 16; ++i) cudaEventDestroy(ctx->c.ev[i]);
+  if (ctx->c.ev_relax) cudaEventDestroy(ctx->c.ev_relax);
+  if (ctx->c.ev_compute) cudaEventDestroy(ctx->c.ev_compute);
   cudaStreamDestroy(ctx->c.stream);
   delete ctx;
   return VF_OK;
@@ -900,6 +904,82 @@ vf_status vf_server_poll(vf_server* s, vf_job_result* out, uint32_t max, uint32_
     s->done.pop_front();
   }
   *n = k;
+  return VF_OK;
+}
+
+// ---- pipelined batches ---------------------------------------------------------
+struct vf_pipeline {
+  vf_ctx* ctx = nullptr;
+  std::vector<vfr::Batch> slots;        // fixed size: batches keep raw device pointers
+  std::vector<std::vector<vf_job>> jobs;  // the submitted jobs of each slot
+  std::deque<int> order;                // slots in flight, oldest first
+};
+
+vf_status vf_pipeline_create(vf_ctx* ctx, uint32_t depth, vf_pipeline** out) {
+  if (!ctx || !out) return fail(VF_ERR_INVALID, "NULL argument");
+  if (depth < 1 || depth > 4) return fail(VF_ERR_RANGE, "pipeline depth must be in [1, 4]");
+  cudaSetDevice(ctx->c.device);
+  vf_pipeline* p = new vf_pipeline();
+  p->ctx = ctx;
+  p->slots.resize(depth);
+  p->jobs.resize(depth);
+  for (auto& b : p->slots) {
+    vf_status st = b.init(&ctx->c, true);
+    if (st) {
+      for (auto& x : p->slots) x.release();
+      delete p;
+      return st;
+    }
+    b.dma_download = true;
+  }
+  *out = p;
+  return VF_OK;
+}
+
+vf_status vf_pipeline_submit(vf_pipeline* p, const vf_job* jobs, uint32_t njobs) {
+  if (!p || (njobs && !jobs)) return fail(VF_ERR_INVALID, "NULL argument");
+  if (njobs == 0) return fail(VF_ERR_INVALID, "empty batch");
+  if (p->order.size() >= p->slots.size())
+    return fail(VF_ERR_BUSY, "pipeline full: collect a batch first");
+  cudaSetDevice(p->ctx->c.device);
+  int slot = 0;
+  while (std::find(p->order.begin(), p->order.end(), slot) != p->order.end()) ++slot;
+  vfr::Batch& B = p->slots[slot];
+  p->jobs[slot].assign(jobs, jobs + njobs);
+  std::vector<const vf_job*> ptrs(njobs);
+  for (uint32_t i = 0; i < njobs; ++i) ptrs[i] = &p->jobs[slot][i];
+  B.stages = vfr::ST_ALL;
+  B.given.clear();
+  vf_status s = B.plan(ptrs.data(), njobs);
+  if (!s) s = B.enqueue_batched();
+  if (s) {
+    // nothing of a failed enqueue is left running: wait for what was issued
+    cudaStreamSynchronize(B.stream);
+    return s;
+  }
+  p->order.push_back(slot);
+  return VF_OK;
+}
+
+vf_status vf_pipeline_collect(vf_pipeline* p, vf_job_result* results, uint32_t max,
+                              uint32_t* njobs) {
+  if (!p || !njobs) return fail(VF_ERR_INVALID, "NULL argument");
+  if (p->order.empty()) return fail(VF_ERR_INVALID, "no batch in flight");
+  const int slot = p->order.front();
+  const uint32_t n = (uint32_t)p->jobs[slot].size();
+  if (max < n || (n && !results)) return fail(VF_ERR_INVALID, "results array shorter than the batch");
+  cudaSetDevice(p->ctx->c.device);
+  p->order.pop_front();
+  *njobs = n;
+  return p->slots[slot].finish(results);
+}
+
+vf_status vf_pipeline_destroy(vf_pipeline* p) {
+  if (!p) return VF_OK;
+  cudaSetDevice(p->ctx->c.device);
+  for (int slot : p->order) cudaStreamSynchronize(p->slots[slot].stream);
+  for (auto& b : p->slots) b.release();
+  delete p;
   return VF_OK;
 }
 

@@ -136,7 +136,7 @@ void Batch::release() {
   for (DevBuf* b : {&grid0, &grid1, &keys, &par, &tets, &range, &ys, &seeds, &counts, &lat,
                     &verts, &faces, &emask, &etab, &tables, &state, &brick_job, &live, &list, &lcount,
                     &q[0], &q[1], &q[2], &scal, &epoch, &fdir, &front[0], &front[1], &pcnt, &pbase,
-                    &psums, &srec, &rle_cnt, &rle_base, &rle_sums, &rle_tot, &rle_starts,
+                    &psums, &srec, &stage_out, &rle_cnt, &rle_base, &rle_sums, &rle_tot, &rle_starts,
                     &rle_rec})
     ctx->free_buf(*b);
   if (h_tables) cudaFreeHost(h_tables);
@@ -336,6 +336,9 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
     p.o_verts = sz.verts; sz.verts += align_up((size_t)j.nverts * 3, 64);
     p.o_faces = sz.faces; sz.faces += align_up((size_t)j.nfaces * 3, 64);
     p.o_emask = sz.emask; sz.emask += align_up(p.emask.size(), 64);
+    p.dma = dma_download && j.out_labels != nullptr;
+    p.o_out = sz.out;
+    if (p.dma) sz.out += align_up(vox * p.Z, 128);  // 256-byte aligned u16 rows
     sz.bricks += p.nbricks;
     sz.faces_total += j.nfaces;
     if (j.params.erode) sz.max_iters = std::max(sz.max_iters, (uint32_t)j.params.erosion_iterations);
@@ -375,6 +378,7 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
   ALLOC(pbase, nf * 8);
   ALLOC(psums, ((nf + 1023) / 1024 + 1) * 8);
   ALLOC(srec, nf * 96);
+  if (sz.out) ALLOC(stage_out, sz.out * 2);
 #undef ALLOC
   const size_t tbytes = sizeof(JobDesc) * ntables * std::max<size_t>(n, 1) + sz.emask * 4 + 256;
   if (tbytes > h_tables_cap) {
@@ -447,7 +451,10 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
     d.out = nullptr;
     d.row_base = sz.rows;
     sz.rows += (uint64_t)p.X * p.Y;
-    if (j.out_labels && ((uintptr_t)j.out_labels & 1) == 0) {
+    if (p.dma) {
+      d.out = static_cast<uint16_t*>(stage_out.p) + p.o_out;
+      p.packed = true;
+    } else if (j.out_labels && ((uintptr_t)j.out_labels & 1) == 0) {
       cudaPointerAttributes at;
       if (cudaPointerGetAttributes(&at, j.out_labels) == cudaSuccess && at.devicePointer &&
           at.type != cudaMemoryTypeUnregistered) {
@@ -612,6 +619,24 @@ static vfk::FloodScratch flood_scratch(Batch& B) {
   return fs;
 }
 
+// the flood relaxation, after the last one issued on the context (any stream)
+cudaError_t Batch::relax_serialized(cudaStream_t st, const JobDesc* tf, JobState* ds,
+                                    const uint32_t* bj, const uint8_t* lv, const vfk::FloodScratch& fs) {
+  const bool chain = !capturing && ctx->ev_relax;
+  std::unique_lock<std::mutex> lk(ctx->relax_mu, std::defer_lock);
+  if (chain) lk.lock();
+  if (chain && ctx->ev_relax_used) {
+    cudaError_t e = cudaStreamWaitEvent(st, ctx->ev_relax, 0);
+    if (e != cudaSuccess) return e;
+  }
+  cudaError_t e = vfk::flood_relax(st, tf, ds, bj, lv, fs, ctx->num_sms, &relax_blocks);
+  if (e == cudaSuccess && chain) {
+    e = cudaEventRecord(ctx->ev_relax, st);
+    ctx->ev_relax_used = e == cudaSuccess;
+  }
+  return e;
+}
+
 vf_status Batch::enqueue_batched(bool do_upload, bool do_download) {
   const uint32_t n = (uint32_t)jobs.size();
   cudaStream_t st = stream;
@@ -625,6 +650,11 @@ vf_status Batch::enqueue_batched(bool do_upload, bool do_download) {
   vf_status s = do_upload ? upload_inputs_impl(*this) : VF_OK;
   if (s) return s;
   mark(1);
+  const bool chain = !capturing && ctx->ev_compute;
+  if (chain) {
+    std::lock_guard<std::mutex> lk(ctx->relax_mu);
+    if (ctx->ev_compute_used) VF_CK(cudaStreamWaitEvent(st, ctx->ev_compute, 0));
+  }
   s = reset_scratch(*this);
   if (s) return s;
   JobState* ds = static_cast<JobState*>(state.p);
@@ -671,7 +701,7 @@ vf_status Batch::enqueue_batched(bool do_upload, bool do_download) {
     vfk::flood_init_keys(st, tf, lst, lc, maxc, bj, lv);
     vfk::flood_seed(st, tf, ds, n, fs, lv);
     VF_CK(record_event(ev_flood0, st));
-    cudaError_t e = vfk::flood_relax(st, tf, ds, bj, lv, fs, ctx->num_sms, &relax_blocks);
+    cudaError_t e = relax_serialized(st, tf, ds, bj, lv, fs);
     if (e != cudaSuccess) return fail(VF_ERR_CUDA, std::string("flood relax launch: ") + cudaGetErrorString(e));
     VF_CK(record_event(ev_flood1, st));
     flood_timed = true;
@@ -691,7 +721,7 @@ vf_status Batch::enqueue_batched(bool do_upload, bool do_download) {
         if (!any) break;
       }
       vfk::flood_disjoint(st, tf, ds, n, lst, lc, maxc, bj, fs, lv);
-      e = vfk::flood_relax(st, tf, ds, bj, lv, fs, ctx->num_sms, &relax_blocks);
+      e = relax_serialized(st, tf, ds, bj, lv, fs);
       if (e != cudaSuccess) return fail(VF_ERR_CUDA, std::string("flood relax launch: ") + cudaGetErrorString(e));
       vfk::flood_finalize(st, tf, ds, lst, lc, maxc, bj, 1);
       launches += 6;
@@ -719,6 +749,11 @@ vf_status Batch::enqueue_batched(bool do_upload, bool do_download) {
     launches += 1;
   }
   mark(10);
+  if (chain) {
+    std::lock_guard<std::mutex> lk(ctx->relax_mu);
+    VF_CK(cudaEventRecord(ctx->ev_compute, st));
+    ctx->ev_compute_used = true;
+  }
   VF_CK(cudaGetLastError());
   // downloads
   if ((stages & ST_DOWNLOAD) && do_download) {
@@ -733,6 +768,9 @@ vf_status Batch::enqueue_batched(bool do_upload, bool do_download) {
     const vf_job& j = *jobs[i];
     const JobPlan& p = plans[i];
     const uint16_t* src = static_cast<uint16_t*>(p.final_cur ? grid1.p : grid0.p) + p.o_grid;
+    if (p.dma)
+      VF_CK(cudaMemcpyAsync(j.out_labels, static_cast<uint16_t*>(stage_out.p) + p.o_out,
+                            (size_t)p.X * p.Y * p.Z * 2, cudaMemcpyDeviceToHost, st));
     if (j.out_labels && !p.packed) {
       if (p.Zp == p.Z)
         VF_CK(cudaMemcpyAsync(j.out_labels, src, (size_t)p.X * p.Y * p.Z * 2, cudaMemcpyDeviceToHost, st));

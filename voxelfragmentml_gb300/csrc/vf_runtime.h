@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -36,6 +37,8 @@ struct JobPlan {
   int final_cur;
   bool prefix_possible;
   bool packed;  // labels written to out_labels by the pack kernel
+  bool dma;     // packed into the staging buffer, then copied to out_labels by DMA
+  size_t o_out; // the job's labels in the staging buffer (u16)
 };
 
 struct Sizes {
@@ -43,6 +46,7 @@ struct Sizes {
          lat = 0, verts = 0, faces = 0, emask = 0, etab = 0;
   uint32_t bricks = 0, faces_total = 0, max_iters = 0;
   uint64_t rows = 0;  // sum of X * Y over the jobs
+  size_t out = 0;     // staging buffer of the DMA download (u16)
 };
 
 struct Ctx;
@@ -62,6 +66,11 @@ struct Batch {
   DevBuf rle_cnt, rle_base, rle_sums, rle_tot, rle_starts, rle_rec;  // RLE export scratch
   DevBuf tables, state, brick_job, live, list, lcount, q[3], scal, epoch, fdir, front[2];
   DevBuf pcnt, pbase, psums, srec;  // flattened per-face work lists, shell setup
+  DevBuf stage_out;  // packed labels of the DMA download
+  // download by DMA: labels are packed into a device staging buffer and
+  // copied to out_labels by the copy engine (no kernel writes host memory,
+  // so the download of one batch overlaps the kernels of the next)
+  bool dma_download = false;
   void* h_tables = nullptr;  // pinned staging
   size_t h_tables_cap = 0;
   JobState* h_state = nullptr;  // pinned
@@ -92,6 +101,8 @@ struct Batch {
   void release();
   vf_status plan(const vf_job* const* js, uint32_t n);
   vf_status enqueue_batched(bool upload_inputs = true, bool download = true);
+  cudaError_t relax_serialized(cudaStream_t st, const JobDesc* tf, JobState* ds, const uint32_t* bj,
+                               const uint8_t* lv, const vfk::FloodScratch& fs);
   // the resident stage chain (no uploads) as a CUDA graph: captured on the
   // first execute after plan(), replayed afterwards; falls back to direct
   // launches when the chain has host steps (sub-seed prefix competition) or
@@ -127,6 +138,18 @@ struct Ctx {
   size_t budget = 0;
   size_t in_use = 0;
   cudaEvent_t ev[16] = {};
+  // the last flood relaxation issued on any of the context's streams: the
+  // next one waits for it, so two cooperative (grid-barrier) launches of
+  // batches in flight never share the GPU
+  cudaEvent_t ev_relax = nullptr;
+  bool ev_relax_used = false;
+  std::mutex relax_mu;  // wait + launch + record as one step (server thread, callers)
+  // the end of the stage chain of the last batch issued on any stream: the
+  // next batch's stages start after it (its upload may run earlier), so the
+  // batches in flight compute one after another while each one's download
+  // overlaps the next one's kernels
+  cudaEvent_t ev_compute = nullptr;
+  bool ev_compute_used = false;
   Batch batch;
   // stats of the last batch
   uint64_t last_launches = 0;
