@@ -555,8 +555,10 @@ __device__ __forceinline__ void test_cell(const JobDesc& J, const float* cs, con
   if (hit) atomicOr(J.shell + ((size_t)i * J.Y + jj) * J.Zw + (k >> 5), 1u << (k & 31));
 }
 
-// Per-face setup of the shell test.  Candidates: the triangle's cell bbox
-// grown by one cell, as columns along the dominant normal axis c.  Per
+// Per-face setup of the shell test.  Candidates: the cells touching the
+// triangle's bounding box (widened by 0.01 cell + 256 ulp of the largest
+// coordinate: any cell further out fails the exact box-axis tests), as
+// columns along the dominant normal axis c.  Per
 // column, (1) the SAT tests that do not involve axis c (the c-family edge
 // axes and the two other box axes) run exactly, once: they are the same for
 // every cell of the column, and a column they reject holds no hit; (2) the
@@ -587,13 +589,25 @@ __device__ bool shell_setup(const JobDesc& J, uint32_t f, ShellSetup& S) {
   const float* q0 = J.verts + 3 * (size_t)fi[0];
   const float* q1 = J.verts + 3 * (size_t)fi[1];
   const float* q2 = J.verts + 3 * (size_t)fi[2];
+  // The largest coordinate in play sets the rounding scale of the float SAT
+  // (box bounds, centres, vertex offsets): its errors are a few ulp of M.
+  float M = 0.0f;
+  for (int a = 0; a < 3; ++a) {
+    M = fmaxf(M, fmaxf(fabsf(J.amin[a]), fabsf(J.amax[a])));
+    M = fmaxf(M, fmaxf(fabsf(q0[a]), fmaxf(fabsf(q1[a]), fabsf(q2[a]))));
+  }
+  const float ulp64 = M * 7.62939453125e-6f;  // 64 * 2^-23 * M
   int lo[3], n[3];
   for (int a = 0; a < 3; ++a) {
     float mn, mx;
     mm3(q0[a], q1[a], q2[a], mn, mx);
-    // one cell of margin on each side: far above the reciprocal's rounding
-    lo[a] = vf_clampi(float_cell(SUB(mn, J.amin[a]) * J.ics[a], dims[a]) - 1, 0, dims[a] - 1);
-    const int hi = vf_clampi(float_cell(SUB(mx, J.amin[a]) * J.ics[a], dims[a]) + 1, 0, dims[a] - 1);
+    // Cells that touch the triangle's extent along a, widened by 0.01 cell +
+    // 256 ulp of M: a cell further out fails the exact SAT's box-axis test,
+    // whose roundings are a few ulp of M; the 0.01 cell covers the rounding
+    // of these index computations (below 2^-11 cell for 4096 cells).
+    const float mc = 0.01f + 4.0f * ulp64 * J.ics[a];
+    lo[a] = vf_clampi(float_cell(SUB(mn, J.amin[a]) * J.ics[a] - mc, dims[a]), 0, dims[a] - 1);
+    const int hi = vf_clampi(float_cell(SUB(mx, J.amin[a]) * J.ics[a] + mc, dims[a]), 0, dims[a] - 1);
     n[a] = hi - lo[a] + 1;
   }
   S.p0 = {q0[0], q0[1], q0[2]};
@@ -639,12 +653,6 @@ __device__ bool shell_setup(const JobDesc& J, uint32_t f, ShellSetup& S) {
   // half cell + margin.  The margin (2% of a cell + 64 ulp of the largest
   // coordinate in play) is far above the rounding of the exact float SAT and
   // of these bounds, so no cell the exact test accepts is dropped.
-  float M = 0.0f;
-  for (int a = 0; a < 3; ++a) {
-    M = fmaxf(M, fmaxf(fabsf(J.amin[a]), fabsf(J.amax[a])));
-    M = fmaxf(M, fmaxf(fabsf(q0[a]), fmaxf(fabsf(q1[a]), fabsf(q2[a]))));
-  }
-  const float ulp64 = M * 7.62939453125e-6f;  // 64 * 2^-23 * M
   S.ha = 0.52f * S.cs_a + ulp64;
   S.hb = 0.52f * S.cs_b + ulp64;
   const float hc = 0.52f * cs_c + ulp64;
