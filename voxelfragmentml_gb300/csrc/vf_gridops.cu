@@ -338,44 +338,58 @@ __device__ __forceinline__ float lerp_(float a, float b, float t) {
 
 __global__ void __launch_bounds__(256) k_perturb(const JobDesc* jobs, const uint32_t* list,
                                                  const uint32_t* count, const uint32_t* brick_job) {
+  // per brick: the lattice index and in-cell coordinate of its 32 z values
+  // (every row of the brick shares them), t = (z mod P) / P rounded as the
+  // oracle divides
+  __shared__ float t2s[VF_BZ];
+  __shared__ uint32_t i2s[VF_BZ];
+  // the thread's row of labels (34-u16 pitch: the u16 of one z from 32
+  // threads falls on 32 distinct banks)
+  __shared__ __align__(16) uint16_t vrows[256 * 34];
+  uint16_t* v = vrows + threadIdx.x * 34;
   const uint32_t n = *count;
   for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
     const uint32_t b = list[it];
     const JobDesc& J = jobs[brick_job[b]];
-    if (!J.active) continue;
+    if (!J.active) continue;  // uniform across the CTA
     uint32_t x0, y0, z0;
     brick_coords(J, b, x0, y0, z0);
+    const uint32_t P = J.noise_period;
+    const float fp = (float)P;
+    __syncthreads();  // the previous brick's rows are done with the tables
+    if (threadIdx.x < VF_BZ) {
+      const uint32_t gz = z0 + threadIdx.x;
+      t2s[threadIdx.x] = __fdiv_rn((float)(gz % P), fp);
+      i2s[threadIdx.x] = gz / P;
+    }
+    __syncthreads();
     const uint32_t x = x0 + threadIdx.x / VF_BY, y = y0 + threadIdx.x % VF_BY;
     if (x >= J.X || y >= J.Y) continue;
     const uint16_t* src = J.grid;
-    uint16_t v[VF_BZ];
     const uint4* s4 = reinterpret_cast<const uint4*>(src + vf_gidx(J, x, y, z0));
     const uint32_t nz = min((uint32_t)VF_BZ, J.Zp - z0);
+    uint32_t* v32 = reinterpret_cast<uint32_t*>(v);  // 4-byte aligned: 68-byte pitch
 #pragma unroll
     for (int q = 0; q < VF_BZ / 8; ++q) {
-      uint4 w = (q * 8 < (int)nz) ? s4[q] : make_uint4(0, 0, 0, 0);
-      v[8 * q + 0] = w.x & 0xFFFF; v[8 * q + 1] = w.x >> 16;
-      v[8 * q + 2] = w.y & 0xFFFF; v[8 * q + 3] = w.y >> 16;
-      v[8 * q + 4] = w.z & 0xFFFF; v[8 * q + 5] = w.z >> 16;
-      v[8 * q + 6] = w.w & 0xFFFF; v[8 * q + 7] = w.w >> 16;
+      const uint4 w = (q * 8 < (int)nz) ? s4[q] : make_uint4(0, 0, 0, 0);
+      v32[4 * q + 0] = w.x; v32[4 * q + 1] = w.y; v32[4 * q + 2] = w.z; v32[4 * q + 3] = w.w;
     }
     // Per labelled voxel: a 3-channel trilinear value noise n(v / P) from the
     // lattice (lerp along z, then y, then x, as the oracle), offset
     // floor(A * n + 0.5) per axis, and the label found there if it is labelled.
     // The lattice cell of this row changes only every P voxels along z: its
     // 8 corners x 3 channels stay in registers; t0, t1 are per row.
-    const uint32_t P = J.noise_period;
-    const float fp = (float)P;
     const float t0 = __fdiv_rn((float)(x % P), fp), t1 = __fdiv_rn((float)(y % P), fp);
     const uint32_t sy = J.lat_nz * 3, sx = J.lat_ny * sy;
     const float* Lrow = J.lattice + (size_t)(x / P) * sx + (size_t)(y / P) * sy;
+    const float amp = J.noise_amplitude;
     float cn[3][8];
     uint32_t cached = 0xFFFFFFFFu;
 #pragma unroll 1
     for (int z = 0; z < VF_BZ; ++z) {
       if (v[z] <= VOXEL_FREE) continue;
       const uint32_t gz = z0 + z;
-      const uint32_t i2 = gz / P;
+      const uint32_t i2 = i2s[z];
       if (i2 != cached) {
         cached = i2;
         const float* L = Lrow + (size_t)i2 * 3;
@@ -387,7 +401,7 @@ __global__ void __launch_bounds__(256) k_perturb(const JobDesc* jobs, const uint
           cn[ch][6] = L[sx + sy + ch]; cn[ch][7] = L[sx + sy + 3 + ch];
         }
       }
-      const float t2 = __fdiv_rn((float)(gz % P), fp);
+      const float t2 = t2s[z];
       int o[3];
 #pragma unroll
       for (int ch = 0; ch < 3; ++ch) {
@@ -395,7 +409,7 @@ __global__ void __launch_bounds__(256) k_perturb(const JobDesc* jobs, const uint
         const float c10 = lerp_(cn[ch][4], cn[ch][5], t2), c11 = lerp_(cn[ch][6], cn[ch][7], t2);
         const float c0 = lerp_(c00, c01, t1), c1 = lerp_(c10, c11, t1);
         const float nz = lerp_(c0, c1, t0);
-        o[ch] = (int)floorf(__fadd_rn(__fmul_rn(J.noise_amplitude, nz), 0.5f));
+        o[ch] = (int)floorf(__fadd_rn(__fmul_rn(amp, nz), 0.5f));
       }
       const long ux = (long)x + o[0], uy = (long)y + o[1], uz = (long)gz + o[2];
       if (ux < 0 || uy < 0 || uz < 0 || ux >= (long)J.X || uy >= (long)J.Y || uz >= (long)J.Z) continue;
