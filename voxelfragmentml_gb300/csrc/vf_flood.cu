@@ -255,7 +255,7 @@ template <int CONN>
 __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, uint32_t b,
                             uint32_t pass, uint32_t* tile, uint32_t* live27, uint32_t* dirs,
                             int* reenq, SweepShared& sw, uint32_t* fbits,
-                            unsigned long long* ph) {
+                            unsigned long long* ph, uint32_t i, uint32_t qn, uint32_t* pre) {
   // ph (thread 0): SM cycles of [1] live map + staging, [2] sweeps, [3] write-back + enqueue
   long long c0 = 0;
   if (threadIdx.x == 0) c0 = clock64();
@@ -290,10 +290,44 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     return;
   }
   // stage keys: rows [x0-1, x0+17) x [y0-1, y0+17), keys z0 .. z0+31 (8 chunks
-  // of 4) and the halo keys z0-1, z0+32.  Each thread keeps SU 16-byte loads in
-  // flight before it stores them.  Keys outside the grid or in a brick without
-  // occupied voxels are zero (EMPTY).
-  {
+  // of 4) and the halo keys z0-1, z0+32, by warps 0-6: each thread keeps SU
+  // 16-byte loads in flight before it stores them.  Keys outside the grid or
+  // in a brick without occupied voxels are zero (EMPTY).  Warp 7 meanwhile
+  // claims this CTA's next brick of the pass (while much of the pass is left)
+  // and prefetches its tile rows into L2.
+  constexpr int NST = 224;  // staging threads
+  if (t >= NST) {
+    const int lane = t - NST;
+    uint32_t nx = 0xFFFFFFFFu;
+    if (lane == 0 && i + 2u * gridDim.x < qn) {
+      const uint32_t c = atomicAdd(&a.qhead[pass % 3u], 1u);
+      if (c < qn) nx = c;
+    }
+    nx = __shfl_sync(0xFFFFFFFFu, nx, 0);
+    if (nx != 0xFFFFFFFFu) {
+      if (lane == 0) *pre = nx;
+      const uint32_t nb = a.queue[pass % 3u][nx];
+      if (nb < a.nbricks) {
+        const uint32_t nj = a.brick_job[nb];
+        if (nj < a.njobs) {
+          const JobDesc& N = a.jobs[nj];
+          const uint32_t nl = nb - N.brick_base;
+          const int nbz = nl % N.nbz, nby = (nl / N.nbz) % N.nby, nbx = nl / (N.nbz * N.nby);
+          const int nx0 = nbx * VF_BX, ny0 = nby * VF_BY, nz0 = nbz * VF_BZ;
+          const int za = max(nz0 - 1, 0), zm = min(nz0 + 15, (int)N.Zk - 1),
+                    zb = min(nz0 + VF_BZ, (int)N.Zk - 1);
+          for (int r = lane; r < KROWS; r += 32) {
+            const int x = nx0 + r / KNY - 1, y = ny0 + r % KNY - 1;
+            if (x < 0 || y < 0 || x >= (int)N.X || y >= (int)N.Y) continue;
+            const uint32_t* row = N.keys + vf_kidx(N, x, y, 0);
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(row + za));
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(row + zm));
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(row + zb));
+          }
+        }
+      }
+    }
+  } else {
     constexpr int SU = 6;
     const size_t nk = (size_t)J.X * J.Y * J.Zk;
     bool bad = false;
@@ -302,7 +336,7 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     uint32_t h[3];
 #pragma unroll
     for (int u = 0; u < 3; ++u) {
-      const int q = t + u * 256;
+      const int q = t + u * NST;
       h[u] = 0;
       if (q < KROWS * 2) {
         const int row = q >> 1, side = q & 1;
@@ -320,11 +354,11 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
       }
     }
 #pragma unroll 1
-    for (int base = t; base < KROWS * 8; base += SU * 256) {
+    for (int base = t; base < KROWS * 8; base += SU * NST) {
       uint4 v[SU];
 #pragma unroll
       for (int u = 0; u < SU; ++u) {
-        const int q = base + u * 256;
+        const int q = base + u * NST;
         v[u] = make_uint4(0, 0, 0, 0);
         if (q < KROWS * 8) {
           const int row = q >> 3, part = q & 7;
@@ -346,13 +380,13 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
       }
 #pragma unroll
       for (int u = 0; u < SU; ++u) {
-        const int q = base + u * 256;
+        const int q = base + u * NST;
         if (q < KROWS * 8) *reinterpret_cast<uint4*>(tile + (q >> 3) * KP + 4 + 4 * (q & 7)) = v[u];
       }
     }
 #pragma unroll
     for (int u = 0; u < 3; ++u) {
-      const int q = t + u * 256;
+      const int q = t + u * NST;
       if (q < KROWS * 2) tile[(q >> 1) * KP + ((q & 1) ? 0 : 3)] = h[u];
     }
     if (bad) flood_anomaly(a, 3u, b, (uint32_t)t);
@@ -611,10 +645,12 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
   __shared__ uint32_t dirs;
   __shared__ int reenq;
   __shared__ uint32_t item;
+  __shared__ uint32_t pre;  // queue index of the next brick, claimed ahead (~0: none)
   __shared__ SweepShared sw;
   __shared__ uint32_t fbits[FLOOD_FDIR];
   __shared__ unsigned long long ph[5];  // thread 0: SM cycles per phase (see flush below)
   if (threadIdx.x < 5) ph[threadIdx.x] = 0;
+  if (threadIdx.x == 0) pre = 0xFFFFFFFFu;
   for (uint32_t p = 0; p < a.max_passes; ++p) {
     const uint32_t cur = p % 3u;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -629,7 +665,8 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
       __syncthreads();
       if (threadIdx.x == 0) {
         c_claim = clock64();
-        item = atomicAdd(&a.qhead[cur], 1u);
+        item = pre != 0xFFFFFFFFu ? pre : atomicAdd(&a.qhead[cur], 1u);
+        pre = 0xFFFFFFFFu;
       }
       __syncthreads();
       const uint32_t i = item;
@@ -647,8 +684,8 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
       const JobDesc& J = a.jobs[jid];
       const int conn6 = J.distance == 1;
       if (threadIdx.x == 0) ph[0] += clock64() - c_claim;
-      if (conn6) relax_brick<6>(a, J, jid, b, p, tile, live27, &dirs, &reenq, sw, fbits, ph);
-      else relax_brick<26>(a, J, jid, b, p, tile, live27, &dirs, &reenq, sw, fbits, ph);
+      if (conn6) relax_brick<6>(a, J, jid, b, p, tile, live27, &dirs, &reenq, sw, fbits, ph, i, qn, &pre);
+      else relax_brick<26>(a, J, jid, b, p, tile, live27, &dirs, &reenq, sw, fbits, ph, i, qn, &pre);
       if (threadIdx.x == 0) atomicMax(&a.st[jid].passes, p + 1);
       ++visits;
     }
