@@ -175,7 +175,8 @@ struct SweepShared {
 // pass, both starting from the row's z halo candidates hlo / hhi.  Returns the
 // z positions whose key changed.
 template <int CONN>
-__device__ __forceinline__ uint32_t relax_row(uint32_t* own_row, uint32_t hlo, uint32_t hhi) {
+__device__ __forceinline__ uint32_t relax_row(uint32_t* own_row, uint32_t hlo, uint32_t hhi,
+                                              bool full_backward) {
   uint32_t chg = 0;
   // forward: cross-row candidates fused with the increasing-z pass
   uint32_t prev = hlo;
@@ -229,10 +230,18 @@ __device__ __forceinline__ uint32_t relax_row(uint32_t* own_row, uint32_t hlo, u
         *reinterpret_cast<uint4*>(own_row + 4 + 4 * q) = make_uint4(f[0], f[1], f[2], f[3]);
     }
   }
-  // backward in-row pass
-  prev = hhi;
+  // Backward in-row pass.  A row that is already consistent along z with its
+  // (unchanged) halo key above needs it only from the highest chunk the
+  // forward pass changed, and only down to where nothing changes and no
+  // forward change lies below; full_backward: the whole row from the halo.
+  int q = 7;
+  if (!full_backward) {
+    if (!chg) return 0u;
+    q = (31 - __clz(chg)) >> 2;
+  }
+  prev = q == 7 ? hhi : own_row[4 + 4 * q + 4];
 #pragma unroll 1
-  for (int q = 7; q >= 0; --q) {
+  for (; q >= 0; --q) {
     const uint4 kv = lds4(own_row + 4 + 4 * q);
     const uint32_t kk[4] = {kv.x, kv.y, kv.z, kv.w};
     uint32_t f[4];
@@ -246,6 +255,8 @@ __device__ __forceinline__ uint32_t relax_row(uint32_t* own_row, uint32_t hlo, u
     if (cq) {
       *reinterpret_cast<uint4*>(own_row + 4 + 4 * q) = make_uint4(f[0], f[1], f[2], f[3]);
       chg |= cq << (4 * q);
+    } else if ((chg & (0xFFFFFFFFu >> (28 - 4 * q))) == 0u) {
+      break;  // this chunk and everything below it unchanged: consistent
     }
   }
   return chg;
@@ -479,7 +490,7 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     if (t < (int)n) {
       const int row = sw.rlist[t];
       uint32_t* rr = tile + (((row >> 4) + 1) * KNY + ((row & 15) + 1)) * KP;
-      chg = relax_row<CONN>(rr, sw.hl[row], sw.hh[row]);
+      chg = relax_row<CONN>(rr, sw.hl[row], sw.hh[row], it == 0);
       if (chg) {
         atomicOr(&sw.rfw[(cur ^ 1) * 8 + (row >> 5)], 1u << (row & 31));
         sw.rowchg[row] |= chg;
