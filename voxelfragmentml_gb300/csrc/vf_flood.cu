@@ -304,8 +304,8 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
   // of 4) and the halo keys z0-1, z0+32, by warps 0-6: each thread keeps SU
   // 16-byte loads in flight before it stores them.  Keys outside the grid or
   // in a brick without occupied voxels are zero (EMPTY).  Warp 7 meanwhile
-  // claims this CTA's next brick of the pass (while much of the pass is left)
-  // and prefetches its tile rows into L2.
+  // claims this CTA's next brick of the pass (while much of the pass is
+  // left), so the next visit starts without a claim round trip.
   constexpr int NST = 224;  // staging threads
   if (t >= NST) {
     const int lane = t - NST;
@@ -315,29 +315,7 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
       if (c < qn) nx = c;
     }
     nx = __shfl_sync(0xFFFFFFFFu, nx, 0);
-    if (nx != 0xFFFFFFFFu) {
-      if (lane == 0) *pre = nx;
-      const uint32_t nb = a.queue[pass % 3u][nx];
-      if (nb < a.nbricks) {
-        const uint32_t nj = a.brick_job[nb];
-        if (nj < a.njobs) {
-          const JobDesc& N = a.jobs[nj];
-          const uint32_t nl = nb - N.brick_base;
-          const int nbz = nl % N.nbz, nby = (nl / N.nbz) % N.nby, nbx = nl / (N.nbz * N.nby);
-          const int nx0 = nbx * VF_BX, ny0 = nby * VF_BY, nz0 = nbz * VF_BZ;
-          const int za = max(nz0 - 1, 0), zm = min(nz0 + 15, (int)N.Zk - 1),
-                    zb = min(nz0 + VF_BZ, (int)N.Zk - 1);
-          for (int r = lane; r < KROWS; r += 32) {
-            const int x = nx0 + r / KNY - 1, y = ny0 + r % KNY - 1;
-            if (x < 0 || y < 0 || x >= (int)N.X || y >= (int)N.Y) continue;
-            const uint32_t* row = N.keys + vf_kidx(N, x, y, 0);
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(row + za));
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(row + zm));
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(row + zb));
-          }
-        }
-      }
-    }
+    if (nx != 0xFFFFFFFFu && lane == 0) *pre = nx;
   } else {
     constexpr int SU = 6;
     const size_t nk = (size_t)J.X * J.Y * J.Zk;
