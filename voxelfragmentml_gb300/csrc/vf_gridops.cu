@@ -736,13 +736,27 @@ __global__ void __launch_bounds__(256) k_pack16(const JobDesc* jobs, int njobs) 
     const unsigned long long total = (unsigned long long)J.X * J.Y * J.Z;
     const unsigned long long units = total / 8;
     uint4* d = reinterpret_cast<uint4*>(J.out);
-    for (unsigned long long u = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; u < units;
-         u += (unsigned long long)gridDim.x * blockDim.x) {
-      const unsigned long long e0 = 8 * u, e1 = e0 + 4;
-      const unsigned long long r0 = e0 / J.Z, r1 = e1 / J.Z;
-      const uint2 a = *reinterpret_cast<const uint2*>(J.grid + r0 * J.Zp + (e0 - r0 * J.Z));
-      const uint2 b = *reinterpret_cast<const uint2*>(J.grid + r1 * J.Zp + (e1 - r1 * J.Z));
-      d[u] = make_uint4(a.x, a.y, b.x, b.y);
+    const uint32_t Z = J.Z;
+    if (total < (1ull << 32)) {
+      // one 32-bit division per unit; the second half's row follows from the first
+      for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < (uint32_t)units;
+           u += gridDim.x * blockDim.x) {
+        const uint32_t e0 = 8 * u;
+        const uint32_t r0 = e0 / Z, o0 = e0 - r0 * Z;
+        const uint32_t r1 = o0 + 4 < Z ? r0 : r0 + 1, o1 = o0 + 4 < Z ? o0 + 4 : o0 + 4 - Z;
+        const uint2 a = *reinterpret_cast<const uint2*>(J.grid + (size_t)r0 * J.Zp + o0);
+        const uint2 b = *reinterpret_cast<const uint2*>(J.grid + (size_t)r1 * J.Zp + o1);
+        d[u] = make_uint4(a.x, a.y, b.x, b.y);
+      }
+    } else {
+      for (unsigned long long u = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; u < units;
+           u += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned long long e0 = 8 * u, e1 = e0 + 4;
+        const unsigned long long r0 = e0 / Z, r1 = e1 / Z;
+        const uint2 a = *reinterpret_cast<const uint2*>(J.grid + r0 * J.Zp + (e0 - r0 * Z));
+        const uint2 b = *reinterpret_cast<const uint2*>(J.grid + r1 * J.Zp + (e1 - r1 * Z));
+        d[u] = make_uint4(a.x, a.y, b.x, b.y);
+      }
     }
     // the last total % 8 labels (a multiple of 4)
     if (blockIdx.x == 0 && threadIdx.x == 0 && (total & 7u)) {
