@@ -718,19 +718,20 @@ __global__ void __launch_bounds__(256) k_init_keys(const JobDesc* jobs, const ui
     const uint32_t x = bx * VF_BX + threadIdx.x / VF_BY, y = by * VF_BY + threadIdx.x % VF_BY;
     const uint32_t z0 = bz * VF_BZ;
     if (x >= J.X || y >= J.Y) continue;
-    const uint2* g = reinterpret_cast<const uint2*>(J.grid + vf_gidx(J, x, y, z0));
+    const uint4* g = reinterpret_cast<const uint4*>(J.grid + vf_gidx(J, x, y, z0));
     uint4* d = reinterpret_cast<uint4*>(J.keys + vf_kidx(J, x, y, z0));
     const uint32_t nq = min((uint32_t)VF_BZ, J.Zk - z0) / 4;
-    // the row's label loads first, then the key stores (Zp >= Zk, both
-    // multiples of 4: 4 labels = one 8-byte word)
-    uint2 a[VF_BZ / 4];
+    // the row's label loads first (8 labels per 16-byte load: Zp >= Zk and Zp
+    // is a multiple of 8), then the key stores (4 keys per 16-byte store)
+    uint4 a[VF_BZ / 8];
 #pragma unroll
-    for (uint32_t q = 0; q < VF_BZ / 4; ++q) a[q] = q < nq ? g[q] : make_uint2(0, 0);
+    for (uint32_t q = 0; q < VF_BZ / 8; ++q) a[q] = 2 * q < nq ? g[q] : make_uint4(0, 0, 0, 0);
 #pragma unroll
     for (uint32_t q = 0; q < VF_BZ / 4; ++q) {
       if (q >= nq) break;
-      __stcg(d + q, make_uint4((a[q].x & 0xFFFFu) ? 1u : 0u, (a[q].x >> 16) ? 1u : 0u,
-                               (a[q].y & 0xFFFFu) ? 1u : 0u, (a[q].y >> 16) ? 1u : 0u));
+      const uint32_t lo = (q & 1) ? a[q >> 1].z : a[q >> 1].x, hi = (q & 1) ? a[q >> 1].w : a[q >> 1].y;
+      __stcg(d + q, make_uint4((lo & 0xFFFFu) ? 1u : 0u, (lo >> 16) ? 1u : 0u,
+                               (hi & 0xFFFFu) ? 1u : 0u, (hi >> 16) ? 1u : 0u));
     }
   }
 }
@@ -787,15 +788,33 @@ __global__ void k_seed_keys(const JobDesc* jobs, JobState* st, int njobs, uint32
 __global__ void __launch_bounds__(256) k_finalize(const JobDesc* jobs, const JobState* st,
                                                   const uint32_t* list, const uint32_t* count,
                                                   const uint32_t* brick_job, int pass2) {
+  // label of each seed slot for the job of the current brick (reloaded when
+  // the job changes): the seed's label (pass 1) or the pass-2 rank value,
+  // reduced to the fragment byte unless the sub-seed prefixes are kept
+  __shared__ uint16_t lab[4096];
+  __shared__ int cached;
+  if (threadIdx.x == 0) cached = -1;
+  __syncthreads();
   const uint32_t n = *count;
   for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
     const uint32_t b = list[it];
     const uint32_t j = brick_job[b];
     const JobDesc& J = jobs[j];
-    if (!J.active) continue;
+    if (!J.active) continue;  // uniform across the CTA
     const JobState& s = st[j];
     if (pass2 && !s.has_prefix) continue;  // keys of every prefix job are final here
-    const bool keep_prefix = !pass2 && s.has_prefix;
+    if ((int)j != cached) {  // uniform: cached changes only between barriers
+      __syncthreads();
+      const bool keep_prefix = !pass2 && s.has_prefix;
+      const uint32_t nl = pass2 ? 256u : min(s.nseeds, 4096u);
+      for (uint32_t k = threadIdx.x; k < nl; k += blockDim.x) {
+        uint32_t v = pass2 ? s.rank_value[k] : J.seeds[4 * k + 3];
+        if (!keep_prefix) v &= 0xFFu;
+        lab[k] = (uint16_t)v;
+      }
+      if (threadIdx.x == 0) cached = (int)j;
+      __syncthreads();
+    }
     const uint32_t lb = b - J.brick_base;
     const uint32_t bz = lb % J.nbz, by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
     const uint32_t x = bx * VF_BX + threadIdx.x / VF_BY, y = by * VF_BY + threadIdx.x % VF_BY;
@@ -813,26 +832,17 @@ __global__ void __launch_bounds__(256) k_finalize(const JobDesc* jobs, const Job
     for (uint32_t q = 0; q < VF_BZ / 4; ++q) {
       if (q >= nq) break;
       const uint32_t ks[4] = {k4[q].x, k4[q].y, k4[q].z, k4[q].w};
-      uint32_t lab[4];
+      uint32_t lv[4];
 #pragma unroll
       for (int h = 0; h < 4; ++h) {
         const uint32_t key = ks[h];
-        uint32_t v;
-        if (key >= VF_KEY_MIN_REACHED) {
-          const uint32_t slot = (~key) & 0xFFFu;
-          v = pass2 ? s.rank_value[slot] : J.seeds[4 * slot + 3];
-          if (!keep_prefix) v &= 0xFFu;
-        } else {
-          v = key;  // 0 EMPTY, 1 FREE
-        }
-        lab[h] = v;
+        // reached: the slot's label; else 0 EMPTY, 1 FREE
+        lv[h] = key >= VF_KEY_MIN_REACHED ? (uint32_t)lab[(~key) & 0xFFFu] : key;
       }
-      g[q] = make_uint2(lab[0] | (lab[1] << 16), lab[2] | (lab[3] << 16));
+      g[q] = make_uint2(lv[0] | (lv[1] << 16), lv[2] | (lv[3] << 16));
     }
   }
 }
-
-// ---- sub-seed prefix competition: component-wise minimum prefix -----------
 __global__ void __launch_bounds__(256) k_competition(const JobDesc* jobs, JobState* st,
                                                      const uint32_t* list, const uint32_t* count,
                                                      const uint32_t* brick_job) {
