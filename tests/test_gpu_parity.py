@@ -496,3 +496,47 @@ def test_smallest_grid_and_extreme_labels(vf, ctx):
     assert np.array_equal(g.data(), exp)
     with pytest.raises(vf.VFError):
         vf.RegularGrid((1, 8, 8), None, None, ctx)  # dims below 2
+
+
+def _serpentine(n_path, length=1450):
+    """A one-voxel corridor in the x = 0 layer of a (2, rows, length) grid
+    that runs along z and turns at alternate ends: n_path voxels, the geodesic
+    distance from its first voxel to its last is n_path - 1.  (Along z a brick
+    visit carries the front across the whole brick in one sweep.)"""
+    rows = 2 * (n_path // (length + 1) + 2)
+    occ = np.zeros((2, rows, length), np.uint16)
+    k, y = 0, 0
+    while k < n_path:
+        take = min(length, n_path - k)
+        if (y // 2) % 2 == 0:
+            occ[0, y, :take] = 1
+        else:
+            occ[0, y, length - take:] = 1
+        k += take
+        if k < n_path:  # the connector to the next corridor row
+            occ[0, y + 1, length - 1 if (y // 2) % 2 == 0 else 0] = 1
+            k += 1
+        y += 2
+    return occ
+
+
+def test_flood_distance_limit(vf, ctx):
+    """Keys hold geodesic distances up to 2^20 - 2: a corridor whose far end
+    sits exactly at that distance floods like the oracle (the distance-limit
+    check runs and finds nothing); one voxel further is VF_ERR_RANGE."""
+    limit = (1 << 20) - 2
+    seeds = np.array([[0, 0, 0, 2]], np.uint32)
+    occ = _serpentine(limit + 1)
+    g = vf.RegularGrid(occ.shape, None, None, ctx)
+    g.upload(occ)
+    fr = vf.FloodFracturer()
+    fr.setDistanceFunction(vf.MANHATTAN)
+    fr.build(g, seeds)
+    exp, _ = O.flood(occ, seeds, vf.MANHATTAN)
+    assert np.array_equal(g.data(), exp)
+    occ = _serpentine(limit + 2)
+    g = vf.RegularGrid(occ.shape, None, None, ctx)
+    g.upload(occ)
+    with pytest.raises(vf.VFError) as e:
+        fr.build(g, seeds)
+    assert e.value.status == vf.ERR_RANGE
