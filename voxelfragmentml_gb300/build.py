@@ -69,7 +69,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_v: bool = False) -> 
                 print(err, file=sys.stderr)
     objs = [o for o, _ in results]
     tmp = LIB + ".tmp"
-    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"]
+    cmd = [cc, *ARCH, "-shared", "-Xlinker", "--no-undefined", "-o", tmp, *objs, "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

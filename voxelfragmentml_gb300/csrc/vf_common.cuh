@@ -88,6 +88,7 @@ struct JobDesc {
   // or device memory; null = copy-engine download) and first global row
   uint16_t* out;
   unsigned long long row_base;
+  uint32_t out_dma;  // out is the device staging buffer of the DMA download
   // stage selection bits for the kernel that receives this table
   uint32_t active;
   float* emask;         // erosion mask (k^3 floats)

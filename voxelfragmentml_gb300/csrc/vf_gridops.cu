@@ -729,10 +729,13 @@ __global__ void __launch_bounds__(256) k_counts(const JobDesc* jobs, JobState* s
 // (8 labels); each unit is two 8-byte halves, and a half never crosses a row
 // (Z % 4 == 0), so it is one 8-byte load from row (e / Z) at z = e % Z.  Units
 // go to consecutive lanes, so every warp store is 512 contiguous bytes.
+// Labels into a caller's buffer the GPU writes directly (mapped pinned host
+// memory): 16-byte units that may straddle rows (Z a multiple of 4), one
+// 32-bit division per unit.
 __global__ void __launch_bounds__(256) k_pack16(const JobDesc* jobs, int njobs) {
   for (int j = blockIdx.y; j < njobs; j += gridDim.y) {
     const JobDesc& J = jobs[j];
-    if (!J.out || (J.Z & 3u) || (reinterpret_cast<uintptr_t>(J.out) & 15u)) continue;
+    if (!J.out || J.out_dma || (J.Z & 3u) || (reinterpret_cast<uintptr_t>(J.out) & 15u)) continue;
     const unsigned long long total = (unsigned long long)J.X * J.Y * J.Z;
     const unsigned long long units = total / 8;
     uint4* d = reinterpret_cast<uint4*>(J.out);
@@ -769,6 +772,10 @@ __global__ void __launch_bounds__(256) k_pack16(const JobDesc* jobs, int njobs) 
 // label download: one warp per (x, y) row, the final grid (row pitch Zp) into
 // the caller's buffer (row pitch Z); 8-byte stores when Z % 4 == 0 and the
 // destination is 8-byte aligned
+// Labels without the z padding into J.out (a device staging buffer, or a
+// caller's buffer k_pack16 does not take): one warp per (x, y) row of any job (rows of all jobs are
+// numbered consecutively, row_base per job), copied with the widest access
+// the row's alignment allows.
 __global__ void __launch_bounds__(256) k_pack(const JobDesc* jobs, int njobs,
                                               unsigned long long total_rows) {
   const int lane = threadIdx.x & 31;
@@ -782,16 +789,26 @@ __global__ void __launch_bounds__(256) k_pack(const JobDesc* jobs, int njobs,
     }
     const JobDesc& J = jobs[lo];
     if (!J.out) continue;
-    if ((J.Z & 3u) == 0u && (reinterpret_cast<uintptr_t>(J.out) & 15u) == 0u) continue;  // k_pack16
+    if (!J.out_dma && (J.Z & 3u) == 0u && (reinterpret_cast<uintptr_t>(J.out) & 15u) == 0u) continue;  // k_pack16
     const unsigned long long lr = r - J.row_base;
-    const uint16_t* src = J.grid + lr * J.Zp;
+    const uint16_t* src = J.grid + lr * J.Zp;  // 16-byte aligned (Zp is a multiple of 8)
     uint16_t* dst = J.out + lr * J.Z;
-    if ((J.Z & 3u) == 0u && ((reinterpret_cast<uintptr_t>(J.out) & 7u) == 0u)) {
+    const uintptr_t da = reinterpret_cast<uintptr_t>(dst);
+    const uint32_t Z = J.Z;
+    if ((Z & 7u) == 0u && (da & 15u) == 0u) {
+      const uint4* s4 = reinterpret_cast<const uint4*>(src);
+      uint4* d4 = reinterpret_cast<uint4*>(dst);
+      for (uint32_t q = lane; q < Z / 8; q += 32) d4[q] = __ldcs(s4 + q);
+    } else if ((Z & 3u) == 0u && (da & 7u) == 0u) {
       const uint2* s2 = reinterpret_cast<const uint2*>(src);
       uint2* d2 = reinterpret_cast<uint2*>(dst);
-      for (uint32_t q = lane; q < J.Z / 4; q += 32) d2[q] = __ldcs(s2 + q);
+      for (uint32_t q = lane; q < Z / 4; q += 32) d2[q] = __ldcs(s2 + q);
+    } else if ((Z & 1u) == 0u && (da & 3u) == 0u) {
+      const uint32_t* s1 = reinterpret_cast<const uint32_t*>(src);
+      uint32_t* d1 = reinterpret_cast<uint32_t*>(dst);
+      for (uint32_t q = lane; q < Z / 2; q += 32) d1[q] = __ldcs(s1 + q);
     } else {
-      for (uint32_t q = lane; q < J.Z; q += 32) dst[q] = src[q];
+      for (uint32_t q = lane; q < Z; q += 32) dst[q] = src[q];
     }
   }
 }

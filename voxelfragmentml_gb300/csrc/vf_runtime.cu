@@ -451,8 +451,10 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
     d.out = nullptr;
     d.row_base = sz.rows;
     sz.rows += (uint64_t)p.X * p.Y;
+    d.out_dma = 0;
     if (p.dma) {
       d.out = static_cast<uint16_t*>(stage_out.p) + p.o_out;
+      d.out_dma = 1;
       p.packed = true;
     } else if (j.out_labels && ((uintptr_t)j.out_labels & 1) == 0) {
       cudaPointerAttributes at;
