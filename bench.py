@@ -179,11 +179,11 @@ def reference_arm(args):
 
 # DRAM bytes per staged flood brick visit: dram__bytes_read.sum +
 # dram__bytes_write.sum of one k_relax launch over the first 48 jobs of
-# mixed-256 (ncu, one GB300: 2316051712 + 204019200 B), divided by the 49728
-# visits of that launch that staged their brick (52021 visits, 2293 found
+# mixed-256 (ncu, one GB300: 2309600768 + 203521792 B), divided by the 49843
+# visits of that launch that staged their brick (52099 visits, 2256 found
 # nothing new).  The roofline's `traffic` is this figure times the staged
 # visits of the timed launch.
-K_RELAX_DRAM_BYTES_PER_VISIT = (2316051712 + 204019200) / 49728
+K_RELAX_DRAM_BYTES_PER_VISIT = (2309600768 + 203521792) / 49843
 
 
 def main():
