@@ -336,7 +336,9 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
     p.o_verts = sz.verts; sz.verts += align_up((size_t)j.nverts * 3, 64);
     p.o_faces = sz.faces; sz.faces += align_up((size_t)j.nfaces * 3, 64);
     p.o_emask = sz.emask; sz.emask += align_up(p.emask.size(), 64);
-    p.dma = dma_download && j.out_labels != nullptr;
+    // rows without z padding (Z a multiple of 8) are already the host layout:
+    // the copy engine takes them from the label grid itself
+    p.dma = dma_download && j.out_labels != nullptr && p.Zp != p.Z;
     p.o_out = sz.out;
     if (p.dma) sz.out += align_up(vox * p.Z, 128);  // 256-byte aligned u16 rows
     sz.bricks += p.nbricks;
@@ -456,7 +458,7 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
       d.out = static_cast<uint16_t*>(stage_out.p) + p.o_out;
       d.out_dma = 1;
       p.packed = true;
-    } else if (j.out_labels && ((uintptr_t)j.out_labels & 1) == 0) {
+    } else if (!dma_download && j.out_labels && ((uintptr_t)j.out_labels & 1) == 0) {
       cudaPointerAttributes at;
       if (cudaPointerGetAttributes(&at, j.out_labels) == cudaSuccess && at.devicePointer &&
           at.type != cudaMemoryTypeUnregistered) {

@@ -67,9 +67,10 @@ struct Batch {
   DevBuf tables, state, brick_job, live, list, lcount, q[3], scal, epoch, fdir, front[2];
   DevBuf pcnt, pbase, psums, srec;  // flattened per-face work lists, shell setup
   DevBuf stage_out;  // packed labels of the DMA download
-  // download by DMA: labels are packed into a device staging buffer and
-  // copied to out_labels by the copy engine (no kernel writes host memory,
-  // so the download of one batch overlaps the kernels of the next)
+  // download by DMA: labels are copied to out_labels by the copy engine, from
+  // the label grid when its rows have no padding, else packed first into a
+  // device staging buffer (no kernel writes host memory, so the download of
+  // one batch overlaps the kernels of the next)
   bool dma_download = false;
   void* h_tables = nullptr;  // pinned staging
   size_t h_tables_cap = 0;
