@@ -708,30 +708,48 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
 // keys from the label grid: EMPTY -> 0, occupied -> 1 (unreached)
 __global__ void __launch_bounds__(256) k_init_keys(const JobDesc* jobs, const uint32_t* list,
                                                    const uint32_t* count, const uint32_t* brick_job) {
+  // IB live bricks per CTA and iteration, one row of each per thread: the
+  // label loads of all of them are in flight before the key stores
+  constexpr int IB = 2;
   const uint32_t n = *count;
-  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
-    const uint32_t b = list[it];
-    const JobDesc& J = jobs[brick_job[b]];
-    if (!J.active) continue;
-    const uint32_t lb = b - J.brick_base;
-    const uint32_t bz = lb % J.nbz, by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
-    const uint32_t x = bx * VF_BX + threadIdx.x / VF_BY, y = by * VF_BY + threadIdx.x % VF_BY;
-    const uint32_t z0 = bz * VF_BZ;
-    if (x >= J.X || y >= J.Y) continue;
-    const uint4* g = reinterpret_cast<const uint4*>(J.grid + vf_gidx(J, x, y, z0));
-    uint4* d = reinterpret_cast<uint4*>(J.keys + vf_kidx(J, x, y, z0));
-    const uint32_t nq = min((uint32_t)VF_BZ, J.Zk - z0) / 4;
-    // the row's label loads first (8 labels per 16-byte load: Zp >= Zk and Zp
-    // is a multiple of 8), then the key stores (4 keys per 16-byte store)
-    uint4 a[VF_BZ / 8];
+  for (uint32_t i0 = blockIdx.x * IB; i0 < n; i0 += gridDim.x * IB) {
+    uint4 a[IB][VF_BZ / 8];
+    uint4* d[IB];
+    uint32_t nq[IB];
 #pragma unroll
-    for (uint32_t q = 0; q < VF_BZ / 8; ++q) a[q] = 2 * q < nq ? g[q] : make_uint4(0, 0, 0, 0);
+    for (int k = 0; k < IB; ++k) {
+      d[k] = nullptr;
+      nq[k] = 0;
 #pragma unroll
-    for (uint32_t q = 0; q < VF_BZ / 4; ++q) {
-      if (q >= nq) break;
-      const uint32_t lo = (q & 1) ? a[q >> 1].z : a[q >> 1].x, hi = (q & 1) ? a[q >> 1].w : a[q >> 1].y;
-      __stcg(d + q, make_uint4((lo & 0xFFFFu) ? 1u : 0u, (lo >> 16) ? 1u : 0u,
-                               (hi & 0xFFFFu) ? 1u : 0u, (hi >> 16) ? 1u : 0u));
+      for (int q = 0; q < VF_BZ / 8; ++q) a[k][q] = make_uint4(0, 0, 0, 0);
+      if (i0 + k >= n) continue;
+      const uint32_t b = list[i0 + k];
+      const JobDesc& J = jobs[brick_job[b]];
+      if (!J.active) continue;
+      const uint32_t lb = b - J.brick_base;
+      const uint32_t bz = lb % J.nbz, by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
+      const uint32_t x = bx * VF_BX + threadIdx.x / VF_BY, y = by * VF_BY + threadIdx.x % VF_BY;
+      const uint32_t z0 = bz * VF_BZ;
+      if (x >= J.X || y >= J.Y) continue;
+      // 8 labels per 16-byte load (Zp >= Zk and Zp is a multiple of 8)
+      const uint4* g = reinterpret_cast<const uint4*>(J.grid + vf_gidx(J, x, y, z0));
+      d[k] = reinterpret_cast<uint4*>(J.keys + vf_kidx(J, x, y, z0));
+      nq[k] = min((uint32_t)VF_BZ, J.Zk - z0) / 4;
+#pragma unroll
+      for (uint32_t q = 0; q < VF_BZ / 8; ++q)
+        if (2 * q < nq[k]) a[k][q] = g[q];
+    }
+#pragma unroll
+    for (int k = 0; k < IB; ++k) {
+      if (!d[k]) continue;
+#pragma unroll
+      for (uint32_t q = 0; q < VF_BZ / 4; ++q) {
+        if (q >= nq[k]) break;
+        const uint4 w = a[k][q >> 1];
+        const uint32_t lo = (q & 1) ? w.z : w.x, hi = (q & 1) ? w.w : w.y;
+        __stcg(d[k] + q, make_uint4((lo & 0xFFFFu) ? 1u : 0u, (lo >> 16) ? 1u : 0u,
+                                    (hi & 0xFFFFu) ? 1u : 0u, (hi >> 16) ? 1u : 0u));
+      }
     }
   }
 }
@@ -986,7 +1004,7 @@ static inline int brick_grid(uint32_t max_count) {
 void flood_init_keys(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
                      const uint32_t* count, uint32_t max_count, const uint32_t* brick_job,
                      const uint8_t*) {
-  if (max_count) k_init_keys<<<brick_grid(max_count), 256, 0, st>>>(dj, list, count, brick_job);
+  if (max_count) k_init_keys<<<brick_grid((max_count + 1) / 2), 256, 0, st>>>(dj, list, count, brick_job);
 }
 
 void flood_seed_bricks(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs, uint8_t* live,
