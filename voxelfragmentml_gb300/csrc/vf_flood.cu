@@ -13,14 +13,16 @@
 //   key(v) <- max(key(v), max_{u in N(v)} key(u) - 4096)
 //
 // Bricks of 16x16x32 voxels are relaxed to local convergence in shared
-// memory (many BFS waves per visit: each sweep recomputes only the rows next
-// to a change and runs forward/backward along the 32-voxel z rows), and a
-// brick whose face voxels changed
-// puts its neighbours on the next pass's queue (deduplicated by a pass
-// epoch, appended with warp ballot/popc).  All passes of all jobs of a batch
-// run in ONE cooperative persistent kernel; passes are separated by a
-// software grid barrier whose spin is bounded (it sets an error word and the
-// kernel returns instead of hanging).
+// memory (many BFS waves per visit).  A sweep runs only the rows next to new
+// halo data (sweep 0, from the brick's change record) or to a row that
+// changed in the previous sweep, compacted onto the lowest warps; a row
+// update is one forward and one backward pass along its 32-voxel z row.  A
+// brick whose boundary voxels changed records what changed in its
+// neighbours' change records and puts them on the next pass's queue
+// (deduplicated by a pass epoch, appended with warp ballot/popc).  All passes
+// of all jobs of a batch run in ONE cooperative persistent kernel; passes are
+// separated by a software grid barrier whose spin is bounded (it sets an
+// error word and the kernel returns instead of hanging).
 //
 // Sub-seed prefixes (extra seeds merged into fragments, Seeder.cpp:115-152)
 // then go through the reference's competition and disjoint cleanup
