@@ -135,6 +135,42 @@ vf_status vf_grid_download(vf_grid* g, uint16_t* host_grid);
  * grid has 2^32 voxels or more. */
 vf_status vf_grid_export_rle(vf_grid* g, uint8_t* out, size_t cap, size_t* written);
 
+/* ---- fragment meshes (RegularGrid::toTriangleMesh) -----------------------
+ * Smoothing of MarchingCubes::triangulateFieldGPU (MarchingCubes.cpp:
+ * 396-401): iterations over the non-boundary, then the boundary vertices. */
+typedef struct vf_mc_params {
+  uint32_t nonboundary_iterations; /* maxVoxels * _nonBoundaryMCIterations */
+  float nonboundary_weight;        /* _nonBoundaryMCWeight */
+  uint32_t boundary_iterations;    /* maxVoxels * _boundaryMCIterations */
+  float boundary_weight;           /* _boundaryMCWeight */
+} vf_mc_params;
+/* FractureParameters defaults (FractureParameters.h:93-94, 109-110):
+ * iterations = (unsigned)(max_voxels * 0.048f), weights 0.9 and 0.2;
+ * max_voxels is the largest voxelization size. */
+void vf_mc_params_default(uint32_t max_voxels, vf_mc_params* p);
+
+/* RegularGrid::toTriangleMesh (RegularGrid.cpp:443-486): one marching-cubes
+ * mesh per fragment value (label & 0x7FFF > 1, ascending), the field
+ * "label == value" on the grid padded by one FREE voxel (MarchingCubes::
+ * setGrid), vertices fused, moved by the grid's box (s = size / dims,
+ * p * s + min - s), face flags = max of vertex flags, then Laplacian
+ * smoothing.  p = NULL: vf_mc_params_default(max(dims)).  The meshes stay on
+ * the device; *nmeshes, *nverts and *nfaces give their sizes.  The reference
+ * leaves vertex and face order to GPU atomics; here vertices follow the
+ * fragment voxel the vertex's edge leaves (x-major) then the direction
+ * -x,+x,-y,+y,-z,+z, faces follow the marched cell (x-major) then the case
+ * table, and a vertex is a boundary vertex when any triangle using it is. */
+vf_status vf_grid_triangulate(vf_grid* g, const vf_mc_params* p, uint32_t* nmeshes,
+                              uint64_t* nverts, uint64_t* nfaces);
+/* The meshes of the last vf_grid_triangulate, to host memory (any pointer may
+ * be NULL): values[nmeshes]; vert_offsets / face_offsets [nmeshes + 1], mesh
+ * i = vertices [vert_offsets[i], vert_offsets[i+1]); verts 4 floats per vertex
+ * (x, y, z, boundary 0/1); faces 4 uint32 per face (three vertex indices
+ * within the mesh, boundary 0/1) -- the vec4 / uvec4 layouts CADModel::insert
+ * receives (MarchingCubes.cpp:403-406). */
+vf_status vf_grid_meshes(vf_grid* g, uint16_t* values, uint64_t* vert_offsets,
+                         uint64_t* face_offsets, float* verts, uint32_t* faces);
+
 /* RegularGrid::fill(Model3D*) (RegularGrid.cpp:173-212): occupancy = FP32
  * tri-box SAT shell (Intersections3D.h:204-258) OR tetra-parity interior
  * (Tetravoxelizer.cpp:42-92, 198-315).  verts: 3 floats per vertex, faces:

@@ -24,7 +24,9 @@ def build(force: bool = False) -> str:
     if force or not os.path.exists(_LIB_PATH) or (
             os.path.getmtime(_LIB_PATH) < max(
                 os.path.getmtime(os.path.join(_HERE, f))
-                for f in ("vf_oracle.c", "vf_oracle.h", "Makefile"))):
+                for f in ("vf_oracle.c", "vf_oracle_mesh.c", "vf_oracle.h", "Makefile",
+                          os.path.join("..", "voxelfragmentml_gb300", "csrc",
+                                       "vf_mc_table.h")))):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
 
@@ -66,6 +68,8 @@ def lib():
             "vfo_count_values": (i32, [P, u32, u32, u32, P, u32, P]),
             "vfo_run_job": (i32, [P, u32, P, u32, u32, u32, u32, P, P, P, P, P, u32, P, P]),
             "vfo_rle_encode": (C.c_size_t, [P, u32, u32, u32, P, C.c_size_t]),
+            "vfo_triangulate": (i32, [P, u32, u32, u32, P, P, u32, f32, u32, f32,
+                                      P, P, P, P, P, P, P, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(_lib, name)
@@ -222,3 +226,23 @@ def rle_encode(grid):
     out = np.zeros(n, np.uint8)
     lib().vfo_rle_encode(_p(g), *g.shape, _p(out), n)
     return out.tobytes()
+
+
+def triangulate(grid, aabb_min, aabb_max, nb_iters=0, nb_weight=0.9, b_iters=0, b_weight=0.2):
+    """RegularGrid::toTriangleMesh: (values, vert_off, face_off, verts (V, 4)
+    float32, faces (T, 4) uint32), meshes concatenated in value order."""
+    g = np.ascontiguousarray(grid, dtype=np.uint16)
+    X, Y, Z = g.shape
+    lo, hi = _f3(aabb_min), _f3(aabb_max)
+    F, V, T = C.c_uint32(), C.c_uint64(), C.c_uint64()
+    args = (_p(g), X, Y, Z, _p(lo), _p(hi), nb_iters, nb_weight, b_iters, b_weight,
+            C.byref(F), C.byref(V), C.byref(T))
+    _check(lib().vfo_triangulate(*args, None, None, None, None, None), "triangulate")
+    vals = np.zeros(F.value, np.uint16)
+    vo = np.zeros(F.value + 1, np.uint64)
+    fo = np.zeros(F.value + 1, np.uint64)
+    verts = np.zeros((V.value, 4), np.float32)
+    faces = np.zeros((T.value, 4), np.uint32)
+    _check(lib().vfo_triangulate(*args, _p(vals), _p(vo), _p(fo), _p(verts), _p(faces)),
+           "triangulate")
+    return vals, vo, fo, verts, faces

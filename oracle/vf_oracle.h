@@ -144,6 +144,19 @@ int vfo_run_job(const float* verts, uint32_t nverts, const uint32_t* faces,
 size_t vfo_rle_encode(const uint16_t* grid, uint32_t X, uint32_t Y, uint32_t Z,
                       uint8_t* out, size_t cap);
 
+/* RegularGrid::toTriangleMesh (RegularGrid.cpp:443-486): one smoothed
+ * marching-cubes mesh per fragment value (label & 0x7FFF > 1, ascending),
+ * vf_oracle_mesh.c.  Sizes go to *nmeshes / *nverts / *nfaces; with values
+ * given, the meshes are written too: values[F], vert_off[F+1],
+ * face_off[F+1], verts 4 floats (x, y, z, boundary) and faces 4 uint32
+ * (three mesh-local vertex indices, boundary) per element. */
+int vfo_triangulate(const uint16_t* grid, uint32_t X, uint32_t Y, uint32_t Z,
+                    const float amin[3], const float amax[3], uint32_t nb_iters,
+                    float nb_weight, uint32_t b_iters, float b_weight,
+                    uint32_t* nmeshes, uint64_t* nverts, uint64_t* nfaces,
+                    uint16_t* values, uint64_t* vert_off, uint64_t* face_off,
+                    float* verts, uint32_t* faces);
+
 #ifdef __cplusplus
 }
 #endif

@@ -128,6 +128,11 @@ EXPORTS = {
     "vf_ctx_last_graph": (C.c_int, [C.c_void_p, C.c_void_p]),
     "vf_ctx_flood_pass_sizes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_grid_export_rle": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "vf_mc_params_default": (None, [C.c_uint32, C.c_void_p]),
+    "vf_grid_triangulate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_void_p]),
+    "vf_grid_meshes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                 C.c_void_p]),
     "vf_ctx_set_tuning": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_ctx_get_tuning": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
@@ -269,6 +274,32 @@ def default_context() -> Context:
     return _default_ctx
 
 
+class MCParams(C.Structure):
+    """vf_mc_params: the smoothing fields of FractureParameters used by
+    MarchingCubes::triangulateFieldGPU (MarchingCubes.cpp:400-401)."""
+    _fields_ = [("nonboundary_iterations", C.c_uint32), ("nonboundary_weight", C.c_float),
+                ("boundary_iterations", C.c_uint32), ("boundary_weight", C.c_float)]
+
+    @classmethod
+    def default(cls, max_voxels: int) -> "MCParams":
+        p = cls()
+        lib().vf_mc_params_default(int(max_voxels), C.byref(p))
+        return p
+
+
+class FragmentMesh:
+    """One fragment's mesh as CADModel::insert receives it: vertices (V, 4)
+    float32 (x, y, z, boundary) and faces (F, 4) uint32 (three vertex
+    indices, boundary)."""
+
+    def __init__(self, value, vertices, faces):
+        self.value, self.vertices, self.faces = int(value), vertices, faces
+
+    def __repr__(self):
+        return (f"FragmentMesh(value={self.value}, vertices={len(self.vertices)}, "
+                f"faces={len(self.faces)})")
+
+
 class RegularGrid:
     """Device-resident uint16 label grid, x-major (RegularGrid.h:142-367)."""
 
@@ -349,6 +380,35 @@ class RegularGrid:
         occ = C.c_uint64()
         _check(lib().vf_count_values(self.h, _p(c), ncounts, C.byref(occ)))
         return c, occ.value
+
+    def triangulate(self, params: MCParams | None = None):
+        """vf_grid_triangulate: build every fragment's mesh on the device and
+        return (meshes, vertices, faces) counts."""
+        F, V, T = C.c_uint32(), C.c_uint64(), C.c_uint64()
+        _check(lib().vf_grid_triangulate(self.h, C.byref(params) if params is not None else None,
+                                         C.byref(F), C.byref(V), C.byref(T)))
+        self._mesh_sizes = (F.value, V.value, T.value)
+        return self._mesh_sizes
+
+    def meshes_arrays(self):
+        """The last triangulation as concatenated arrays: (values, vert_off,
+        face_off, verts (V, 4) float32, faces (T, 4) uint32)."""
+        F, V, T = self._mesh_sizes
+        vals = np.zeros(max(F, 1), np.uint16)
+        vo = np.zeros(F + 1, np.uint64)
+        fo = np.zeros(F + 1, np.uint64)
+        verts = np.zeros((V, 4), np.float32)
+        faces = np.zeros((T, 4), np.uint32)
+        _check(lib().vf_grid_meshes(self.h, _p(vals), _p(vo), _p(fo), _p(verts), _p(faces)))
+        return vals[:F], vo, fo, verts, faces
+
+    def toTriangleMesh(self, params: MCParams | None = None):
+        """RegularGrid::toTriangleMesh (RegularGrid.cpp:443-486): one smoothed
+        marching-cubes mesh per fragment value, in ascending value order."""
+        self.triangulate(params)
+        vals, vo, fo, verts, faces = self.meshes_arrays()
+        return [FragmentMesh(v, verts[vo[i]:vo[i + 1]], faces[fo[i]:fo[i + 1]])
+                for i, v in enumerate(vals)]
 
 
 class Seeder:

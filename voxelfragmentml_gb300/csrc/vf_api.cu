@@ -34,11 +34,28 @@ struct vf_ctx {
   vfr::Ctx c;
 };
 
+// device state of vf_grid_triangulate, kept for vf_grid_meshes
+struct MeshState {
+  vfr::DevBuf mask, vbase, rcnt, rbase, trcnt, tbase, sums, tot, present, dense, table, vkey, vown,
+      vflag, vperm, tmp, vinv, tkey, tv, tperm, hist, hbase, vert, gface, face, voff, foff, acc, err;
+  std::vector<uint16_t> values;
+  uint64_t V = 0, T = 0;
+  bool ready = false;
+  void release(vfr::Ctx& c) {
+    for (vfr::DevBuf* b : {&mask, &vbase, &rcnt, &rbase, &trcnt, &tbase, &sums, &tot, &present,
+                           &dense, &table, &vkey, &vown, &vflag, &vperm, &tmp, &vinv, &tkey, &tv,
+                           &tperm, &hist, &hbase, &vert, &gface, &face, &voff, &foff, &acc, &err})
+      c.free_buf(*b);
+    ready = false;
+  }
+};
+
 struct vf_grid {
   vf_ctx* ctx = nullptr;
   vfr::Batch b;
   vf_job job;
   std::vector<uint32_t> seeds;  // last seeds used by fracture_model
+  MeshState mesh;
 };
 
 extern "C" {
@@ -224,6 +241,7 @@ vf_status vf_grid_destroy(vf_grid* g) {
   if (!g) return VF_OK;
   cudaSetDevice(g->ctx->c.device);
   if (g->b.stream) cudaStreamSynchronize(g->b.stream);
+  g->mesh.release(g->ctx->c);
   g->b.release();
   delete g;
   return VF_OK;
@@ -300,6 +318,167 @@ vf_status vf_grid_export_rle(vf_grid* g, uint8_t* out, size_t cap, size_t* writt
   if (nruns) VF_CK(cudaMemcpyAsync(out + 12, B.rle_rec.p, 6 * (size_t)nruns, cudaMemcpyDeviceToHost, st));
   VF_CK(cudaStreamSynchronize(st));
   VF_CK(cudaGetLastError());
+  return VF_OK;
+}
+
+void vf_mc_params_default(uint32_t max_voxels, vf_mc_params* p) {
+  if (!p) return;
+  // MarchingCubes.cpp:400-401: iterations = maxVoxels * _(non)BoundaryMCIterations,
+  // converted to unsigned; FractureParameters.h:93-94, 109-110
+  p->nonboundary_iterations = (uint32_t)((float)max_voxels * 0.048f);
+  p->nonboundary_weight = 0.9f;
+  p->boundary_iterations = (uint32_t)((float)max_voxels * 0.048f);
+  p->boundary_weight = 0.2f;
+}
+
+vf_status vf_grid_triangulate(vf_grid* g, const vf_mc_params* mp, uint32_t* nmeshes,
+                              uint64_t* nverts, uint64_t* nfaces) {
+  if (!g) return fail(VF_ERR_INVALID, "grid is NULL");
+  vf_mc_params dp;
+  const uint32_t* d = g->job.dims;
+  if (!mp) {
+    vf_mc_params_default(std::max(d[0], std::max(d[1], d[2])), &dp);
+    mp = &dp;
+  }
+  cudaSetDevice(g->ctx->c.device);
+  vfr::Ctx& c = g->ctx->c;
+  vfr::Batch& B = g->b;
+  MeshState& M = g->mesh;
+  M.ready = false;
+  const vfr::JobPlan& p = B.plans[0];
+  const uint64_t rows = (uint64_t)p.X * p.Y, nvox = rows * p.Z;
+  const uint64_t crows = (uint64_t)(p.X + 1) * (p.Y + 1);
+  if (nvox >= 0xFFFFFFFFull) return fail(VF_ERR_RANGE, "triangulate: grids of 2^32 voxels or more");
+  cudaStream_t st = B.stream;
+  const int nsm = c.num_sms;
+  const vfk::MeshGrid G{static_cast<const uint16_t*>(B.grid0.p), p.X, p.Y, p.Z, p.Zp};
+  vf_status s;
+  if ((s = c.alloc(M.mask, nvox)) || (s = c.alloc(M.vbase, nvox * 4)) ||
+      (s = c.alloc(M.rcnt, rows * 4)) || (s = c.alloc(M.rbase, rows * 8)) ||
+      (s = c.alloc(M.trcnt, crows * 4)) || (s = c.alloc(M.tbase, crows * 8)) ||
+      (s = c.alloc(M.tot, 64)) || (s = c.alloc(M.present, 32768)) ||
+      (s = c.alloc(M.dense, 32768 * 2)) || (s = c.alloc(M.table, 256 * 9)) ||
+      (s = c.alloc(M.err, 64)))
+    return s;
+  auto scan_scratch = [&](uint64_t n) { return c.alloc(M.sums, ((n + 1023) / 1024 + 2) * 8); };
+  if ((s = scan_scratch(std::max(rows, crows)))) return s;
+  unsigned long long tri[256];
+  uint8_t ntri[256];
+  vfk::mc_pack_table(tri, ntri);
+  unsigned long long* dtri = static_cast<unsigned long long*>(M.table.p);
+  uint8_t* dntri = reinterpret_cast<uint8_t*>(dtri + 256);
+  VF_CK(cudaMemcpyAsync(dtri, tri, sizeof(tri), cudaMemcpyHostToDevice, st));
+  VF_CK(cudaMemcpyAsync(dntri, ntri, sizeof(ntri), cudaMemcpyHostToDevice, st));
+  VF_CK(cudaMemsetAsync(M.present.p, 0, 32768, st));
+  VF_CK(cudaMemsetAsync(M.err.p, 0, 4, st));
+  auto sums = static_cast<unsigned long long*>(M.sums.p);
+  auto tot = static_cast<unsigned long long*>(M.tot.p);
+  auto mask = static_cast<uint8_t*>(M.mask.p);
+  auto rbase = static_cast<unsigned long long*>(M.rbase.p);
+  auto tbase = static_cast<unsigned long long*>(M.tbase.p);
+  auto err = static_cast<uint32_t*>(M.err.p);
+  // counts: vertices (exposed faces of fragment voxels) and triangles
+  vfk::mc_vertex_count(st, G, mask, static_cast<uint32_t*>(M.rcnt.p),
+                       static_cast<uint8_t*>(M.present.p), nsm);
+  vfk::exclusive_scan(st, static_cast<uint32_t*>(M.rcnt.p), rbase, sums, (uint32_t)rows, tot);
+  vfk::mc_tri_count(st, G, dtri, dntri, static_cast<uint32_t*>(M.trcnt.p), nsm);
+  vfk::exclusive_scan(st, static_cast<uint32_t*>(M.trcnt.p), tbase, sums, (uint32_t)crows, tot + 1);
+  unsigned long long tots[2] = {0, 0};
+  std::vector<uint8_t> present(32768);
+  VF_CK(cudaMemcpyAsync(tots, tot, 16, cudaMemcpyDeviceToHost, st));
+  VF_CK(cudaMemcpyAsync(present.data(), M.present.p, 32768, cudaMemcpyDeviceToHost, st));
+  VF_CK(cudaStreamSynchronize(st));
+  VF_CK(cudaGetLastError());
+  const uint64_t V = tots[0], T = tots[1];
+  if (V >= 0xFFFFFFFFull || T >= 0xFFFFFFFFull)
+    return fail(VF_ERR_RANGE, "triangulate: 2^32 vertices or triangles or more");
+  std::vector<uint16_t> dense(32768, 0xFFFFu);
+  M.values.clear();
+  for (uint32_t v = 2; v < 32768; ++v)
+    if (present[v]) {
+      dense[v] = (uint16_t)M.values.size();
+      M.values.push_back((uint16_t)v);
+    }
+  const uint32_t F = (uint32_t)M.values.size();
+  VF_CK(cudaMemcpyAsync(M.dense.p, dense.data(), 32768 * 2, cudaMemcpyHostToDevice, st));
+  const uint16_t* ddense = static_cast<const uint16_t*>(M.dense.p);
+  const uint64_t V1 = std::max<uint64_t>(V, 1), T1 = std::max<uint64_t>(T, 1);
+  const uint64_t hw = std::max(vfk::split_hist_words(V), vfk::split_hist_words(T));
+  if ((s = c.alloc(M.vkey, V1 * 2)) || (s = c.alloc(M.vown, V1 * 8)) ||
+      (s = c.alloc(M.vflag, ((V1 + 31) / 32) * 4)) || (s = c.alloc(M.vperm, V1 * 4)) ||
+      (s = c.alloc(M.vinv, V1 * 4)) || (s = c.alloc(M.tmp, std::max(V1, T1) * 4)) ||
+      (s = c.alloc(M.tkey, T1 * 2)) || (s = c.alloc(M.tv, T1 * 16)) ||
+      (s = c.alloc(M.tperm, T1 * 4)) || (s = c.alloc(M.hist, hw * 4)) ||
+      (s = c.alloc(M.hbase, hw * 8)) || (s = scan_scratch(std::max<uint64_t>(hw, std::max(rows, crows)))) ||
+      (s = c.alloc(M.vert, V1 * 16)) || (s = c.alloc(M.gface, T1 * 16)) ||
+      (s = c.alloc(M.face, T1 * 16)) || (s = c.alloc(M.voff, (F + 1) * 8)) ||
+      (s = c.alloc(M.foff, (F + 1) * 8)) || (s = c.alloc(M.acc, V1 * 16)))
+    return s;
+  sums = static_cast<unsigned long long*>(M.sums.p);
+  auto vkey = static_cast<uint16_t*>(M.vkey.p);
+  auto vown = static_cast<unsigned long long*>(M.vown.p);
+  auto vflag = static_cast<uint32_t*>(M.vflag.p);
+  auto vperm = static_cast<uint32_t*>(M.vperm.p);
+  auto vinv = static_cast<uint32_t*>(M.vinv.p);
+  auto tkey = static_cast<uint16_t*>(M.tkey.p);
+  auto tv = static_cast<uint4*>(M.tv.p);
+  auto tperm = static_cast<uint32_t*>(M.tperm.p);
+  auto vert = static_cast<float4*>(M.vert.p);
+  auto gface = static_cast<uint4*>(M.gface.p);
+  auto voff = static_cast<unsigned long long*>(M.voff.p);
+  auto foff = static_cast<unsigned long long*>(M.foff.p);
+  VF_CK(cudaMemsetAsync(vflag, 0, ((V1 + 31) / 32) * 4, st));
+  vfk::mc_vertex_emit(st, G, mask, rbase, ddense, static_cast<uint32_t*>(M.vbase.p), vkey, vown, nsm);
+  vfk::mc_tri_emit(st, G, dtri, dntri, tbase, mask, static_cast<const uint32_t*>(M.vbase.p), ddense,
+                   tkey, tv, vflag, err, nsm);
+  auto tmp = static_cast<uint32_t*>(M.tmp.p);
+  auto hist = static_cast<uint32_t*>(M.hist.p);
+  auto hbase = static_cast<unsigned long long*>(M.hbase.p);
+  vfk::stable_split16(st, vkey, V, F, tmp, vperm, hist, hbase, sums, tot + 2);
+  vfk::stable_split16(st, tkey, T, F, tmp, tperm, hist, hbase, sums, tot + 3);
+  // the grid's affine map (RegularGrid.cpp:478-480): s = size / dims, min - s
+  float sc[3], c0[3];
+  for (int a = 0; a < 3; ++a) {
+    const float size = g->job.aabb_max[a] - g->job.aabb_min[a];
+    sc[a] = size / (float)d[a];
+    c0[a] = g->job.aabb_min[a] - sc[a];
+  }
+  vfk::mc_outputs(st, G, vperm, vown, vflag, V, sc, c0, vinv, vert, tperm, tv, T, gface, nsm);
+  vfk::mc_offsets(st, vkey, vperm, V, F, voff);
+  vfk::mc_offsets(st, tkey, tperm, T, F, foff);
+  auto acc = static_cast<int4*>(M.acc.p);
+  vfk::mc_smooth(st, gface, T, vert, V, acc, mp->nonboundary_iterations, mp->nonboundary_weight, 0,
+                 nsm);
+  vfk::mc_smooth(st, gface, T, vert, V, acc, mp->boundary_iterations, mp->boundary_weight, 1, nsm);
+  vfk::mc_local_faces(st, gface, tperm, tkey, voff, T, static_cast<uint4*>(M.face.p), nsm);
+  uint32_t herr = 0;
+  VF_CK(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
+  VF_CK(cudaStreamSynchronize(st));
+  VF_CK(cudaGetLastError());
+  if (herr) return fail(VF_ERR_CUDA, "triangulate: a triangle edge has no vertex (internal check)");
+  M.V = V;
+  M.T = T;
+  M.ready = true;
+  if (nmeshes) *nmeshes = F;
+  if (nverts) *nverts = V;
+  if (nfaces) *nfaces = T;
+  return VF_OK;
+}
+
+vf_status vf_grid_meshes(vf_grid* g, uint16_t* values, uint64_t* vert_offsets,
+                         uint64_t* face_offsets, float* verts, uint32_t* faces) {
+  if (!g) return fail(VF_ERR_INVALID, "grid is NULL");
+  MeshState& M = g->mesh;
+  if (!M.ready) return fail(VF_ERR_INVALID, "no meshes: call vf_grid_triangulate first");
+  cudaSetDevice(g->ctx->c.device);
+  cudaStream_t st = g->b.stream;
+  const size_t F = M.values.size();
+  if (values) std::memcpy(values, M.values.data(), F * 2);
+  if (vert_offsets) VF_CK(cudaMemcpyAsync(vert_offsets, M.voff.p, (F + 1) * 8, cudaMemcpyDeviceToHost, st));
+  if (face_offsets) VF_CK(cudaMemcpyAsync(face_offsets, M.foff.p, (F + 1) * 8, cudaMemcpyDeviceToHost, st));
+  if (verts && M.V) VF_CK(cudaMemcpyAsync(verts, M.vert.p, M.V * 16, cudaMemcpyDeviceToHost, st));
+  if (faces && M.T) VF_CK(cudaMemcpyAsync(faces, M.face.p, M.T * 16, cudaMemcpyDeviceToHost, st));
+  VF_CK(cudaStreamSynchronize(st));
   return VF_OK;
 }
 

@@ -55,6 +55,46 @@ void rle_write(cudaStream_t st, const uint16_t* g, uint32_t X, uint32_t Y, uint3
                const unsigned long long* row_base, const unsigned long long* nruns,
                unsigned long long* starts, uint16_t* records, int num_sms);
 
+// ---- marching cubes per fragment (vf_mesh.cu) ----
+struct MeshGrid {
+  const uint16_t* g;  // [X][Y][Zp] labels
+  uint32_t X, Y, Z, Zp;
+};
+// the case table packed for the kernels: 4 bits per edge, triangle count
+void mc_pack_table(unsigned long long tri[256], uint8_t ntri[256]);
+// exposed-face masks (X*Y*Z bytes), vertices per grid row, present[value]
+void mc_vertex_count(cudaStream_t st, const MeshGrid& G, uint8_t* mask, uint32_t* rcnt,
+                     uint8_t* present, int num_sms);
+// vertex id base per voxel, fragment key and (voxel * 8 + direction) per vertex
+void mc_vertex_emit(cudaStream_t st, const MeshGrid& G, const uint8_t* mask,
+                    const unsigned long long* rbase, const uint16_t* dense, uint32_t* vbase,
+                    uint16_t* vkey, unsigned long long* vown, int num_sms);
+// triangles per cell row ((X+1)*(Y+1) rows of Z+1 cells)
+void mc_tri_count(cudaStream_t st, const MeshGrid& G, const unsigned long long* tri,
+                  const uint8_t* ntri, uint32_t* rcnt, int num_sms);
+void mc_tri_emit(cudaStream_t st, const MeshGrid& G, const unsigned long long* tri,
+                 const uint8_t* ntri, const unsigned long long* rbase, const uint8_t* mask,
+                 const uint32_t* vbase, const uint16_t* dense, uint16_t* tkey, uint4* tv,
+                 uint32_t* vflag, uint32_t* err, int num_sms);
+// stable order of items 0..n-1 by key[item] (< nkeys <= 65536) into out;
+// tmp: n words (two passes), hist: split_hist_words(n) words, hbase the
+// same count of u64, sums/tot: exclusive_scan scratch for that many words
+size_t split_hist_words(uint64_t n);
+void stable_split16(cudaStream_t st, const uint16_t* key, uint64_t n, uint32_t nkeys, uint32_t* tmp,
+                    uint32_t* out, uint32_t* hist, unsigned long long* hbase,
+                    unsigned long long* sums, unsigned long long* tot);
+void mc_outputs(cudaStream_t st, const MeshGrid& G, const uint32_t* vperm,
+                const unsigned long long* vown, const uint32_t* vflag, uint64_t V, const float s[3],
+                const float c[3], uint32_t* vinv, float4* vert, const uint32_t* tperm,
+                const uint4* tv, uint64_t T, uint4* gface, int num_sms);
+// off[f] = first sorted position with key >= f, f = 0..F
+void mc_offsets(cudaStream_t st, const uint16_t* key, const uint32_t* perm, uint64_t n, uint32_t F,
+                unsigned long long* off);
+void mc_smooth(cudaStream_t st, const uint4* gface, uint64_t T, float4* vert, uint64_t V, int4* acc,
+               uint32_t iters, float weight, int boundary, int num_sms);
+void mc_local_faces(cudaStream_t st, const uint4* gface, const uint32_t* tperm, const uint16_t* tkey,
+                    const unsigned long long* voff, uint64_t T, uint4* out, int num_sms);
+
 // ---- seeds ----
 void sample_seeds(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs);
 
