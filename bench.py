@@ -200,6 +200,11 @@ def main():
     ap.add_argument("--configs", action="store_true",
                     help="single-instance configurations 1-3 (128^3, 256^3, 512^3 vessels): "
                          "one JSON line each with batched, plain and CPU times and a parity check")
+    ap.add_argument("--mesh", action="store_true",
+                    help="fragment meshes (RegularGrid::toTriangleMesh) of one fractured vessel: "
+                         "one JSON line")
+    ap.add_argument("--mesh-dim", type=int, default=512, choices=[128, 256, 512],
+                    help="--mesh workload: the 128^3 / 256^3 / 512^3 vessel of --configs")
     ap.add_argument("--cpu-stride", type=int, default=2,
                     help="cpu_baseline sample: every n-th job of the workload (2: about 10-15 s)")
     ap.add_argument("--ref-stride", type=int, default=4,
@@ -212,6 +217,8 @@ def main():
         return reference_arm(args)
     if args.configs:
         return single_configs(args)
+    if args.mesh:
+        return mesh_bench(args)
 
     from voxelfragmentml_gb300 import replicas as R
     # replicas: every rank runs the whole workload on its own GPU; no collective on
@@ -543,6 +550,135 @@ def single_configs(args):
                                         and not cnt[spec.counts.shape[0]:].any())}), flush=True)
     ctx.close()
     return 0
+
+
+# ncu DRAM bytes (read + write) of one non-boundary k_lap_gather launch on the
+# 512^3 mesh workload (profiles/mesh_kernels_512.md)
+K_LAP_GATHER_NB_DRAM_BYTES_512 = 125.624576e6 + 17.66e6
+
+MESH_JOBS = {
+    128: ("128x96 vessel, 128^3, 8 fragments, Manhattan", (128, 128, 96, 8, 1, 0.0, 16, False, 42, 42)),
+    256: ("256x192 vessel, 256^3, 16 fragments, Euclidean, noise A=2 P=16, one 3x3x3 erosion",
+          (256, 256, 192, 16, 0, 2.0, 16, True, 42, 42)),
+    512: ("512x384 vessel, 512^3, 64 fragments, Chebyshev, noise A=2 P=16",
+          (512, 512, 384, 64, 2, 2.0, 16, False, 42, 42)),
+}
+
+
+def mesh_bench(args):
+    """Fragment meshes: RegularGrid::toTriangleMesh of one fractured vessel
+    (the --configs vessel of --mesh-dim, fractured on the GPU before timing),
+    every fragment's marching-cubes mesh with the reference's default
+    smoothing (max_dim * 0.048 iterations per vertex class).
+
+    value: grid voxels meshed per second, vf_grid_triangulate with the label
+           grid resident (wall clock per call: two size read-backs included);
+    e2e:   the same with the labels uploaded from pinned host memory and the
+           meshes (vec4 vertices, uvec4 faces) downloaded to pinned memory;
+    roofline: the smoothing gather kernel (k_lap_gather, CUDA events around
+              its iterations) against the measured HBM peak;
+    cpu_baseline: the oracle (OpenMP over fragments) on the same grid."""
+    import ctypes as C
+    import oracle as O
+    import voxelfragmentml_gb300 as V
+    from voxelfragmentml_gb300 import build as B, vessel as Vs, workloads as W
+    B.build()
+    O.build()
+    name, a = MESH_JOBS[args.mesh_dim]
+    job = W.single(*a)
+    v, f = W.mesh_for(job)
+    mn, mx = Vs.mesh_aabb(v)
+    dims = Vs.grid_dims(mn, mx, job["max_dim"])
+    ctx = V.Context(0)
+    g = V.RegularGrid(dims, mn, mx, ctx)
+    g.fill(v, f)
+    V.fracture_model(g, V.Params.default(**W.params_for(job, V)))
+    labels = V.pinned_array(dims, np.uint16)
+    labels[...] = g.data()
+    p = V.MCParams.default(max(dims))
+    nvox = int(np.prod(dims))
+    for _ in range(max(args.warmup, 1)):
+        sizes = g.triangulate(p)
+    F, NV, NT = sizes
+    clocks = Clocks()
+    clocks.start()
+    wall, phases = [], []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        g.triangulate(p)
+        wall.append(time.perf_counter() - t)
+        phases.append(g.mesh_phase_ms())
+    L = V.lib()
+    hvals = np.zeros(max(F, 1), np.uint16)
+    hvo = V.pinned_array((F + 1,), np.uint64)
+    hfo = V.pinned_array((F + 1,), np.uint64)
+    hv = V.pinned_array((NV, 4), np.float32)
+    hf = V.pinned_array((NT, 4), np.uint32)
+    e2e = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        g.upload(labels)
+        g.triangulate(p)
+        V._check(L.vf_grid_meshes(g.h, V._p(hvals), V._p(hvo), V._p(hfo), V._p(hv), V._p(hf)))
+        e2e.append(time.perf_counter() - t)
+    clk = clocks.stop()
+    st = g.mesh_phase_ms()
+    cnt = g.mesh_counters()
+    t = time.perf_counter()
+    e = O.triangulate(labels, mn, mx, p.nonboundary_iterations, p.nonboundary_weight,
+                      p.boundary_iterations, p.boundary_weight)
+    cpu_s = time.perf_counter() - t
+    parity = (np.array_equal(hvals[:F], e[0]) and np.array_equal(hvo, e[1]) and
+              np.array_equal(hfo, e[2]) and np.array_equal(hf, e[4]) and
+              np.array_equal(hv.view(np.uint32), e[3].view(np.uint32)))
+    step_s = statistics.median(wall)
+    e2e_s = statistics.median(e2e)
+    dev_ms = [sum(ph) - ph[1] for ph in phases]
+    peak, src = _peaks()
+    sm = statistics.median(ph[4] for ph in phases)
+    # k_lap_gather, per launch: every vertex reads its 8-byte meta word; each
+    # vertex of the pass's type reads and writes its 16-byte position and
+    # reads its 4-byte neighbour entries (neighbour positions come from L2)
+    nv, _, vb, _, ne, neb = cnt
+    per_nb = 8 * nv + 32 * (nv - vb) + 4 * (ne - neb)
+    per_b = 8 * nv + 32 * vb + 4 * neb
+    alg = p.nonboundary_iterations * per_nb + p.boundary_iterations * per_b
+    print(json.dumps({
+        "metric": "fragment-mesh grid voxels/s (RegularGrid::toTriangleMesh, all fragments)",
+        "value": nvox / step_s, "unit": "voxels/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": name, "dims": list(dims), "fragments": F, "vertices": NV,
+                   "faces": NT, "smoothing_iterations": [p.nonboundary_iterations,
+                                                          p.boundary_iterations],
+                   "l2": "label grid and mesh arrays larger than L2" if nvox * 2 > 129e6
+                   else "label grid smaller than L2"},
+        "faces_per_s": NT / step_s,
+        "device_ms": statistics.median(dev_ms), "phase_ms": dict(zip(
+            ["counts", "size_readback", "records_split_outputs", "smoothing_lists",
+             "smoothing_iterations", "local_indices"], [round(x, 3) for x in st])),
+        "counters": dict(zip(["vertices", "faces", "boundary_vertices", "face_incidences",
+                              "neighbour_entries", "boundary_neighbour_entries"], cnt)),
+        "e2e": {"value": nvox / e2e_s, "unit": "voxels/s", "ms": 1e3 * e2e_s,
+                "h2d_bytes_per_step": int(labels.nbytes),
+                "d2h_bytes_per_step": int(hv.nbytes + hf.nbytes + hvo.nbytes + hfo.nbytes)},
+        "roofline": {"bound": "hbm", "kernel": "k_lap_gather (smoothing iterations)",
+                     "launches": p.nonboundary_iterations + p.boundary_iterations,
+                     "bytes_per_launch": [per_nb, per_b],
+                     "achieved": (alg / (sm / 1e3) / 1e9) if sm else None, "peak": peak,
+                     "unit": "GB/s", "frac": (alg / (sm / 1e3) / 1e9 / peak) if sm else None,
+                     "peak_source": src,
+                     "traffic": K_LAP_GATHER_NB_DRAM_BYTES_512 if args.mesh_dim == 512 else None,
+                     "traffic_note": "ncu DRAM bytes of one non-boundary launch (its algorithmic "
+                                     "bytes: bytes_per_launch[0])"},
+        "cpu_baseline": {"value": nvox / cpu_s, "unit": "voxels/s", "cores": os.cpu_count(),
+                         "kind": "port", "sample": "the same grid, once"},
+        "parity_with_oracle": bool(parity),
+        "clocks": clk,
+    }), flush=True)
+    g.close()
+    ctx.close()
+    return 0 if parity else 1
 
 
 if __name__ == "__main__":

@@ -170,6 +170,16 @@ vf_status vf_grid_triangulate(vf_grid* g, const vf_mc_params* p, uint32_t* nmesh
  * receives (MarchingCubes.cpp:403-406). */
 vf_status vf_grid_meshes(vf_grid* g, uint16_t* values, uint64_t* vert_offsets,
                          uint64_t* face_offsets, float* verts, uint32_t* faces);
+/* Device time of the last vf_grid_triangulate's phases, CUDA events on the
+ * grid's stream: [0] face masks + counts, [1] the wait for the sizes (host
+ * round trip), [2] vertex and triangle records + split by fragment +
+ * positions and faces, [3] smoothing neighbour lists, [4] smoothing
+ * iterations, [5] mesh-local face indices. */
+vf_status vf_grid_mesh_phase_ms(const vf_grid* g, float* ms, uint32_t n);
+/* Sizes of the last vf_grid_triangulate: [0] vertices, [1] faces, [2]
+ * boundary vertices, [3] face incidences the smoothing sums, [4] distinct
+ * neighbour entries, [5] those of boundary vertices (0 without smoothing). */
+vf_status vf_grid_mesh_counters(const vf_grid* g, uint64_t* out, uint32_t n);
 
 /* RegularGrid::fill(Model3D*) (RegularGrid.cpp:173-212): occupancy = FP32
  * tri-box SAT shell (Intersections3D.h:204-258) OR tetra-parity interior

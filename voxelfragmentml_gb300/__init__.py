@@ -133,6 +133,8 @@ EXPORTS = {
                                       C.c_void_p]),
     "vf_grid_meshes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_void_p]),
+    "vf_grid_mesh_phase_ms": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "vf_grid_mesh_counters": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_ctx_set_tuning": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_ctx_get_tuning": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
@@ -401,6 +403,21 @@ class RegularGrid:
         faces = np.zeros((T, 4), np.uint32)
         _check(lib().vf_grid_meshes(self.h, _p(vals), _p(vo), _p(fo), _p(verts), _p(faces)))
         return vals[:F], vo, fo, verts, faces
+
+    def mesh_phase_ms(self):
+        """Device ms of the last triangulation's phases: counts, size read-back,
+        records + split + outputs, smoothing lists, smoothing iterations,
+        local indices."""
+        ms = np.zeros(6, np.float32)
+        _check(lib().vf_grid_mesh_phase_ms(self.h, _p(ms), 6))
+        return [float(x) for x in ms]
+
+    def mesh_counters(self):
+        """Sizes of the last triangulation: vertices, faces, boundary vertices,
+        smoothing face incidences, neighbour entries, boundary-vertex entries."""
+        c = np.zeros(6, np.uint64)
+        _check(lib().vf_grid_mesh_counters(self.h, _p(c), 6))
+        return [int(x) for x in c]
 
     def toTriangleMesh(self, params: MCParams | None = None):
         """RegularGrid::toTriangleMesh (RegularGrid.cpp:443-486): one smoothed

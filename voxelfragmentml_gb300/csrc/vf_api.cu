@@ -37,14 +37,29 @@ struct vf_ctx {
 // device state of vf_grid_triangulate, kept for vf_grid_meshes
 struct MeshState {
   vfr::DevBuf mask, vbase, rcnt, rbase, trcnt, tbase, sums, tot, present, dense, table, vkey, vown,
-      vflag, vperm, tmp, vinv, tkey, tv, tperm, hist, hbase, vert, gface, face, voff, foff, acc, err;
+      vflag, vperm, tmp, vinv, tkey, tv, tperm, hist, hbase, vert, gface, face, voff, foff, acc, err,
+      deg, start, ustart, ent, nbr, meta;
   std::vector<uint16_t> values;
   uint64_t V = 0, T = 0;
   bool ready = false;
+  // phase boundaries on the grid's stream: 0 start, 1 counted, 2 sizes read
+  // back, 3 records + split + positions + faces, 4 smoothing lists, 5
+  // smoothed, 6 end
+  cudaEvent_t ev[7] = {};
+  float phase_ms[6] = {};
+  // [0] vertices [1] faces [2] boundary vertices [3] face incidences summed by
+  // the smoothing [4] neighbour entries [5] neighbour entries of boundary vertices
+  uint64_t counters[6] = {};
   void release(vfr::Ctx& c) {
+    for (cudaEvent_t& e : ev)
+      if (e) {
+        cudaEventDestroy(e);
+        e = nullptr;
+      }
     for (vfr::DevBuf* b : {&mask, &vbase, &rcnt, &rbase, &trcnt, &tbase, &sums, &tot, &present,
                            &dense, &table, &vkey, &vown, &vflag, &vperm, &tmp, &vinv, &tkey, &tv,
-                           &tperm, &hist, &hbase, &vert, &gface, &face, &voff, &foff, &acc, &err})
+                           &tperm, &hist, &hbase, &vert, &gface, &face, &voff, &foff, &acc, &err,
+                           &deg, &start, &ustart, &ent, &nbr, &meta})
       c.free_buf(*b);
     ready = false;
   }
@@ -353,7 +368,8 @@ vf_status vf_grid_triangulate(vf_grid* g, const vf_mc_params* mp, uint32_t* nmes
   const int nsm = c.num_sms;
   const vfk::MeshGrid G{static_cast<const uint16_t*>(B.grid0.p), p.X, p.Y, p.Z, p.Zp};
   vf_status s;
-  if ((s = c.alloc(M.mask, nvox)) || (s = c.alloc(M.vbase, nvox * 4)) ||
+  const uint64_t npad = rows * p.Zp;  // face masks and id bases use the grid's row pitch
+  if ((s = c.alloc(M.mask, npad)) || (s = c.alloc(M.vbase, npad * 4)) ||
       (s = c.alloc(M.rcnt, rows * 4)) || (s = c.alloc(M.rbase, rows * 8)) ||
       (s = c.alloc(M.trcnt, crows * 4)) || (s = c.alloc(M.tbase, crows * 8)) ||
       (s = c.alloc(M.tot, 64)) || (s = c.alloc(M.present, 32768)) ||
@@ -369,6 +385,9 @@ vf_status vf_grid_triangulate(vf_grid* g, const vf_mc_params* mp, uint32_t* nmes
   uint8_t* dntri = reinterpret_cast<uint8_t*>(dtri + 256);
   VF_CK(cudaMemcpyAsync(dtri, tri, sizeof(tri), cudaMemcpyHostToDevice, st));
   VF_CK(cudaMemcpyAsync(dntri, ntri, sizeof(ntri), cudaMemcpyHostToDevice, st));
+  for (cudaEvent_t& e : M.ev)
+    if (!e) VF_CK(cudaEventCreate(&e));
+  VF_CK(cudaEventRecord(M.ev[0], st));
   VF_CK(cudaMemsetAsync(M.present.p, 0, 32768, st));
   VF_CK(cudaMemsetAsync(M.err.p, 0, 4, st));
   auto sums = static_cast<unsigned long long*>(M.sums.p);
@@ -377,12 +396,15 @@ vf_status vf_grid_triangulate(vf_grid* g, const vf_mc_params* mp, uint32_t* nmes
   auto rbase = static_cast<unsigned long long*>(M.rbase.p);
   auto tbase = static_cast<unsigned long long*>(M.tbase.p);
   auto err = static_cast<uint32_t*>(M.err.p);
-  // counts: vertices (exposed faces of fragment voxels) and triangles
+  // counts: vertices (exposed faces of fragment voxels) and triangles; the
+  // mask kernel stores non-zero masks only
+  VF_CK(cudaMemsetAsync(mask, 0, npad, st));
   vfk::mc_vertex_count(st, G, mask, static_cast<uint32_t*>(M.rcnt.p),
                        static_cast<uint8_t*>(M.present.p), nsm);
   vfk::exclusive_scan(st, static_cast<uint32_t*>(M.rcnt.p), rbase, sums, (uint32_t)rows, tot);
   vfk::mc_tri_count(st, G, dtri, dntri, static_cast<uint32_t*>(M.trcnt.p), nsm);
   vfk::exclusive_scan(st, static_cast<uint32_t*>(M.trcnt.p), tbase, sums, (uint32_t)crows, tot + 1);
+  VF_CK(cudaEventRecord(M.ev[1], st));
   unsigned long long tots[2] = {0, 0};
   std::vector<uint8_t> present(32768);
   VF_CK(cudaMemcpyAsync(tots, tot, 16, cudaMemcpyDeviceToHost, st));
@@ -390,8 +412,8 @@ vf_status vf_grid_triangulate(vf_grid* g, const vf_mc_params* mp, uint32_t* nmes
   VF_CK(cudaStreamSynchronize(st));
   VF_CK(cudaGetLastError());
   const uint64_t V = tots[0], T = tots[1];
-  if (V >= 0xFFFFFFFFull || T >= 0xFFFFFFFFull)
-    return fail(VF_ERR_RANGE, "triangulate: 2^32 vertices or triangles or more");
+  if (V >= (1ull << 28) || T >= 0xFFFFFFFFull)
+    return fail(VF_ERR_RANGE, "triangulate: 2^28 vertices or 2^32 triangles or more");
   std::vector<uint16_t> dense(32768, 0xFFFFu);
   M.values.clear();
   for (uint32_t v = 2; v < 32768; ++v)
@@ -412,7 +434,11 @@ vf_status vf_grid_triangulate(vf_grid* g, const vf_mc_params* mp, uint32_t* nmes
       (s = c.alloc(M.hbase, hw * 8)) || (s = scan_scratch(std::max<uint64_t>(hw, std::max(rows, crows)))) ||
       (s = c.alloc(M.vert, V1 * 16)) || (s = c.alloc(M.gface, T1 * 16)) ||
       (s = c.alloc(M.face, T1 * 16)) || (s = c.alloc(M.voff, (F + 1) * 8)) ||
-      (s = c.alloc(M.foff, (F + 1) * 8)) || (s = c.alloc(M.acc, V1 * 16)))
+      (s = c.alloc(M.foff, (F + 1) * 8)) || (s = c.alloc(M.acc, V1 * 16)) ||
+      (s = c.alloc(M.deg, V1 * 4)) || (s = c.alloc(M.start, (V1 + 1) * 8)) ||
+      (s = c.alloc(M.ent, T1 * 3 * 8)) || (s = c.alloc(M.ustart, (V1 + 1) * 8)) ||
+      (s = c.alloc(M.nbr, T1 * 3 * 4)) || (s = c.alloc(M.meta, V1 * 8)) ||
+      (s = scan_scratch(std::max<uint64_t>(V1, hw))))
     return s;
   sums = static_cast<unsigned long long*>(M.sums.p);
   auto vkey = static_cast<uint16_t*>(M.vkey.p);
@@ -427,6 +453,7 @@ vf_status vf_grid_triangulate(vf_grid* g, const vf_mc_params* mp, uint32_t* nmes
   auto gface = static_cast<uint4*>(M.gface.p);
   auto voff = static_cast<unsigned long long*>(M.voff.p);
   auto foff = static_cast<unsigned long long*>(M.foff.p);
+  VF_CK(cudaEventRecord(M.ev[2], st));
   VF_CK(cudaMemsetAsync(vflag, 0, ((V1 + 31) / 32) * 4, st));
   vfk::mc_vertex_emit(st, G, mask, rbase, ddense, static_cast<uint32_t*>(M.vbase.p), vkey, vown, nsm);
   vfk::mc_tri_emit(st, G, dtri, dntri, tbase, mask, static_cast<const uint32_t*>(M.vbase.p), ddense,
@@ -446,22 +473,59 @@ vf_status vf_grid_triangulate(vf_grid* g, const vf_mc_params* mp, uint32_t* nmes
   vfk::mc_outputs(st, G, vperm, vown, vflag, V, sc, c0, vinv, vert, tperm, tv, T, gface, nsm);
   vfk::mc_offsets(st, vkey, vperm, V, F, voff);
   vfk::mc_offsets(st, tkey, tperm, T, F, foff);
-  auto acc = static_cast<int4*>(M.acc.p);
-  vfk::mc_smooth(st, gface, T, vert, V, acc, mp->nonboundary_iterations, mp->nonboundary_weight, 0,
-                 nsm);
-  vfk::mc_smooth(st, gface, T, vert, V, acc, mp->boundary_iterations, mp->boundary_weight, 1, nsm);
+  VF_CK(cudaEventRecord(M.ev[3], st));
+  auto ustart = static_cast<unsigned long long*>(M.ustart.p);
+  auto start = static_cast<unsigned long long*>(M.start.p);
+  const bool smooth = (mp->nonboundary_iterations || mp->boundary_iterations) && V && T;
+  if (smooth)
+    VF_CK(vfk::mc_smooth_lists(st, gface, T, vert, V, static_cast<uint32_t*>(M.deg.p), start, ustart,
+                               sums, static_cast<uint2*>(M.ent.p), static_cast<uint32_t*>(M.nbr.p),
+                               static_cast<uint2*>(M.meta.p), err, tot + 4, nsm));
+  VF_CK(cudaEventRecord(M.ev[4], st));
+  if (smooth)
+    VF_CK(vfk::mc_smooth_iterate(st, vert, static_cast<float4*>(M.acc.p), V,
+                                 static_cast<const uint2*>(M.meta.p),
+                                 static_cast<const uint32_t*>(M.nbr.p), mp->nonboundary_iterations,
+                                 mp->nonboundary_weight, mp->boundary_iterations,
+                                 mp->boundary_weight, nsm));
+  VF_CK(cudaEventRecord(M.ev[5], st));
   vfk::mc_local_faces(st, gface, tperm, tkey, voff, T, static_cast<uint4*>(M.face.p), nsm);
+  VF_CK(cudaEventRecord(M.ev[6], st));
   uint32_t herr = 0;
+  unsigned long long smc[4] = {0, 0, 0, 0};  // incidences, entries, boundary vertices, their entries
   VF_CK(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
+  if (smooth) {
+    VF_CK(cudaMemcpyAsync(smc + 0, start + V, 8, cudaMemcpyDeviceToHost, st));
+    VF_CK(cudaMemcpyAsync(smc + 1, ustart + V, 8, cudaMemcpyDeviceToHost, st));
+    VF_CK(cudaMemcpyAsync(smc + 2, tot + 4, 16, cudaMemcpyDeviceToHost, st));
+  }
   VF_CK(cudaStreamSynchronize(st));
   VF_CK(cudaGetLastError());
-  if (herr) return fail(VF_ERR_CUDA, "triangulate: a triangle edge has no vertex (internal check)");
+  for (int i = 0; i < 6; ++i) cudaEventElapsedTime(&M.phase_ms[i], M.ev[i], M.ev[i + 1]);
+  const uint64_t cn[6] = {V, T, smc[2], smc[0], smc[1], smc[3]};
+  std::memcpy(M.counters, cn, sizeof(cn));
+  if (herr & 1u) return fail(VF_ERR_CUDA, "triangulate: a triangle edge has no vertex (internal check)");
+  if (herr & 2u) return fail(VF_ERR_RANGE, "triangulate: a vertex has too many incident faces");
   M.V = V;
   M.T = T;
   M.ready = true;
   if (nmeshes) *nmeshes = F;
   if (nverts) *nverts = V;
   if (nfaces) *nfaces = T;
+  return VF_OK;
+}
+
+vf_status vf_grid_mesh_phase_ms(const vf_grid* g, float* ms, uint32_t n) {
+  if (!g || (n && !ms)) return fail(VF_ERR_INVALID, "NULL argument");
+  if (!g->mesh.ready) return fail(VF_ERR_INVALID, "no meshes: call vf_grid_triangulate first");
+  for (uint32_t i = 0; i < n && i < 6; ++i) ms[i] = g->mesh.phase_ms[i];
+  return VF_OK;
+}
+
+vf_status vf_grid_mesh_counters(const vf_grid* g, uint64_t* out, uint32_t n) {
+  if (!g || (n && !out)) return fail(VF_ERR_INVALID, "NULL argument");
+  if (!g->mesh.ready) return fail(VF_ERR_INVALID, "no meshes: call vf_grid_triangulate first");
+  for (uint32_t i = 0; i < n && i < 6; ++i) out[i] = g->mesh.counters[i];
   return VF_OK;
 }
 

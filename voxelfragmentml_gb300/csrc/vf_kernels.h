@@ -90,8 +90,22 @@ void mc_outputs(cudaStream_t st, const MeshGrid& G, const uint32_t* vperm,
 // off[f] = first sorted position with key >= f, f = 0..F
 void mc_offsets(cudaStream_t st, const uint16_t* key, const uint32_t* perm, uint64_t n, uint32_t F,
                 unsigned long long* off);
-void mc_smooth(cudaStream_t st, const uint4* gface, uint64_t T, float4* vert, uint64_t V, int4* acc,
-               uint32_t iters, float weight, int boundary, int num_sms);
+// smoothSurface (MarchingCubes.cpp:489-510), in two steps.  mc_smooth_lists:
+// per vertex, the distinct neighbours (with multiplicity) of the faces its
+// pass sums, and meta; scratch deg V u32, start / ustart V + 1 u64, sums
+// exclusive_scan scratch for V, ent / nbr one uint2 / u32 per counted face
+// incidence (at most 3 T), meta V uint2, stats 2 u64 (boundary vertices,
+// their neighbour entries); err bit 2 if a vertex has more incidences than
+// its meta holds; needs V < 2^28.  mc_smooth_iterate: nb_iters over the
+// non-boundary vertices, then b_iters over the boundary ones (tmp: V float4).
+cudaError_t mc_smooth_lists(cudaStream_t st, const uint4* gface, uint64_t T, const float4* vert,
+                            uint64_t V, uint32_t* deg, unsigned long long* start,
+                            unsigned long long* ustart, unsigned long long* sums, uint2* ent,
+                            uint32_t* nbr, uint2* meta, uint32_t* err, unsigned long long* stats,
+                            int num_sms);
+cudaError_t mc_smooth_iterate(cudaStream_t st, float4* vert, float4* tmp, uint64_t V,
+                              const uint2* meta, const uint32_t* nbr, uint32_t nb_iters,
+                              float nb_weight, uint32_t b_iters, float b_weight, int num_sms);
 void mc_local_faces(cudaStream_t st, const uint4* gface, const uint32_t* tperm, const uint16_t* tkey,
                     const unsigned long long* voff, uint64_t T, uint4* out, int num_sms);
 
