@@ -205,6 +205,10 @@ def main():
                          "one JSON line")
     ap.add_argument("--mesh-dim", type=int, default=512, choices=[128, 256, 512],
                     help="--mesh workload: the 128^3 / 256^3 / 512^3 vessel of --configs")
+    ap.add_argument("--impact", action="store_true",
+                    help="impact path (ray entry voxels, nearSeeds) on the voxelized vessel of "
+                         "--mesh-dim: one JSON line")
+    ap.add_argument("--rays", type=int, default=1 << 20, help="--impact: rays per step")
     ap.add_argument("--cpu-stride", type=int, default=2,
                     help="cpu_baseline sample: every n-th job of the workload (2: about 10-15 s)")
     ap.add_argument("--ref-stride", type=int, default=4,
@@ -219,6 +223,8 @@ def main():
         return single_configs(args)
     if args.mesh:
         return mesh_bench(args)
+    if args.impact:
+        return impact_bench(args)
 
     from voxelfragmentml_gb300 import replicas as R
     # replicas: every rank runs the whole workload on its own GPU; no collective on
@@ -674,6 +680,89 @@ def mesh_bench(args):
         "cpu_baseline": {"value": nvox / cpu_s, "unit": "voxels/s", "cores": os.cpu_count(),
                          "kind": "port", "sample": "the same grid, once"},
         "parity_with_oracle": bool(parity),
+        "clocks": clk,
+    }), flush=True)
+    g.close()
+    ctx.close()
+    return 0 if parity else 1
+
+
+def impact_rays(mn, mx, n, seed=5):
+    """n rays from a sphere around the box towards random points inside it."""
+    rng = np.random.default_rng(seed)
+    mn, mx = np.asarray(mn, np.float64), np.asarray(mx, np.float64)
+    c, r = (mn + mx) / 2, np.linalg.norm(mx - mn)
+    u = rng.normal(size=(n, 3))
+    o = c + r * u / np.linalg.norm(u, axis=1, keepdims=True)
+    t = mn + rng.random((n, 3)) * (mx - mn)
+    return np.concatenate([o, t - o], axis=1).astype(np.float32)
+
+
+def impact_bench(args):
+    """Impact path on the voxelized vessel of --mesh-dim (CADScene::hit +
+    Seeder::nearSeeds): a batch of rays through vf_ray_entry_voxels (host
+    rays in, entry voxels out, per step), and nearSeeds calls with the
+    reference's defaults (32 seeds, spreading 5) around 6 uniform seeds."""
+    import oracle as O
+    import voxelfragmentml_gb300 as V
+    from voxelfragmentml_gb300 import build as B, vessel as Vs, workloads as W
+    B.build()
+    O.build()
+    name, a = MESH_JOBS[args.mesh_dim]
+    job = W.single(*a)
+    v, f = W.mesh_for(job)
+    mn, mx = Vs.mesh_aabb(v)
+    dims = Vs.grid_dims(mn, mx, job["max_dim"])
+    ctx = V.Context(0)
+    g = V.RegularGrid(dims, mn, mx, ctx)
+    g.fill(v, f)
+    occ = g.data()
+    rays = V.pinned_array((args.rays, 6), np.float32)
+    rays[...] = impact_rays(mn, mx, args.rays)
+    out = V.pinned_array((args.rays, 3), np.uint32)
+    L = V.lib()
+    for _ in range(max(args.warmup, 1)):
+        V._check(L.vf_ray_entry_voxels(g.h, V._p(rays), args.rays, V._p(out)))
+    clocks = Clocks()
+    clocks.start()
+    wall = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        V._check(L.vf_ray_entry_voxels(g.h, V._p(rays), args.rays, V._p(out)))
+        wall.append(time.perf_counter() - t)
+    frags = V.Seeder.uniform(g, 6, 80, V.OUTER)
+    near = []
+    for i in range(args.steps + args.warmup):
+        t = time.perf_counter()
+        seeds = V.Seeder.nearSeeds(g, frags, 1, 32, 5, 80 + i)
+        if i >= args.warmup:
+            near.append(time.perf_counter() - t)
+    clk = clocks.stop()
+    step_s = statistics.median(wall)
+    sample = min(args.rays, 1 << 18)
+    t = time.perf_counter()
+    e = O.ray_entry_batch(occ, mn, mx, rays[:sample])
+    cpu_s = time.perf_counter() - t
+    te = time.perf_counter()
+    es = O.near_seeds(occ, frags, 1, 32, 5, 80 + args.warmup + args.steps - 1)
+    cpu_near_s = time.perf_counter() - te
+    parity = bool(np.array_equal(out[:sample], e) and np.array_equal(seeds, es))
+    print(json.dumps({
+        "metric": "ray entry voxels/s (RegularGrid::getClosestEntryVoxel, batched), host rays in "
+                  "and voxels out per step; nearSeeds latency",
+        "value": args.rays / step_s, "unit": "rays/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "voxelized " + name.split(",")[0], "dims": list(dims),
+                   "rays": args.rays, "hits": int((out[:, 0] != 0xFFFFFFFF).sum()),
+                   "near_seeds": {"impacts": 1, "seeds": 32, "spreading": 5, "given": 6}},
+        "e2e": {"value": args.rays / step_s, "unit": "rays/s",
+                "h2d_bytes_per_step": int(rays.nbytes), "d2h_bytes_per_step": int(out.nbytes)},
+        "near_seeds_ms": {"p50": 1e3 * statistics.median(near), "max": 1e3 * max(near)},
+        "cpu_baseline": {"value": sample / cpu_s, "unit": "rays/s", "cores": os.cpu_count(),
+                         "kind": "port", "sample": f"the first {sample} rays",
+                         "near_seeds_ms": 1e3 * cpu_near_s},
+        "parity_with_oracle": parity,
         "clocks": clk,
     }), flush=True)
     g.close()

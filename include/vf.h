@@ -235,6 +235,30 @@ vf_status vf_undo_mask(vf_grid* g);
 vf_status vf_count_values(vf_grid* g, uint32_t* counts, uint32_t ncounts,
                           uint64_t* occupied);
 
+/* ---- impact path (CADScene::hit + Seeder::nearSeeds) ---------------------
+ * RegularGrid::getClosestEntryVoxel -> rayTraversalAmanatidesWoo
+ * (RegularGrid.cpp:265-270, 853-1004) for n rays on the GPU.  rays: 6 floats
+ * per ray (origin xyz, direction xyz), host.  out: 3 uint32 per ray, the
+ * reference's 1-based index of the first occupied (non-EMPTY) voxel along the
+ * ray (voxel index + 1, which CADScene::hit uses as the impact seed), or
+ * 0xFFFFFFFF x3 when the ray misses the box or every voxel on it is EMPTY.
+ * VF_ERR_INVALID for a zero direction (the reference loops forever). */
+vf_status vf_ray_entry_voxels(vf_grid* g, const float* rays, uint32_t n, uint32_t* out);
+/* Seeder::nearSeeds (Seeder.cpp:49-113) on the GPU: num_impacts times, pick one
+ * of the given seeds and place 1..pending new seeds on surface voxels
+ * (occupied, an EMPTY voxel in the 3x3x3 box) within min(dims)/2 of it, at
+ * offsets dims/2 - sum of `spreading` uniform draws in [0, dims/spreading)
+ * (wrapped), at most num_seeds in all.  out_xyzw (4*(nfrags + num_seeds)
+ * uint32) = the given seeds followed by the new ones in (x, y, z) order,
+ * labelled on from the last given label; *nout = the count.  The draws come
+ * from `seed` (counter-based, identical on every host).  VF_ERR_SEED_SEARCH
+ * when an impact finds too few voxels in 2^20 candidates (the reference
+ * loops forever); VF_ERR_INVALID for impacts without given seeds or
+ * spreading outside [1, min(dims)]. */
+vf_status vf_near_seeds(vf_grid* g, const uint32_t* frags_xyzw, uint32_t nfrags,
+                        uint32_t num_impacts, uint32_t num_seeds, uint32_t spreading,
+                        uint64_t seed, uint32_t* out_xyzw, uint32_t* nout);
+
 /* CADScene::fractureModel (CADScene.cpp:624-691) on an already voxelized
  * grid: seeds -> fracture -> [perturb] -> erode | detectBoundaries.  The
  * seeds used are returned when seeds_out (4*(2n+extra) uint32) is given. */

@@ -24,7 +24,8 @@ def build(force: bool = False) -> str:
     if force or not os.path.exists(_LIB_PATH) or (
             os.path.getmtime(_LIB_PATH) < max(
                 os.path.getmtime(os.path.join(_HERE, f))
-                for f in ("vf_oracle.c", "vf_oracle_mesh.c", "vf_oracle.h", "Makefile",
+                for f in ("vf_oracle.c", "vf_oracle_mesh.c", "vf_oracle_impact.c", "vf_oracle.h",
+                          "Makefile",
                           os.path.join("..", "voxelfragmentml_gb300", "csrc",
                                        "vf_mc_table.h")))):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
@@ -70,6 +71,9 @@ def lib():
             "vfo_rle_encode": (C.c_size_t, [P, u32, u32, u32, P, C.c_size_t]),
             "vfo_triangulate": (i32, [P, u32, u32, u32, P, P, u32, f32, u32, f32,
                                       P, P, P, P, P, P, P, P]),
+            "vfo_ray_entry": (i32, [P, u32, u32, u32, P, P, P, P, P]),
+            "vfo_ray_entry_batch": (i32, [P, u32, u32, u32, P, P, P, u32, P]),
+            "vfo_near_seeds": (i32, [P, u32, u32, u32, P, u32, u32, u32, u32, u64, P, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(_lib, name)
@@ -246,3 +250,35 @@ def triangulate(grid, aabb_min, aabb_max, nb_iters=0, nb_weight=0.9, b_iters=0, 
     _check(lib().vfo_triangulate(*args, _p(vals), _p(vo), _p(fo), _p(verts), _p(faces)),
            "triangulate")
     return vals, vo, fo, verts, faces
+
+
+def ray_entry(grid, aabb_min, aabb_max, origin, direction):
+    """RegularGrid::getClosestEntryVoxel: the 1-based index of the first
+    occupied voxel on the ray, or None."""
+    g = np.ascontiguousarray(grid, dtype=np.uint16)
+    lo, hi, o, d = _f3(aabb_min), _f3(aabb_max), _f3(origin), _f3(direction)
+    out = np.zeros(3, np.uint32)
+    _check(lib().vfo_ray_entry(_p(g), *g.shape, _p(lo), _p(hi), _p(o), _p(d), _p(out)), "ray_entry")
+    return None if out[0] == 0xFFFFFFFF else tuple(int(v) for v in out)
+
+
+def near_seeds(grid, frags, num_impacts, num_seeds, spreading, seed):
+    """Seeder::nearSeeds: frags followed by the seeds placed around impacts."""
+    g = np.ascontiguousarray(grid, dtype=np.uint16)
+    f = np.ascontiguousarray(frags, dtype=np.uint32).reshape(-1, 4)
+    out = np.zeros((f.shape[0] + num_seeds + 1, 4), np.uint32)
+    n = C.c_uint32()
+    _check(lib().vfo_near_seeds(_p(g), *g.shape, _p(f), f.shape[0], num_impacts, num_seeds,
+                                spreading, seed, _p(out), C.byref(n)), "near_seeds")
+    return out[:n.value]
+
+
+def ray_entry_batch(grid, aabb_min, aabb_max, rays):
+    """ray_entry for (n, 6) rays at once (OpenMP): (n, 3) uint32, 0xFFFFFFFF on a miss."""
+    g = np.ascontiguousarray(grid, dtype=np.uint16)
+    r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+    lo, hi = _f3(aabb_min), _f3(aabb_max)
+    out = np.zeros((r.shape[0], 3), np.uint32)
+    _check(lib().vfo_ray_entry_batch(_p(g), *g.shape, _p(lo), _p(hi), _p(r), r.shape[0], _p(out)),
+           "ray_entry_batch")
+    return out

@@ -157,6 +157,23 @@ int vfo_triangulate(const uint16_t* grid, uint32_t X, uint32_t Y, uint32_t Z,
                     uint16_t* values, uint64_t* vert_off, uint64_t* face_off,
                     float* verts, uint32_t* faces);
 
+/* Impact path (vf_oracle_impact.c): the 1-based index of the first occupied
+ * voxel a ray enters (RegularGrid::rayTraversalAmanatidesWoo, RegularGrid.cpp:
+ * 900-1004; 0xFFFFFFFF x3 on a miss), and Seeder::nearSeeds (Seeder.cpp:
+ * 49-113): out = frags followed by the new seeds, 4 uint32 each, *nout the
+ * count (at most nfrags + num_seeds). */
+#define VFO_NEAR_MAX_CANDIDATES (1u << 20)
+int vfo_ray_entry(const uint16_t* grid, uint32_t X, uint32_t Y, uint32_t Z,
+                  const float amin[3], const float amax[3], const float origin[3],
+                  const float dir[3], uint32_t out[3]);
+int vfo_ray_entry_batch(const uint16_t* grid, uint32_t X, uint32_t Y, uint32_t Z,
+                        const float amin[3], const float amax[3], const float* rays,
+                        uint32_t n, uint32_t* out);
+int vfo_near_seeds(const uint16_t* grid, uint32_t X, uint32_t Y, uint32_t Z,
+                   const uint32_t* frags, uint32_t nfrags, uint32_t num_impacts,
+                   uint32_t num_seeds, uint32_t spreading, uint64_t seed,
+                   uint32_t* out, uint32_t* nout);
+
 #ifdef __cplusplus
 }
 #endif

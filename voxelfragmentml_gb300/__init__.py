@@ -128,6 +128,9 @@ EXPORTS = {
     "vf_ctx_last_graph": (C.c_int, [C.c_void_p, C.c_void_p]),
     "vf_ctx_flood_pass_sizes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_grid_export_rle": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "vf_ray_entry_voxels": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "vf_near_seeds": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
+                                C.c_uint32, C.c_uint64, C.c_void_p, C.c_void_p]),
     "vf_mc_params_default": (None, [C.c_uint32, C.c_void_p]),
     "vf_grid_triangulate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_void_p]),
@@ -383,6 +386,20 @@ class RegularGrid:
         _check(lib().vf_count_values(self.h, _p(c), ncounts, C.byref(occ)))
         return c, occ.value
 
+    def getClosestEntryVoxel(self, origin, direction):
+        """RegularGrid::getClosestEntryVoxel: the 1-based index of the first
+        occupied voxel on the ray (as CADScene::hit uses it), or None."""
+        r = self.rayEntryVoxels(np.concatenate([_f3(origin), _f3(direction)]).reshape(1, 6))
+        return None if r[0, 0] == 0xFFFFFFFF else tuple(int(v) for v in r[0])
+
+    def rayEntryVoxels(self, rays):
+        """Entry voxels of many rays (n, 6: origin, direction) on the GPU:
+        (n, 3) uint32, 0xFFFFFFFF rows for misses."""
+        r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+        out = np.zeros((r.shape[0], 3), np.uint32)
+        _check(lib().vf_ray_entry_voxels(self.h, _p(r), r.shape[0], _p(out)))
+        return out
+
     def triangulate(self, params: MCParams | None = None):
         """vf_grid_triangulate: build every fragment's mesh on the device and
         return (meshes, vertices, faces) counts."""
@@ -443,6 +460,18 @@ class Seeder:
         s = np.array(seeds, dtype=np.uint32, copy=True, order="C").reshape(-1, 4)
         _check(lib().vf_merge_seeds(_p(f), f.shape[0], _p(s), s.shape[0], dfunc))
         return s
+
+    @staticmethod
+    def nearSeeds(grid: RegularGrid, frags, numImpacts: int, numSeeds: int, spreading: int,
+                  seed: int = 80):
+        """Seeder::nearSeeds (Seeder.cpp:49-113): frags followed by seeds placed
+        on surface voxels around numImpacts randomly chosen frags."""
+        f = np.ascontiguousarray(frags, dtype=np.uint32).reshape(-1, 4)
+        out = np.zeros((f.shape[0] + numSeeds + 1, 4), np.uint32)
+        n = C.c_uint32()
+        _check(lib().vf_near_seeds(grid.h, _p(f), f.shape[0], numImpacts, numSeeds, spreading,
+                                   seed, _p(out), C.byref(n)))
+        return out[:n.value]
 
     @staticmethod
     def fracture_seeds(grid: RegularGrid, params: Params):

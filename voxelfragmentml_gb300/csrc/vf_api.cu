@@ -65,12 +65,21 @@ struct MeshState {
   }
 };
 
+// device scratch of the impact path (rays, nearSeeds)
+struct ImpactState {
+  vfr::DevBuf rays, hits, frags, chosen, out, status;
+  void release(vfr::Ctx& c) {
+    for (vfr::DevBuf* b : {&rays, &hits, &frags, &chosen, &out, &status}) c.free_buf(*b);
+  }
+};
+
 struct vf_grid {
   vf_ctx* ctx = nullptr;
   vfr::Batch b;
   vf_job job;
   std::vector<uint32_t> seeds;  // last seeds used by fracture_model
   MeshState mesh;
+  ImpactState impact;
 };
 
 extern "C" {
@@ -257,6 +266,7 @@ vf_status vf_grid_destroy(vf_grid* g) {
   cudaSetDevice(g->ctx->c.device);
   if (g->b.stream) cudaStreamSynchronize(g->b.stream);
   g->mesh.release(g->ctx->c);
+  g->impact.release(g->ctx->c);
   g->b.release();
   delete g;
   return VF_OK;
@@ -543,6 +553,86 @@ vf_status vf_grid_meshes(vf_grid* g, uint16_t* values, uint64_t* vert_offsets,
   if (verts && M.V) VF_CK(cudaMemcpyAsync(verts, M.vert.p, M.V * 16, cudaMemcpyDeviceToHost, st));
   if (faces && M.T) VF_CK(cudaMemcpyAsync(faces, M.face.p, M.T * 16, cudaMemcpyDeviceToHost, st));
   VF_CK(cudaStreamSynchronize(st));
+  return VF_OK;
+}
+
+static vfk::ImpactGrid impact_grid(const vf_grid* g) {
+  const vfr::JobPlan& p = g->b.plans[0];
+  vfk::ImpactGrid G;
+  G.g = static_cast<const uint16_t*>(g->b.grid0.p);
+  G.X = p.X;
+  G.Y = p.Y;
+  G.Z = p.Z;
+  G.Zp = p.Zp;
+  const uint32_t d[3] = {p.X, p.Y, p.Z};
+  for (int a = 0; a < 3; ++a) {
+    G.amin[a] = g->job.aabb_min[a];
+    G.amax[a] = g->job.aabb_max[a];
+    // RegularGrid::setAABB (RegularGrid.cpp:437): _cellSize = _aabb.size() / _numDivs
+    G.cell[a] = (G.amax[a] - G.amin[a]) / (float)d[a];
+  }
+  return G;
+}
+
+vf_status vf_ray_entry_voxels(vf_grid* g, const float* rays, uint32_t n, uint32_t* out) {
+  if (!g || (n && (!rays || !out))) return fail(VF_ERR_INVALID, "NULL argument");
+  if (!n) return VF_OK;
+  for (uint32_t r = 0; r < n; ++r)
+    if (rays[6 * r + 3] == 0.0f && rays[6 * r + 4] == 0.0f && rays[6 * r + 5] == 0.0f)
+      return fail(VF_ERR_INVALID, "ray " + std::to_string(r) + " has a zero direction");
+  cudaSetDevice(g->ctx->c.device);
+  vfr::Ctx& c = g->ctx->c;
+  ImpactState& I = g->impact;
+  vf_status s;
+  if ((s = c.alloc(I.rays, (size_t)n * 24)) || (s = c.alloc(I.hits, (size_t)n * 12))) return s;
+  cudaStream_t st = g->b.stream;
+  VF_CK(cudaMemcpyAsync(I.rays.p, rays, (size_t)n * 24, cudaMemcpyHostToDevice, st));
+  vfk::ray_entry(st, impact_grid(g), static_cast<const float*>(I.rays.p), n,
+                 static_cast<uint32_t*>(I.hits.p), c.num_sms);
+  VF_CK(cudaMemcpyAsync(out, I.hits.p, (size_t)n * 12, cudaMemcpyDeviceToHost, st));
+  VF_CK(cudaStreamSynchronize(st));
+  VF_CK(cudaGetLastError());
+  return VF_OK;
+}
+
+vf_status vf_near_seeds(vf_grid* g, const uint32_t* frags_xyzw, uint32_t nfrags,
+                        uint32_t num_impacts, uint32_t num_seeds, uint32_t spreading, uint64_t seed,
+                        uint32_t* out_xyzw, uint32_t* nout) {
+  if (!g || !out_xyzw || !nout || (nfrags && !frags_xyzw)) return fail(VF_ERR_INVALID, "NULL argument");
+  const vfr::JobPlan& p = g->b.plans[0];
+  const uint32_t mind = std::min(p.X, std::min(p.Y, p.Z));
+  if (num_impacts && !nfrags) return fail(VF_ERR_INVALID, "nearSeeds: impacts need at least one seed");
+  if (num_impacts && (spreading < 1 || spreading > mind))
+    return fail(VF_ERR_INVALID, "nearSeeds: spreading must be in [1, min(dims)]");
+  if (num_seeds > VF_MAX_SEEDS) return fail(VF_ERR_INVALID, "nearSeeds: too many seeds");
+  if (num_impacts > (1u << 20)) return fail(VF_ERR_INVALID, "nearSeeds: too many impacts");
+  for (uint32_t i = 0; i < nfrags; ++i)
+    if (frags_xyzw[4 * i] >= p.X + 1 || frags_xyzw[4 * i + 1] >= p.Y + 1 || frags_xyzw[4 * i + 2] >= p.Z + 1)
+      return fail(VF_ERR_INVALID, "nearSeeds: seed outside the grid");
+  std::memcpy(out_xyzw, frags_xyzw, (size_t)nfrags * 16);
+  *nout = nfrags;
+  if (!num_impacts || !num_seeds) return VF_OK;
+  cudaSetDevice(g->ctx->c.device);
+  vfr::Ctx& c = g->ctx->c;
+  ImpactState& I = g->impact;
+  vf_status s;
+  if ((s = c.alloc(I.frags, (size_t)nfrags * 16)) || (s = c.alloc(I.chosen, (size_t)num_seeds * 12)) ||
+      (s = c.alloc(I.out, (size_t)num_seeds * 16)) || (s = c.alloc(I.status, 16)))
+    return s;
+  cudaStream_t st = g->b.stream;
+  VF_CK(cudaMemcpyAsync(I.frags.p, frags_xyzw, (size_t)nfrags * 16, cudaMemcpyHostToDevice, st));
+  const uint32_t label0 = frags_xyzw[4 * (nfrags - 1) + 3];
+  vfk::near_seeds(st, impact_grid(g), static_cast<const uint32_t*>(I.frags.p), nfrags, num_impacts,
+                  num_seeds, spreading, seed, label0, static_cast<uint32_t*>(I.chosen.p),
+                  static_cast<uint32_t*>(I.out.p), static_cast<uint32_t*>(I.status.p));
+  uint32_t status[2] = {0, 0};
+  VF_CK(cudaMemcpyAsync(status, I.status.p, 8, cudaMemcpyDeviceToHost, st));
+  VF_CK(cudaStreamSynchronize(st));
+  VF_CK(cudaGetLastError());
+  if (status[1]) return fail(VF_ERR_SEED_SEARCH, "nearSeeds: an impact found too few surface voxels");
+  if (status[0] > num_seeds) return fail(VF_ERR_CUDA, "nearSeeds: count out of range");
+  VF_CK(cudaMemcpy(out_xyzw + 4 * (size_t)nfrags, I.out.p, (size_t)status[0] * 16, cudaMemcpyDeviceToHost));
+  *nout = nfrags + status[0];
   return VF_OK;
 }
 

@@ -109,6 +109,25 @@ cudaError_t mc_smooth_iterate(cudaStream_t st, float4* vert, float4* tmp, uint64
 void mc_local_faces(cudaStream_t st, const uint4* gface, const uint32_t* tperm, const uint16_t* tkey,
                     const unsigned long long* voff, uint64_t T, uint4* out, int num_sms);
 
+// ---- impact path (vf_impact.cu) ----
+struct ImpactGrid {
+  const uint16_t* g;  // [X][Y][Zp] labels
+  uint32_t X, Y, Z, Zp;
+  float amin[3], amax[3], cell[3];  // the grid's box and (amax - amin) / dims
+};
+// per ray (origin xyz, direction xyz): the 1-based index of the first
+// occupied voxel, 0xFFFFFFFF x3 when none; zero directions are rejected by
+// the caller
+void ray_entry(cudaStream_t st, const ImpactGrid& G, const float* rays, uint32_t n, uint32_t* out,
+               int num_sms);
+// Seeder::nearSeeds: the new seeds (4 uint32 each, labels label0 + 1, ...)
+// in (x, y, z) order into out; chosen: 3 * num_seeds scratch; status[0] =
+// count, status[1] = 0 or VF_ERR_SEED_SEARCH.  Needs nfrags >= 1 and
+// 1 <= spreading <= min(dims) when num_impacts > 0.
+void near_seeds(cudaStream_t st, const ImpactGrid& G, const uint32_t* frags, uint32_t nfrags,
+                uint32_t num_impacts, uint32_t num_seeds, uint32_t spreading, uint64_t seed,
+                uint32_t label0, uint32_t* chosen, uint32_t* out, uint32_t* status);
+
 // ---- seeds ----
 void sample_seeds(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs);
 
