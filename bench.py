@@ -627,6 +627,14 @@ def mesh_bench(args):
         g.triangulate(p)
         V._check(L.vf_grid_meshes(g.h, V._p(hvals), V._p(hvo), V._p(hfo), V._p(hv), V._p(hf)))
         e2e.append(time.perf_counter() - t)
+    # point clouds of every fragment mesh (CADModel::sampleCPU, 1024 points: the
+    # reference's default _targetPoints)
+    pc_wall = []
+    for i in range(args.steps + 1):
+        t = time.perf_counter()
+        clouds = g.samplePointClouds(1024, 80)
+        if i:
+            pc_wall.append(time.perf_counter() - t)
     clk = clocks.stop()
     st = g.mesh_phase_ms()
     cnt = g.mesh_counters()
@@ -634,6 +642,12 @@ def mesh_bench(args):
     e = O.triangulate(labels, mn, mx, p.nonboundary_iterations, p.nonboundary_weight,
                       p.boundary_iterations, p.boundary_weight)
     cpu_s = time.perf_counter() - t
+    t = time.perf_counter()
+    e_pc = [O.sample_mesh(e[3][e[1][i]:e[1][i + 1]], e[4][e[2][i]:e[2][i + 1]], 1024, 80, int(v))
+            for i, v in enumerate(e[0])]
+    cpu_pc_s = time.perf_counter() - t
+    pc_parity = len(e_pc) == len(clouds) and all(
+        np.array_equal(a.view(np.uint32), b.view(np.uint32)) for a, b in zip(clouds, e_pc))
     parity = (np.array_equal(hvals[:F], e[0]) and np.array_equal(hvo, e[1]) and
               np.array_equal(hfo, e[2]) and np.array_equal(hf, e[4]) and
               np.array_equal(hv.view(np.uint32), e[3].view(np.uint32)))
@@ -680,11 +694,14 @@ def mesh_bench(args):
         "cpu_baseline": {"value": nvox / cpu_s, "unit": "voxels/s", "cores": os.cpu_count(),
                          "kind": "port", "sample": "the same grid, once"},
         "parity_with_oracle": bool(parity),
+        "point_clouds": {"points_per_mesh": 1024, "meshes": F,
+                         "ms": 1e3 * statistics.median(pc_wall),
+                         "cpu_oracle_ms": 1e3 * cpu_pc_s, "parity_with_oracle": bool(pc_parity)},
         "clocks": clk,
     }), flush=True)
     g.close()
     ctx.close()
-    return 0 if parity else 1
+    return 0 if (parity and pc_parity) else 1
 
 
 def impact_rays(mn, mx, n, seed=5):

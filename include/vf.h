@@ -235,6 +235,30 @@ vf_status vf_undo_mask(vf_grid* g);
 vf_status vf_count_values(vf_grid* g, uint32_t* counts, uint32_t ncounts,
                           uint64_t* occupied);
 
+/* ---- point clouds (CADModel::sampleCPU) ----------------------------------
+ * CADModel::sampleCPU(max_samples) (CADModel.cpp:264-370) for every mesh of
+ * the last vf_grid_triangulate, as the dataset generator samples each
+ * fragment (CADScene.cpp:129-143, 340-372).  A mesh of T faces gets
+ * min(P, S) points when S = max_samples > T (P = sum over faces of
+ * max(ceil(area / sumArea * S), 1)), else S points on S distinct faces.
+ * point_offsets (nmeshes + 1, may be NULL) and *npoints give the layout; the
+ * points (x, y, z, 1) stay on the device for vf_grid_points.  The noise and
+ * face draws come from `seed` and the mesh's fragment value (counter-based,
+ * identical on every host); samples are in face order, and more than S
+ * samples keep the systematic sample floor((i+1) S / P) > floor(i S / P)
+ * (the reference shuffles with an unseeded generator).  VF_ERR_INVALID
+ * without a triangulation. */
+vf_status vf_grid_sample_meshes(vf_grid* g, uint32_t max_samples, uint64_t seed,
+                                uint64_t* point_offsets, uint64_t* npoints);
+/* the points of the last vf_grid_sample_meshes: 4 floats each, host */
+vf_status vf_grid_points(vf_grid* g, float* points);
+/* CADModel::sampleCPU of one host mesh (verts 3 floats, faces 3 uint32 per
+ * element; mesh key 0): at most max_samples points (4 floats each) into
+ * points, *npoints the count. */
+vf_status vf_sample_mesh(vf_ctx* ctx, const float* verts, uint32_t nverts, const uint32_t* faces,
+                         uint32_t nfaces, uint32_t max_samples, uint64_t seed, float* points,
+                         uint64_t* npoints);
+
 /* ---- impact path (CADScene::hit + Seeder::nearSeeds) ---------------------
  * RegularGrid::getClosestEntryVoxel -> rayTraversalAmanatidesWoo
  * (RegularGrid.cpp:265-270, 853-1004) for n rays on the GPU.  rays: 6 floats

@@ -24,7 +24,8 @@ def build(force: bool = False) -> str:
     if force or not os.path.exists(_LIB_PATH) or (
             os.path.getmtime(_LIB_PATH) < max(
                 os.path.getmtime(os.path.join(_HERE, f))
-                for f in ("vf_oracle.c", "vf_oracle_mesh.c", "vf_oracle_impact.c", "vf_oracle.h",
+                for f in ("vf_oracle.c", "vf_oracle_mesh.c", "vf_oracle_impact.c",
+                          "vf_oracle_sample.c", "vf_oracle.h",
                           "Makefile",
                           os.path.join("..", "voxelfragmentml_gb300", "csrc",
                                        "vf_mc_table.h")))):
@@ -72,6 +73,7 @@ def lib():
             "vfo_triangulate": (i32, [P, u32, u32, u32, P, P, u32, f32, u32, f32,
                                       P, P, P, P, P, P, P, P]),
             "vfo_ray_entry": (i32, [P, u32, u32, u32, P, P, P, P, P]),
+            "vfo_sample_mesh": (i32, [P, P, u32, u32, u64, u32, P, P]),
             "vfo_ray_entry_batch": (i32, [P, u32, u32, u32, P, P, P, u32, P]),
             "vfo_near_seeds": (i32, [P, u32, u32, u32, P, u32, u32, u32, u32, u64, P, P]),
         }
@@ -282,3 +284,15 @@ def ray_entry_batch(grid, aabb_min, aabb_max, rays):
     _check(lib().vfo_ray_entry_batch(_p(g), *g.shape, _p(lo), _p(hi), _p(r), r.shape[0], _p(out)),
            "ray_entry_batch")
     return out
+
+
+def sample_mesh(verts4, faces4, max_samples, seed, key=0):
+    """CADModel::sampleCPU: (n, 4) float32 points (x, y, z, 1) on the mesh
+    (verts4: (V, 4) float32, faces4: (T, 4) uint32 mesh-local indices)."""
+    v = np.ascontiguousarray(verts4, dtype=np.float32).reshape(-1, 4)
+    f = np.ascontiguousarray(faces4, dtype=np.uint32).reshape(-1, 4)
+    out = np.zeros((max(max_samples, 1), 4), np.float32)
+    n = C.c_uint64()
+    _check(lib().vfo_sample_mesh(_p(v), _p(f), f.shape[0], max_samples, seed, key, _p(out),
+                                 C.byref(n)), "sample_mesh")
+    return out[:n.value]

@@ -162,6 +162,12 @@ int vfo_triangulate(const uint16_t* grid, uint32_t X, uint32_t Y, uint32_t Z,
  * 900-1004; 0xFFFFFFFF x3 on a miss), and Seeder::nearSeeds (Seeder.cpp:
  * 49-113): out = frags followed by the new seeds, 4 uint32 each, *nout the
  * count (at most nfrags + num_seeds). */
+/* CADModel::sampleCPU (vf_oracle_sample.c): at most S points (4 floats:
+ * x, y, z, 1) on the mesh verts (4 floats per vertex) / faces (4 uint32 per
+ * face: three vertex indices, unused); key: the mesh's draw key. */
+int vfo_sample_mesh(const float* verts, const uint32_t* faces, uint32_t nfaces, uint32_t S,
+                    uint64_t seed, uint32_t key, float* out, uint64_t* nout);
+
 #define VFO_NEAR_MAX_CANDIDATES (1u << 20)
 int vfo_ray_entry(const uint16_t* grid, uint32_t X, uint32_t Y, uint32_t Z,
                   const float amin[3], const float amax[3], const float origin[3],

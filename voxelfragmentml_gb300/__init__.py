@@ -128,6 +128,11 @@ EXPORTS = {
     "vf_ctx_last_graph": (C.c_int, [C.c_void_p, C.c_void_p]),
     "vf_ctx_flood_pass_sizes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_grid_export_rle": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "vf_grid_sample_meshes": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64, C.c_void_p,
+                                        C.c_void_p]),
+    "vf_grid_points": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "vf_sample_mesh": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32,
+                                 C.c_uint32, C.c_uint64, C.c_void_p, C.c_void_p]),
     "vf_ray_entry_voxels": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     "vf_near_seeds": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
                                 C.c_uint32, C.c_uint64, C.c_void_p, C.c_void_p]),
@@ -436,6 +441,18 @@ class RegularGrid:
         _check(lib().vf_grid_mesh_counters(self.h, _p(c), 6))
         return [int(x) for x in c]
 
+    def samplePointClouds(self, max_samples: int, seed: int = 80):
+        """CADModel::sampleCPU of every mesh of the last triangulation: a list of
+        (n, 4) float32 point arrays (x, y, z, 1), one per fragment value."""
+        F = self._mesh_sizes[0]
+        offs = np.zeros(F + 1, np.uint64)
+        n = C.c_uint64()
+        _check(lib().vf_grid_sample_meshes(self.h, max_samples, seed, _p(offs), C.byref(n)))
+        pts = np.zeros((max(n.value, 1), 4), np.float32)
+        if n.value:
+            _check(lib().vf_grid_points(self.h, _p(pts)))
+        return [pts[offs[i]:offs[i + 1]] for i in range(F)]
+
     def toTriangleMesh(self, params: MCParams | None = None):
         """RegularGrid::toTriangleMesh (RegularGrid.cpp:443-486): one smoothed
         marching-cubes mesh per fragment value, in ascending value order."""
@@ -523,6 +540,18 @@ def fracture_model(grid: RegularGrid, params: Params):
     out = np.zeros((max(cap, 1), 4), np.uint32)
     n = C.c_uint32()
     _check(lib().vf_fracture_model(grid.h, C.byref(params), _p(out), C.byref(n)))
+    return out[:n.value]
+
+
+def sample_mesh(verts, faces, max_samples: int, seed: int = 80, ctx: "Context | None" = None):
+    """CADModel::sampleCPU of one mesh on the GPU: (n, 4) float32 points."""
+    ctx = ctx or default_context()
+    v = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
+    f = np.ascontiguousarray(faces, dtype=np.uint32).reshape(-1, 3)
+    out = np.zeros((max(max_samples, 1), 4), np.float32)
+    n = C.c_uint64()
+    _check(lib().vf_sample_mesh(ctx.h, _p(v), v.shape[0], _p(f), f.shape[0], max_samples, seed,
+                                _p(out), C.byref(n)))
     return out[:n.value]
 
 

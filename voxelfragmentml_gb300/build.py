@@ -19,7 +19,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libvfgb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 SOURCES = ["vf_voxelize.cu", "vf_gridops.cu", "vf_flood.cu", "vf_plain.cu",
-           "vf_runtime.cu", "vf_api.cu", "vf_noalloc.cu", "vf_rle.cu", "vf_mesh.cu", "vf_impact.cu"]
+           "vf_runtime.cu", "vf_api.cu", "vf_noalloc.cu", "vf_rle.cu", "vf_mesh.cu", "vf_impact.cu", "vf_sample.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

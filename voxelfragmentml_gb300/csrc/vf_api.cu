@@ -73,6 +73,22 @@ struct ImpactState {
   }
 };
 
+// device state of point sampling (CADModel::sampleCPU)
+struct SampleState {
+  vfr::DevBuf area, cstart, cend, csum, cmax, mchunk, msum, nb, big, sel, chosen, err, cnt, P, soff,
+      sums, out_off, out, keys, verts, faces, voff, foff;
+  uint64_t npoints = 0;
+  std::vector<uint64_t> offsets;  // per mesh, F + 1
+  bool ready = false;
+  void release(vfr::Ctx& c) {
+    for (vfr::DevBuf* b : {&area, &cstart, &cend, &csum, &cmax, &mchunk, &msum, &nb, &big, &sel, &chosen,
+                           &err, &cnt, &P, &soff, &sums, &out_off, &out, &keys, &verts, &faces, &voff,
+                           &foff})
+      c.free_buf(*b);
+    ready = false;
+  }
+};
+
 struct vf_grid {
   vf_ctx* ctx = nullptr;
   vfr::Batch b;
@@ -80,6 +96,7 @@ struct vf_grid {
   std::vector<uint32_t> seeds;  // last seeds used by fracture_model
   MeshState mesh;
   ImpactState impact;
+  SampleState sample;
 };
 
 extern "C" {
@@ -267,6 +284,7 @@ vf_status vf_grid_destroy(vf_grid* g) {
   if (g->b.stream) cudaStreamSynchronize(g->b.stream);
   g->mesh.release(g->ctx->c);
   g->impact.release(g->ctx->c);
+  g->sample.release(g->ctx->c);
   g->b.release();
   delete g;
   return VF_OK;
@@ -537,6 +555,192 @@ vf_status vf_grid_mesh_counters(const vf_grid* g, uint64_t* out, uint32_t n) {
   if (!g->mesh.ready) return fail(VF_ERR_INVALID, "no meshes: call vf_grid_triangulate first");
   for (uint32_t i = 0; i < n && i < 6; ++i) out[i] = g->mesh.counters[i];
   return VF_OK;
+}
+
+// CADModel::sampleCPU for the meshes M (host copy of their face offsets: fo);
+// the points stay in P.out at P.offsets
+static vf_status sample_meshes(vfr::Ctx& c, cudaStream_t st, SampleState& P, vfk::SampleMeshes M,
+                               const std::vector<uint64_t>& fo, uint32_t S, uint64_t seed) {
+  P.ready = false;
+  const uint32_t F = M.F;
+  std::vector<unsigned long long> cs, ce, mc(F + 1);
+  std::vector<uint8_t> big(std::max<uint32_t>(F, 1));
+  std::vector<uint32_t> sel;
+  for (uint32_t m = 0; m < F; ++m) {
+    mc[m] = cs.size();
+    for (uint64_t t = fo[m]; t < fo[m + 1]; t += 1024) {
+      cs.push_back(t);
+      ce.push_back(std::min<uint64_t>(t + 1024, fo[m + 1]));
+    }
+    const uint64_t T = fo[m + 1] - fo[m];
+    big[m] = S > T ? 1 : 0;
+    if (!big[m] && T) sel.push_back(m);
+  }
+  mc[F] = cs.size();
+  const uint32_t nch = (uint32_t)cs.size();
+  const uint64_t nf = M.nfaces, nf1 = std::max<uint64_t>(nf, 1), F1 = std::max<uint32_t>(F, 1);
+  vf_status s;
+  if ((s = c.alloc(P.area, nf1 * 4)) || (s = c.alloc(P.cstart, std::max<uint32_t>(nch, 1) * 8)) ||
+      (s = c.alloc(P.cend, std::max<uint32_t>(nch, 1) * 8)) ||
+      (s = c.alloc(P.csum, std::max<uint32_t>(nch, 1) * 8)) ||
+      (s = c.alloc(P.cmax, std::max<uint32_t>(nch, 1) * 4)) || (s = c.alloc(P.mchunk, (F1 + 1) * 8)) ||
+      (s = c.alloc(P.msum, F1 * 4)) || (s = c.alloc(P.nb, F1 * 8)) || (s = c.alloc(P.big, F1)) ||
+      (s = c.alloc(P.sel, F1 * 4)) || (s = c.alloc(P.chosen, ((nf1 + 31) / 32) * 4)) ||
+      (s = c.alloc(P.err, 16)) || (s = c.alloc(P.cnt, nf1 * 4)) || (s = c.alloc(P.P, F1 * 8)) ||
+      (s = c.alloc(P.soff, (nf1 + 1) * 8)) || (s = c.alloc(P.sums, ((nf1 + 1023) / 1024 + 2) * 8)) ||
+      (s = c.alloc(P.out_off, (F1 + 1) * 8)))
+    return s;
+  if (nch) {
+    VF_CK(cudaMemcpyAsync(P.cstart.p, cs.data(), nch * 8, cudaMemcpyHostToDevice, st));
+    VF_CK(cudaMemcpyAsync(P.cend.p, ce.data(), nch * 8, cudaMemcpyHostToDevice, st));
+  }
+  VF_CK(cudaMemcpyAsync(P.mchunk.p, mc.data(), (F + 1) * 8, cudaMemcpyHostToDevice, st));
+  VF_CK(cudaMemcpyAsync(P.big.p, big.data(), big.size(), cudaMemcpyHostToDevice, st));
+  if (!sel.empty())
+    VF_CK(cudaMemcpyAsync(P.sel.p, sel.data(), sel.size() * 4, cudaMemcpyHostToDevice, st));
+  VF_CK(cudaMemsetAsync(P.chosen.p, 0, ((nf1 + 31) / 32) * 4, st));
+  VF_CK(cudaMemsetAsync(P.err.p, 0, 4, st));
+  const int nsm = c.num_sms;
+  auto msum = static_cast<float*>(P.msum.p);
+  auto nb = static_cast<uint64_t*>(P.nb.p);
+  auto bigd = static_cast<const uint8_t*>(P.big.p);
+  auto chosen = static_cast<uint32_t*>(P.chosen.p);
+  auto cnt = static_cast<uint32_t*>(P.cnt.p);
+  auto soff = static_cast<unsigned long long*>(P.soff.p);
+  vfk::pc_areas(st, M, static_cast<float*>(P.area.p), static_cast<const unsigned long long*>(P.cstart.p),
+                static_cast<const unsigned long long*>(P.cend.p), nch, static_cast<double*>(P.csum.p),
+                static_cast<float*>(P.cmax.p), static_cast<const unsigned long long*>(P.mchunk.p), S, msum,
+                nb, nsm);
+  vfk::pc_select(st, M, static_cast<const uint32_t*>(P.sel.p), (uint32_t)sel.size(), S, seed, chosen,
+                 static_cast<uint32_t*>(P.err.p));
+  vfk::pc_count(st, M, static_cast<const float*>(P.area.p), msum, bigd, S, chosen, cnt,
+                static_cast<unsigned long long*>(P.P.p), soff, static_cast<unsigned long long*>(P.sums.p),
+                nsm);
+  std::vector<unsigned long long> Pm(F1, 0);
+  uint32_t err = 0;
+  if (nf) VF_CK(cudaMemcpyAsync(Pm.data(), P.P.p, F * 8, cudaMemcpyDeviceToHost, st));
+  VF_CK(cudaMemcpyAsync(&err, P.err.p, 4, cudaMemcpyDeviceToHost, st));
+  VF_CK(cudaStreamSynchronize(st));
+  VF_CK(cudaGetLastError());
+  if (err) return fail(VF_ERR_RANGE, "sample: the face draws ran out before S distinct faces");
+  P.offsets.assign(F + 1, 0);
+  for (uint32_t m = 0; m < F; ++m) {
+    const uint64_t T = fo[m + 1] - fo[m];
+    const uint64_t n = !T ? 0 : (big[m] ? std::min<uint64_t>(Pm[m], S) : S);
+    P.offsets[m + 1] = P.offsets[m] + n;
+  }
+  P.npoints = P.offsets[F];
+  if ((s = c.alloc(P.out, std::max<uint64_t>(P.npoints, 1) * 16))) return s;
+  VF_CK(cudaMemcpyAsync(P.out_off.p, P.offsets.data(), (F + 1) * 8, cudaMemcpyHostToDevice, st));
+  vfk::pc_points(st, M, cnt, soff, nb, bigd, static_cast<const unsigned long long*>(P.out_off.p), S, seed,
+                 static_cast<float4*>(P.out.p), nsm);
+  VF_CK(cudaStreamSynchronize(st));
+  VF_CK(cudaGetLastError());
+  P.ready = true;
+  return VF_OK;
+}
+
+vf_status vf_grid_sample_meshes(vf_grid* g, uint32_t max_samples, uint64_t seed, uint64_t* point_offsets,
+                                uint64_t* npoints) {
+  if (!g || !npoints) return fail(VF_ERR_INVALID, "NULL argument");
+  MeshState& M = g->mesh;
+  if (!M.ready) return fail(VF_ERR_INVALID, "no meshes: call vf_grid_triangulate first");
+  cudaSetDevice(g->ctx->c.device);
+  vfr::Ctx& c = g->ctx->c;
+  SampleState& P = g->sample;
+  cudaStream_t st = g->b.stream;
+  const uint32_t F = (uint32_t)M.values.size();
+  std::vector<uint64_t> fo(F + 1, 0);
+  std::vector<uint32_t> keys(M.values.begin(), M.values.end());
+  vf_status s;
+  if ((s = c.alloc(P.keys, std::max<uint32_t>(F, 1) * 4))) return s;
+  if (F) {
+    VF_CK(cudaMemcpyAsync(fo.data(), M.foff.p, (F + 1) * 8, cudaMemcpyDeviceToHost, st));
+    VF_CK(cudaMemcpyAsync(P.keys.p, keys.data(), F * 4, cudaMemcpyHostToDevice, st));
+    VF_CK(cudaStreamSynchronize(st));
+  }
+  vfk::SampleMeshes SM{static_cast<const float4*>(M.vert.p), static_cast<const uint4*>(M.face.p),
+                       static_cast<const unsigned long long*>(M.voff.p),
+                       static_cast<const unsigned long long*>(M.foff.p),
+                       static_cast<const uint32_t*>(P.keys.p), F, M.T};
+  if (!F) {
+    P.offsets.assign(1, 0);
+    P.npoints = 0;
+    P.ready = true;
+  } else if ((s = sample_meshes(c, st, P, SM, fo, max_samples, seed))) {
+    return s;
+  }
+  *npoints = P.npoints;
+  if (point_offsets) std::memcpy(point_offsets, P.offsets.data(), P.offsets.size() * 8);
+  return VF_OK;
+}
+
+vf_status vf_grid_points(vf_grid* g, float* points) {
+  if (!g || !points) return fail(VF_ERR_INVALID, "NULL argument");
+  SampleState& P = g->sample;
+  if (!P.ready) return fail(VF_ERR_INVALID, "no points: call vf_grid_sample_meshes first");
+  cudaSetDevice(g->ctx->c.device);
+  if (P.npoints)
+    VF_CK(cudaMemcpyAsync(points, P.out.p, P.npoints * 16, cudaMemcpyDeviceToHost, g->b.stream));
+  VF_CK(cudaStreamSynchronize(g->b.stream));
+  return VF_OK;
+}
+
+vf_status vf_sample_mesh(vf_ctx* ctx, const float* verts, uint32_t nverts, const uint32_t* faces,
+                         uint32_t nfaces, uint32_t max_samples, uint64_t seed, float* points,
+                         uint64_t* npoints) {
+  if (!ctx || !npoints || (nfaces && (!verts || !faces)) || (max_samples && !points))
+    return fail(VF_ERR_INVALID, "NULL argument");
+  for (uint64_t i = 0; i < 3ull * nfaces; ++i)
+    if (faces[i] >= nverts) return fail(VF_ERR_INVALID, "face index out of range");
+  *npoints = 0;
+  if (!nfaces || !max_samples) return VF_OK;
+  cudaSetDevice(ctx->c.device);
+  vfr::Ctx& c = ctx->c;
+  SampleState P;
+  std::vector<float> v4(4 * (size_t)nverts);
+  std::vector<uint32_t> f4(4 * (size_t)nfaces);
+  for (uint32_t i = 0; i < nverts; ++i) {
+    v4[4 * (size_t)i] = verts[3 * (size_t)i];
+    v4[4 * (size_t)i + 1] = verts[3 * (size_t)i + 1];
+    v4[4 * (size_t)i + 2] = verts[3 * (size_t)i + 2];
+    v4[4 * (size_t)i + 3] = 0.0f;
+  }
+  for (uint32_t i = 0; i < nfaces; ++i) {
+    f4[4 * (size_t)i] = faces[3 * (size_t)i];
+    f4[4 * (size_t)i + 1] = faces[3 * (size_t)i + 1];
+    f4[4 * (size_t)i + 2] = faces[3 * (size_t)i + 2];
+    f4[4 * (size_t)i + 3] = 0;
+  }
+  const unsigned long long vo[2] = {0, nverts}, fo2[2] = {0, nfaces};
+  const uint32_t key = 0;
+  cudaStream_t st = c.stream;
+  vf_status s;
+  if ((s = c.alloc(P.verts, v4.size() * 4)) || (s = c.alloc(P.faces, f4.size() * 4)) ||
+      (s = c.alloc(P.voff, 16)) || (s = c.alloc(P.foff, 16)) || (s = c.alloc(P.keys, 4))) {
+    P.release(c);
+    return s;
+  }
+  cudaMemcpyAsync(P.verts.p, v4.data(), v4.size() * 4, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(P.faces.p, f4.data(), f4.size() * 4, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(P.voff.p, vo, 16, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(P.foff.p, fo2, 16, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(P.keys.p, &key, 4, cudaMemcpyHostToDevice, st);
+  vfk::SampleMeshes SM{static_cast<const float4*>(P.verts.p), static_cast<const uint4*>(P.faces.p),
+                       static_cast<const unsigned long long*>(P.voff.p),
+                       static_cast<const unsigned long long*>(P.foff.p),
+                       static_cast<const uint32_t*>(P.keys.p), 1, nfaces};
+  const std::vector<uint64_t> fo = {0, nfaces};
+  s = sample_meshes(c, st, P, SM, fo, max_samples, seed);
+  if (!s) {
+    if (P.npoints) {
+      const cudaError_t e = cudaMemcpy(points, P.out.p, P.npoints * 16, cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) s = fail(VF_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+    }
+    *npoints = P.npoints;
+  }
+  P.release(c);
+  return s;
 }
 
 vf_status vf_grid_meshes(vf_grid* g, uint16_t* values, uint64_t* vert_offsets,

@@ -133,6 +133,8 @@ __host__ __device__ __forceinline__ float vf_u01(uint64_t h) {
 #define VF_STREAM_IMPACT 4u  // nearSeeds: fragment pick and seed count per impact
 #define VF_STREAM_NEAR 5u    // nearSeeds: candidate offsets
 #define VF_NEAR_MAX_CANDIDATES (1u << 20)  // candidates one impact may try
+#define VF_STREAM_SAMPLE 6u       // point sampling: noise buffer
+#define VF_STREAM_SAMPLE_FACE 7u  // point sampling: face draws
 
 __host__ __device__ __forceinline__ uint32_t vf_roundup(uint32_t v, uint32_t m) {
   return (v + m - 1) / m * m;

@@ -128,6 +128,35 @@ void near_seeds(cudaStream_t st, const ImpactGrid& G, const uint32_t* frags, uin
                 uint32_t num_impacts, uint32_t num_seeds, uint32_t spreading, uint64_t seed,
                 uint32_t label0, uint32_t* chosen, uint32_t* out, uint32_t* status);
 
+// ---- point sampling of meshes (vf_sample.cu) ----
+struct SampleMeshes {
+  const float4* verts;  // x, y, z, (w)
+  const uint4* faces;   // three vertex indices within the mesh, (w)
+  const unsigned long long* vert_off;  // F + 1
+  const unsigned long long* face_off;  // F + 1
+  const uint32_t* keys;                // F: the noise and draw key of each mesh
+  uint32_t F;
+  uint64_t nfaces;
+};
+// areas, per-chunk sums (chunks of at most 1024 faces that start at each
+// mesh's first face: cstart/cend, mchunk[m] = first chunk of mesh m, F + 1),
+// per mesh sumArea (msum) and noise length (nb)
+void pc_areas(cudaStream_t st, const SampleMeshes& M, float* area, const unsigned long long* cstart,
+              const unsigned long long* cend, uint32_t nchunks, double* csum, float* cmax,
+              const unsigned long long* mchunk, uint32_t S, float* msum, uint64_t* nb, int num_sms);
+// for the meshes listed in sel (S <= T): S distinct faces into the bitmap
+// chosen (one bit per global face, zeroed); err bit 0 if the draws run out
+void pc_select(cudaStream_t st, const SampleMeshes& M, const uint32_t* sel, uint32_t nsel, uint32_t S,
+               uint64_t seed, uint32_t* chosen, uint32_t* err);
+// samples per face (cnt), their exclusive scan (soff, nfaces + 1), P per mesh
+void pc_count(cudaStream_t st, const SampleMeshes& M, const float* area, const float* msum,
+              const uint8_t* big, uint32_t S, const uint32_t* chosen, uint32_t* cnt,
+              unsigned long long* P, unsigned long long* soff, unsigned long long* sums, int num_sms);
+// the points (x, y, z, 1) of mesh m at out[out_off[m] ..]
+void pc_points(cudaStream_t st, const SampleMeshes& M, const uint32_t* cnt, const unsigned long long* soff,
+               const uint64_t* nb, const uint8_t* big, const unsigned long long* out_off, uint32_t S,
+               uint64_t seed, float4* out, int num_sms);
+
 // ---- seeds ----
 void sample_seeds(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs);
 
