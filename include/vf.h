@@ -90,10 +90,15 @@ typedef struct vf_params {
   float erosion_probability;  /* _erosionProbability */
   float erosion_threshold;    /* _erosionThreshold */
   int32_t boundary_size;      /* detectBoundaries(1) when not eroding */
+  int32_t num_impacts;        /* _numImpacts: > 0 places bias_seeds more main
+                                 seeds around impacts (Seeder::nearSeeds) */
+  int32_t bias_seeds;         /* _biasSeeds: seeds nearSeeds may place */
+  int32_t bias_focus;         /* _biasFocus: nearSeeds spreading */
 } vf_params;
 
 /* FractureParameters() defaults (FractureParameters.h:91-145), with
- * num_extra_seeds 0 and seed_location VF_OUTER as in CADScene.cpp:633. */
+ * num_extra_seeds 0 and seed_location VF_OUTER as in CADScene.cpp:633;
+ * num_impacts 0, bias_seeds 32, bias_focus 5. */
 void vf_params_default(vf_params* p);
 
 const char* vf_last_error(void);
@@ -196,8 +201,10 @@ vf_status vf_sample_seeds(vf_grid* g, uint32_t n, uint64_t seed, int location,
 vf_status vf_merge_seeds(const uint32_t* frags_xyzw, uint32_t nfrags,
                          uint32_t* seeds_xyzw, uint32_t nseeds, int distance);
 /* CADScene::fractureModel seed assembly (CADScene.cpp:628-655):
- * uniform(main, location) [+ uniform(extra, BOTH) + mergeSeeds].  out
- * holds 4*(2*num_seeds + num_extra_seeds) uint32; *nout gets the count. */
+ * uniform(main, location) [+ nearSeeds(num_impacts, bias_seeds, bias_focus)
+ * when num_impacts > 0] [+ uniform(extra, BOTH) + mergeSeeds].  out holds
+ * 4*(2*(num_seeds + bias_seeds) + num_extra_seeds) uint32; *nout gets the
+ * count. */
 vf_status vf_fracture_seeds(vf_grid* g, const vf_params* p, uint32_t* out_xyzw,
                             uint32_t* nout);
 

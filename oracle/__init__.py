@@ -42,7 +42,8 @@ class Params(C.Structure):
                 ("erosion_type", C.c_int32), ("erosion_size", C.c_int32),
                 ("erosion_iterations", C.c_int32),
                 ("erosion_probability", C.c_float),
-                ("erosion_threshold", C.c_float), ("boundary_size", C.c_int32)]
+                ("erosion_threshold", C.c_float), ("boundary_size", C.c_int32),
+                ("num_impacts", C.c_int32), ("bias_seeds", C.c_int32), ("bias_focus", C.c_int32)]
 
 
 def lib():
@@ -59,7 +60,8 @@ def lib():
             "vfo_grid_dims": (None, [P, P, u32, P]),
             "vfo_seeder_uniform": (i32, [P, u32, u32, u32, u32, u64, i32, P]),
             "vfo_merge_seeds": (i32, [P, u32, P, u32, i32]),
-            "vfo_fracture_seeds": (i32, [P, u32, u32, u32, u32, u32, i32, i32, u64, P, P]),
+            "vfo_fracture_seeds": (i32, [P, u32, u32, u32, u32, u32, i32, i32, u64, u32, u32,
+                                         u32, P, P]),
             "vfo_flood": (i32, [P, u32, u32, u32, P, u32, i32, P]),
             "vfo_naive": (i32, [P, u32, u32, u32, P, u32, i32]),
             "vfo_perturb": (i32, [P, u32, u32, u32, f32, u32, u64]),
@@ -134,14 +136,16 @@ def seeder_uniform(grid, n, seed, location):
     return out[:n]
 
 
-def fracture_seeds(grid, n_main, n_extra, location, merge_dfunc, seed):
+def fracture_seeds(grid, n_main, n_extra, location, merge_dfunc, seed, num_impacts=0,
+                   bias_seeds=32, bias_focus=5):
     g = np.ascontiguousarray(grid, dtype=np.uint16)
-    cap = 2 * n_main + n_extra
+    cap = 2 * (n_main + (bias_seeds if num_impacts else 0)) + n_extra
     out = np.zeros((max(cap, 1), 4), np.uint32)
     n = C.c_uint32(0)
     _check(lib().vfo_fracture_seeds(_p(g), *g.shape, int(n_main), int(n_extra),
-                                    int(location), int(merge_dfunc), int(seed),
-                                    _p(out), C.byref(n)), "fracture_seeds")
+                                    int(location), int(merge_dfunc), int(seed), int(num_impacts),
+                                    int(bias_seeds), int(bias_focus), _p(out), C.byref(n)),
+           "fracture_seeds")
     return out[:n.value]
 
 
@@ -216,7 +220,8 @@ def run_job(verts, faces, dims, aabb_min, aabb_max, params: Params, ncounts=3276
     f = np.ascontiguousarray(faces, dtype=np.uint32)
     g = np.empty((X, Y, Z), dtype=np.uint16)
     c = np.zeros(ncounts, np.uint32)
-    cap = 2 * params.num_seeds + params.num_extra_seeds
+    cap = 2 * (params.num_seeds + (params.bias_seeds if params.num_impacts > 0 else 0)) + \
+        params.num_extra_seeds
     s = np.zeros((max(cap, 1), 4), np.uint32)
     ns = C.c_uint32(0)
     mn, mx = _f3(aabb_min), _f3(aabb_max)

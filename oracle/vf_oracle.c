@@ -520,12 +520,29 @@ int vfo_merge_seeds(const uint32_t* frags, uint32_t nfrags, uint32_t* seeds,
 
 int vfo_fracture_seeds(const uint16_t* grid, uint32_t X, uint32_t Y, uint32_t Z,
                        uint32_t n_main, uint32_t n_extra, int location,
-                       int merge_dfunc, uint64_t seed, uint32_t* out,
+                       int merge_dfunc, uint64_t seed, uint32_t num_impacts,
+                       uint32_t bias_seeds, uint32_t bias_focus, uint32_t* out,
                        uint32_t* nout) {
   if (n_main > 254) return VFO_ERR_RANGE; /* 8-bit fragment ids 2..255 */
-  if ((uint64_t)2 * n_main + n_extra > MAX_SEEDS) return VFO_ERR_RANGE;
+  const uint32_t bias = num_impacts ? bias_seeds : 0u;
+  if ((uint64_t)2 * (n_main + bias) + n_extra > MAX_SEEDS) return VFO_ERR_RANGE;
   int st = vfo_seeder_uniform(grid, X, Y, Z, n_main, seed, location, out);
   if (st) return st;
+  if (num_impacts && n_main && bias_seeds) {
+    /* CADScene.cpp:636-638: seeds = nearSeeds(seeds, numImpacts, biasSeeds,
+     * biasFocus); the placed seeds become main seeds */
+    uint32_t* tmp = (uint32_t*)malloc(4 * sizeof(uint32_t) * (size_t)(n_main + bias_seeds));
+    if (!tmp) return VFO_ERR_RANGE;
+    uint32_t nn = 0;
+    st = vfo_near_seeds(grid, X, Y, Z, out, n_main, num_impacts, bias_seeds, bias_focus, seed, tmp, &nn);
+    if (!st) {
+      memcpy(out, tmp, 4 * sizeof(uint32_t) * (size_t)nn);
+      n_main = nn;
+    }
+    free(tmp);
+    if (st) return st;
+    if (n_main > 254) return VFO_ERR_RANGE;
+  }
   uint32_t total = n_main;
   if (n_extra > 0 && n_main > 0) {
     /* extraSeeds = uniform(BOTH); insert(begin, seeds); mergeSeeds(seeds,
@@ -937,12 +954,14 @@ int vfo_run_job(const float* verts, uint32_t nverts, const uint32_t* faces,
                 uint32_t ncounts, uint32_t* seeds_out, uint32_t* nseeds_out) {
   int st = vfo_voxelize(verts, nverts, faces, nfaces, X, Y, Z, aabb_min, aabb_max, grid, 3);
   if (st) return st;
-  uint32_t cap = 2 * (uint32_t)p->num_seeds + (uint32_t)p->num_extra_seeds;
+  const uint32_t bias = p->num_impacts > 0 ? (uint32_t)p->bias_seeds : 0u;
+  uint32_t cap = 2 * ((uint32_t)p->num_seeds + bias) + (uint32_t)p->num_extra_seeds;
   uint32_t* seeds = (uint32_t*)malloc(sizeof(uint32_t) * 4 * (cap ? cap : 1));
   uint32_t ns = 0;
   st = vfo_fracture_seeds(grid, X, Y, Z, (uint32_t)p->num_seeds,
                           (uint32_t)p->num_extra_seeds, p->seed_location,
-                          p->merge_distance, p->seed, seeds, &ns);
+                          p->merge_distance, p->seed, (uint32_t)(p->num_impacts > 0 ? p->num_impacts : 0),
+                          (uint32_t)p->bias_seeds, (uint32_t)p->bias_focus, seeds, &ns);
   if (!st) {
     if (p->algorithm == VFO_FLOOD) st = vfo_flood(grid, X, Y, Z, seeds, ns, p->distance, NULL);
     else if (p->algorithm == VFO_NAIVE) st = vfo_naive(grid, X, Y, Z, seeds, ns, p->distance);

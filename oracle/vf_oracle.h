@@ -85,12 +85,15 @@ int vfo_seeder_uniform(const uint16_t* grid, uint32_t X, uint32_t Y, uint32_t Z,
                        uint32_t* out_xyzw);
 int vfo_merge_seeds(const uint32_t* frags, uint32_t nfrags, uint32_t* seeds,
                     uint32_t nseeds, int dfunc);
-/* CADScene::fractureModel seed assembly (CADScene.cpp:624-655) without
- * impacts: uniform(main) [+ uniform(extra, BOTH) + mergeSeeds].  out must
- * hold 4*(n_main + n_main + n_extra) entries; *nout receives the count. */
+/* CADScene::fractureModel seed assembly (CADScene.cpp:624-655):
+ * uniform(main) [+ nearSeeds(num_impacts, bias_seeds, bias_focus) when
+ * num_impacts > 0, the placed seeds joining the main ones] [+ uniform(extra,
+ * BOTH) + mergeSeeds].  out must hold 4*(2*(n_main + bias_seeds) + n_extra)
+ * entries; *nout receives the count. */
 int vfo_fracture_seeds(const uint16_t* grid, uint32_t X, uint32_t Y, uint32_t Z,
                        uint32_t n_main, uint32_t n_extra, int location,
-                       int merge_dfunc, uint64_t seed, uint32_t* out,
+                       int merge_dfunc, uint64_t seed, uint32_t num_impacts,
+                       uint32_t bias_seeds, uint32_t bias_focus, uint32_t* out,
                        uint32_t* nout);
 
 /* ---- fracturers ---- */
@@ -131,6 +134,7 @@ typedef struct vfo_params {
   int32_t erode, erosion_type, erosion_size, erosion_iterations;
   float erosion_probability, erosion_threshold;
   int32_t boundary_size;
+  int32_t num_impacts, bias_seeds, bias_focus; /* nearSeeds after the main seeds */
 } vfo_params;
 
 int vfo_run_job(const float* verts, uint32_t nverts, const uint32_t* faces,

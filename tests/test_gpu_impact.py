@@ -118,3 +118,57 @@ def test_near_seeds_errors_match(vf, ctx):
         vf.Seeder.nearSeeds(g, frags, 1, 3, 0, 5)
     assert np.array_equal(vf.Seeder.nearSeeds(g, frags, 0, 3, 2, 5), frags)
     g.close()
+
+
+# ---- impacts inside CADScene::fractureModel (num_impacts > 0) ---------------
+def _job(name):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLD, "make_golden.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m.case_inputs(name)
+
+
+def _oracle_params(vf, p):
+    q = O.Params()
+    for name, _ in O.Params._fields_:
+        setattr(q, name, getattr(p, name))
+    return q
+
+
+@pytest.mark.parametrize("name,impacts,bias,focus,extra", [
+    ("flood_manhattan_48", 2, 32, 5, 0), ("flood_chebyshev_noise_60", 1, 12, 3, 0),
+    ("flood_extra_seeds_44", 3, 20, 5, 16)])
+def test_fracture_model_with_impacts(vf, ctx, name, impacts, bias, focus, extra):
+    v, f, mn, mx, dims, _, kw = _job(name)
+    kw = dict(kw, num_impacts=impacts, bias_seeds=bias, bias_focus=focus)
+    if extra:
+        kw["num_extra_seeds"] = extra
+    p = vf.Params.default(**kw)
+    g = vf.RegularGrid(dims, mn, mx, ctx)
+    g.fill(v, f)
+    seeds = vf.fracture_model(g, p)
+    lab, cnt, es = O.run_job(v, f, dims, mn, mx, _oracle_params(vf, p), ncounts=1024)
+    assert np.array_equal(seeds, es)
+    assert len(seeds) > p.num_seeds  # the impacts placed seeds
+    assert np.array_equal(g.data(), lab)
+    g.close()
+
+
+def test_batch_and_plain_paths_with_impacts(vf, ctx):
+    specs, exp = [], []
+    for name in ("flood_manhattan_48", "naive_euclid_40"):
+        v, f, mn, mx, dims, _, kw = _job(name)
+        p = vf.Params.default(**dict(kw, num_impacts=2, bias_seeds=16, bias_focus=4))
+        specs.append(vf.JobSpec(v, f, p, dims=dims, aabb=(mn, mx), ncounts=1024))
+        exp.append(O.run_job(v, f, dims, mn, mx, _oracle_params(vf, p), ncounts=1024))
+    res = vf.batch_run(specs, ctx)
+    for s, r, (lab, cnt, es) in zip(specs, res, exp):
+        assert r.status == 0 and r.nseeds == len(es)
+        assert np.array_equal(s.labels, lab)
+        assert np.array_equal(s.counts, cnt[:1024])
+    plain = [vf.JobSpec(s.verts, s.faces, s.params, dims=s.dims, aabb=s.aabb, ncounts=1024)
+             for s in specs]
+    vf.plain_run(plain, ctx)
+    for a, b in zip(plain, specs):
+        assert np.array_equal(a.labels, b.labels)

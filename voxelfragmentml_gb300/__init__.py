@@ -56,7 +56,8 @@ class Params(C.Structure):
                 ("erosion_type", C.c_int32), ("erosion_size", C.c_int32),
                 ("erosion_iterations", C.c_int32),
                 ("erosion_probability", C.c_float),
-                ("erosion_threshold", C.c_float), ("boundary_size", C.c_int32)]
+                ("erosion_threshold", C.c_float), ("boundary_size", C.c_int32),
+                ("num_impacts", C.c_int32), ("bias_seeds", C.c_int32), ("bias_focus", C.c_int32)]
 
     @classmethod
     def default(cls, **kw) -> "Params":
@@ -65,6 +66,11 @@ class Params(C.Structure):
         for k, v in kw.items():
             setattr(p, k, v)
         return p
+
+    def seed_capacity(self) -> int:
+        """Seeds fractureModel may use: 2 * (main + nearSeeds' bias) + extra."""
+        bias = self.bias_seeds if self.num_impacts > 0 else 0
+        return 2 * (self.num_seeds + bias) + self.num_extra_seeds
 
 
 class Job(C.Structure):
@@ -492,7 +498,7 @@ class Seeder:
 
     @staticmethod
     def fracture_seeds(grid: RegularGrid, params: Params):
-        cap = 2 * params.num_seeds + params.num_extra_seeds
+        cap = params.seed_capacity()
         out = np.zeros((max(cap, 1), 4), np.uint32)
         n = C.c_uint32()
         _check(lib().vf_fracture_seeds(grid.h, C.byref(params), _p(out), C.byref(n)))
@@ -536,7 +542,7 @@ class NaiveFracturer(_Fracturer):
 
 def fracture_model(grid: RegularGrid, params: Params):
     """CADScene::fractureModel on a voxelized grid; returns the seeds used."""
-    cap = 2 * params.num_seeds + params.num_extra_seeds
+    cap = params.seed_capacity()
     out = np.zeros((max(cap, 1), 4), np.uint32)
     n = C.c_uint32()
     _check(lib().vf_fracture_model(grid.h, C.byref(params), _p(out), C.byref(n)))

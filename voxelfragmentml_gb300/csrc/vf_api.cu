@@ -120,6 +120,9 @@ void vf_params_default(vf_params* p) {
   p->erosion_probability = 0.5f;
   p->erosion_threshold = 0.5f;
   p->boundary_size = 1;            // detectBoundaries(1)
+  p->num_impacts = 0;    // _numImpacts(0)
+  p->bias_seeds = 32;    // _biasSeeds(32)
+  p->bias_focus = 5;     // _biasFocus(5)
 }
 
 const char* vf_last_error(void) { return vfr::last_error(); }
@@ -875,6 +878,7 @@ vf_status vf_sample_seeds(vf_grid* g, uint32_t n, uint64_t seed, int location, u
   vf_params saved = g->job.params;
   g->job.params.num_seeds = (int32_t)n;
   g->job.params.num_extra_seeds = 0;
+  g->job.params.num_impacts = 0;
   g->job.params.seed = seed;
   g->job.params.seed_location = location;
   g->b.given.clear();

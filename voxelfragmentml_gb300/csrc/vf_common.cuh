@@ -82,6 +82,7 @@ struct JobDesc {
   int32_t erode, erosion_type, erosion_size, erosion_iterations;
   float erosion_probability, erosion_threshold;
   int32_t boundary_size;
+  int32_t num_impacts, bias_seeds, bias_focus;  // Seeder::nearSeeds after the main seeds
   float* lattice;       // perturbation lattice values, 3 per point
   uint32_t lat_nx, lat_ny, lat_nz;
   // label download: device-accessible destination (mapped pinned host memory

@@ -224,8 +224,13 @@ static vf_status check_params(const vf_params& p, uint32_t& ek) {
   if (p.distance < 0 || p.distance > 2 || p.merge_distance < 0 || p.merge_distance > 2)
     return fail(VF_ERR_INVALID, "distance function out of range");
   if (p.num_seeds < 0 || p.num_seeds > 254) return fail(VF_ERR_RANGE, "num_seeds must be in [0, 254]");
-  if (p.num_extra_seeds < 0 || 2 * p.num_seeds + p.num_extra_seeds > (int)VF_MAX_SEEDS)
-    return fail(VF_ERR_RANGE, "2*num_seeds + num_extra_seeds must be <= 4095");
+  if (p.num_impacts < 0 || p.num_impacts > (1 << 20))
+    return fail(VF_ERR_INVALID, "num_impacts must be in [0, 2^20]");
+  if (p.num_impacts > 0 && (p.bias_seeds < 0 || p.bias_seeds > 254 || p.bias_focus < 1))
+    return fail(VF_ERR_INVALID, "bias_seeds must be in [0, 254] and bias_focus >= 1");
+  const int bias = p.num_impacts > 0 ? p.bias_seeds : 0;
+  if (p.num_extra_seeds < 0 || 2 * (p.num_seeds + bias) + p.num_extra_seeds > (int)VF_MAX_SEEDS)
+    return fail(VF_ERR_RANGE, "2*(num_seeds + bias_seeds) + num_extra_seeds must be <= 4095");
   if (p.seed_location < VF_INNER || p.seed_location > VF_BOTH)
     return fail(VF_ERR_INVALID, "seed_location out of range");
   if (!(p.noise_amplitude >= 0.0f) || p.noise_amplitude > 64.0f)
@@ -307,7 +312,8 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
     p.nbx = (p.X + VF_BX - 1) / VF_BX; p.nby = (p.Y + VF_BY - 1) / VF_BY; p.nbz = (p.Z + VF_BZ - 1) / VF_BZ;
     p.nbricks = p.nbx * p.nby * p.nbz;
     p.ncounts = std::max(j.ncounts, 256u);
-    p.seeds_cap = std::max<uint32_t>(2 * j.params.num_seeds + j.params.num_extra_seeds, 1);
+    const int32_t bias = j.params.num_impacts > 0 ? j.params.bias_seeds : 0;
+    p.seeds_cap = std::max<uint32_t>(2 * (j.params.num_seeds + bias) + j.params.num_extra_seeds, 1);
     const uint32_t ngiven = i < given.size() ? given[i].second : 0u;
     if (ngiven > VF_MAX_SEEDS) return fail(VF_ERR_RANGE, "at most 4095 seeds");
     p.seeds_cap = std::max(p.seeds_cap, ngiven);
@@ -442,6 +448,7 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
     d.erode = q.erode; d.erosion_type = q.erosion_type; d.erosion_size = q.erosion_size;
     d.erosion_iterations = q.erosion_iterations; d.erosion_probability = q.erosion_probability;
     d.erosion_threshold = q.erosion_threshold; d.boundary_size = q.boundary_size;
+    d.num_impacts = q.num_impacts; d.bias_seeds = q.bias_seeds; d.bias_focus = q.bias_focus;
     d.lattice = static_cast<float*>(lat.p) + p.o_lat;
     d.lat_nx = p.lat_nx; d.lat_ny = p.lat_ny; d.lat_nz = p.lat_nz;
     d.emask = static_cast<float*>(emask.p) + p.o_emask;
