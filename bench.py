@@ -635,6 +635,13 @@ def mesh_bench(args):
         clouds = g.samplePointClouds(1024, 80)
         if i:
             pc_wall.append(time.perf_counter() - t)
+    # RegularGrid::exportRLE of the same labels (the dataset's grid format)
+    rle_wall = []
+    for i in range(args.steps + 1):
+        t = time.perf_counter()
+        rle = g.exportRLE()
+        if i:
+            rle_wall.append(time.perf_counter() - t)
     clk = clocks.stop()
     st = g.mesh_phase_ms()
     cnt = g.mesh_counters()
@@ -648,6 +655,10 @@ def mesh_bench(args):
     cpu_pc_s = time.perf_counter() - t
     pc_parity = len(e_pc) == len(clouds) and all(
         np.array_equal(a.view(np.uint32), b.view(np.uint32)) for a, b in zip(clouds, e_pc))
+    t = time.perf_counter()
+    e_rle = O.rle_encode(labels)
+    cpu_rle_s = time.perf_counter() - t
+    rle_parity = bytes(e_rle) == rle
     parity = (np.array_equal(hvals[:F], e[0]) and np.array_equal(hvo, e[1]) and
               np.array_equal(hfo, e[2]) and np.array_equal(hf, e[4]) and
               np.array_equal(hv.view(np.uint32), e[3].view(np.uint32)))
@@ -697,11 +708,14 @@ def mesh_bench(args):
         "point_clouds": {"points_per_mesh": 1024, "meshes": F,
                          "ms": 1e3 * statistics.median(pc_wall),
                          "cpu_oracle_ms": 1e3 * cpu_pc_s, "parity_with_oracle": bool(pc_parity)},
+        "rle_export": {"bytes": len(rle), "ms": 1e3 * statistics.median(rle_wall),
+                       "note": "vf_grid_export_rle: size query + records to host",
+                       "cpu_oracle_ms": 1e3 * cpu_rle_s, "parity_with_oracle": bool(rle_parity)},
         "clocks": clk,
     }), flush=True)
     g.close()
     ctx.close()
-    return 0 if (parity and pc_parity) else 1
+    return 0 if (parity and pc_parity and rle_parity) else 1
 
 
 def impact_rays(mn, mx, n, seed=5):
