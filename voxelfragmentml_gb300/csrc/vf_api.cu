@@ -67,9 +67,9 @@ struct MeshState {
 
 // device scratch of the impact path (rays, nearSeeds)
 struct ImpactState {
-  vfr::DevBuf rays, hits, frags, chosen, out, status;
+  vfr::DevBuf rays, hits, frags, out, status;
   void release(vfr::Ctx& c) {
-    for (vfr::DevBuf* b : {&rays, &hits, &frags, &chosen, &out, &status}) c.free_buf(*b);
+    for (vfr::DevBuf* b : {&rays, &hits, &frags, &out, &status}) c.free_buf(*b);
   }
 };
 
@@ -823,15 +823,15 @@ vf_status vf_near_seeds(vf_grid* g, const uint32_t* frags_xyzw, uint32_t nfrags,
   vfr::Ctx& c = g->ctx->c;
   ImpactState& I = g->impact;
   vf_status s;
-  if ((s = c.alloc(I.frags, (size_t)nfrags * 16)) || (s = c.alloc(I.chosen, (size_t)num_seeds * 12)) ||
-      (s = c.alloc(I.out, (size_t)num_seeds * 16)) || (s = c.alloc(I.status, 16)))
+  if ((s = c.alloc(I.frags, (size_t)nfrags * 16)) || (s = c.alloc(I.out, (size_t)num_seeds * 16)) ||
+      (s = c.alloc(I.status, 16)))
     return s;
   cudaStream_t st = g->b.stream;
   VF_CK(cudaMemcpyAsync(I.frags.p, frags_xyzw, (size_t)nfrags * 16, cudaMemcpyHostToDevice, st));
   const uint32_t label0 = frags_xyzw[4 * (nfrags - 1) + 3];
   vfk::near_seeds(st, impact_grid(g), static_cast<const uint32_t*>(I.frags.p), nfrags, num_impacts,
-                  num_seeds, spreading, seed, label0, static_cast<uint32_t*>(I.chosen.p),
-                  static_cast<uint32_t*>(I.out.p), static_cast<uint32_t*>(I.status.p));
+                  num_seeds, spreading, seed, label0, static_cast<uint32_t*>(I.out.p),
+                  static_cast<uint32_t*>(I.status.p));
   uint32_t status[2] = {0, 0};
   VF_CK(cudaMemcpyAsync(status, I.status.p, 8, cudaMemcpyDeviceToHost, st));
   VF_CK(cudaStreamSynchronize(st));

@@ -14,6 +14,7 @@
 #include <algorithm>
 
 #include "vf_kernels.h"
+#include "vf_near.cuh"
 
 #include <cfloat>
 
@@ -173,102 +174,23 @@ __device__ bool uniform_block(const JobDesc& J, SeedSmem& S, uint32_t n, uint64_
   return true;
 }
 
-// Seeder::nearSeeds (Seeder.cpp:49-113) on the job's occupancy grid, after
-// its nf main seeds in `seeds`: appends the placed seeds in (x, y, z) order,
-// labelled on from the last main seed; returns their count, or -1 when an
-// impact's 2^20 candidates run out (the same candidates, draws and order as
-// vf_near_seeds).  1024 candidates per round are tested in parallel, warp 0
-// keeps the first valid ones in candidate order.
+// Seeder::nearSeeds (vfnear::place) on the job's occupancy grid, after its nf
+// main seeds in `seeds`: appends the placed seeds, labelled on from the last
+// main seed; returns their count, or -1 when an impact runs out of candidates
+struct JobGrid {
+  const JobDesc& J;
+  __device__ bool occupied(uint32_t x, uint32_t y, uint32_t z) const {
+    return occupied_at(J, (int)x, (int)y, (int)z);
+  }
+  __device__ bool boundary(uint32_t x, uint32_t y, uint32_t z) const {
+    return is_boundary(J, (int)x, (int)y, (int)z);
+  }
+};
+
 __device__ int near_block(const JobDesc& J, SeedSmem& S, uint32_t* seeds, uint32_t nf) {
-  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  const uint32_t dims[3] = {J.X, J.Y, J.Z}, half[3] = {J.X / 2, J.Y / 2, J.Z / 2};
-  const uint32_t mind = min(J.X, min(J.Y, J.Z));
-  const float minDiv = (float)(mind / 2);
-  const uint32_t spreading = (uint32_t)J.bias_focus;
-  const uint64_t seed = J.seed;
-  if (t == 0) { S.cnt = 0; S.fail = 0; }
-  __syncthreads();
-  uint32_t pending = (uint32_t)J.bias_seeds;
-  for (uint32_t i = 0; i < (uint32_t)J.num_impacts; ++i) {
-    const uint32_t fi = (uint32_t)__fmul_rn(vf_u01(vf_hash(seed, VF_STREAM_IMPACT, 2ull * i)), (float)nf);
-    const uint32_t* f = seeds + 4 * (uint64_t)min(fi, nf - 1);
-    if (!pending) continue;
-    uint32_t want =
-        1u + (uint32_t)__fmul_rn(vf_u01(vf_hash(seed, VF_STREAM_IMPACT, 2ull * i + 1)), (float)pending);
-    if (want > pending) want = pending;
-    const uint32_t goal = S.cnt + want;
-    for (uint64_t k0 = 0; k0 < VF_NEAR_MAX_CANDIDATES; k0 += 1024) {
-      const uint64_t k = k0 + t;
-      uint32_t v[3];
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const uint32_t m = dims[a] / spreading;
-        uint32_t bsum = 0;
-        for (uint32_t jj = 0; jj < spreading; ++jj) {
-          const uint64_t ctr = ((uint64_t)i << 44) + (k * 3u + (uint64_t)a) * spreading + jj;
-          bsum += (uint32_t)(vf_hash(seed, VF_STREAM_NEAR, ctr) >> 33) % m;
-        }
-        const int64_t off = (int64_t)half[a] - (int64_t)bsum;
-        v[a] = (uint32_t)(((int64_t)f[a] + off + (int64_t)dims[a]) % (int64_t)dims[a]);
-      }
-      const float dx = __fsub_rn((float)f[0], (float)v[0]), dy = __fsub_rn((float)f[1], (float)v[1]),
-                  dz = __fsub_rn((float)f[2], (float)v[2]);
-      const float dist = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
-      bool good = k < VF_NEAR_MAX_CANDIDATES && !(dist > minDiv) && occupied_at(J, (int)v[0], (int)v[1], (int)v[2]);
-      if (good) good = is_boundary(J, (int)v[0], (int)v[1], (int)v[2]);
-      S.cand[t] = good ? (((unsigned long long)v[0] << 24) | ((unsigned long long)v[1] << 12) | v[2]) : ~0ull;
-      __syncthreads();
-      if (warp == 0) {
-        uint32_t cnt = S.cnt;
-        for (int c = 0; c < 1024 && cnt < goal; ++c) {
-          const unsigned long long key = S.cand[c];
-          if (key == ~0ull) continue;
-          bool dup = false;
-          for (uint32_t m = lane; m < cnt; m += 32) dup |= (S.acc[m] == key);
-          dup = __any_sync(0xFFFFFFFFu, dup);
-          if (!dup) {
-            if (lane == 0) S.acc[cnt] = key;
-            ++cnt;
-          }
-          __syncwarp();
-        }
-        if (lane == 0) S.cnt = cnt;
-      }
-      __syncthreads();
-      if (S.cnt >= goal) break;
-    }
-    if (S.cnt < goal) return -1;
-    pending -= want;
-  }
-  const uint32_t n = S.cnt;
-  // (x, y, z) order, labels on from the last main seed
-  const uint32_t label0 = seeds[4 * (nf - 1) + 3];
-  uint32_t P = 1;
-  while (P < n) P <<= 1;
-  for (uint32_t q = n + t; q < P; q += blockDim.x) S.acc[q] = ~0ull;
-  __syncthreads();
-  for (uint32_t kk = 2; kk <= P; kk <<= 1)
-    for (uint32_t jx = kk >> 1; jx > 0; jx >>= 1) {
-      for (uint32_t q = t; q < P; q += blockDim.x) {
-        const uint32_t l = q ^ jx;
-        if (l > q) {
-          const unsigned long long a = S.acc[q], b = S.acc[l];
-          const bool up = (q & kk) == 0;
-          if ((a > b) == up) { S.acc[q] = b; S.acc[l] = a; }
-        }
-      }
-      __syncthreads();
-    }
-  uint32_t* out = seeds + 4 * (uint64_t)nf;
-  for (uint32_t q = t; q < n; q += blockDim.x) {
-    const unsigned long long key = S.acc[q];
-    out[4 * q] = (uint32_t)(key >> 24);
-    out[4 * q + 1] = (uint32_t)((key >> 12) & 0xFFF);
-    out[4 * q + 2] = (uint32_t)(key & 0xFFF);
-    out[4 * q + 3] = label0 + 1 + q;
-  }
-  __syncthreads();
-  return (int)n;
+  return vfnear::place(JobGrid{J}, J.X, J.Y, J.Z, seeds, nf, (uint32_t)J.num_impacts,
+                       (uint32_t)J.bias_seeds, (uint32_t)J.bias_focus, J.seed, seeds[4 * (nf - 1) + 3],
+                       S.cand, S.acc, &S.cnt, seeds + 4 * (uint64_t)nf);
 }
 
 __device__ __forceinline__ float seed_dist(int dfunc, const uint32_t* s, const uint32_t* f) {

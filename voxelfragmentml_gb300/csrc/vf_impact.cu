@@ -9,17 +9,15 @@
 //                 Amanatides-Woo walk in its operation order (every float
 //                 step rounded as written); the walk is bounded by
 //                 X + Y + Z + 3 steps, more than a ray can take
-//   k_near_seeds  one CTA: impacts in order; per impact, rounds of 256
-//                 candidates drawn from the counter-based hash and tested in
-//                 parallel (distance to the impact's fragment seed, occupied,
-//                 an EMPTY voxel in the clamped 3x3x3 box, not chosen
-//                 before); the first valid ones in candidate order are kept;
-//                 at the end the chosen voxels are ranked in (x, y, z) order
-//                 (the reference's std::set) and labelled
+//   k_near_seeds  one CTA running vfnear::place (vf_near.cuh): impacts in
+//                 order, rounds of 256 candidates tested in parallel, the
+//                 first valid ones in candidate order kept, then sorted in
+//                 (x, y, z) order (the reference's std::set) and labelled
 #include <cfloat>
 
 #include "vf.h"
 #include "vf_kernels.h"
+#include "vf_near.cuh"
 
 namespace {
 
@@ -131,126 +129,36 @@ __global__ void __launch_bounds__(256) k_ray_entry(vfk::ImpactGrid G, const floa
   }
 }
 
-__device__ bool is_boundary(const vfk::ImpactGrid& G, int x, int y, int z) {
-  const int lo0 = max(x - 1, 0), lo1 = max(y - 1, 0), lo2 = max(z - 1, 0);
-  const int hi0 = min(x + 1, (int)G.X - 1), hi1 = min(y + 1, (int)G.Y - 1), hi2 = min(z + 1, (int)G.Z - 1);
-  for (int i = lo0; i <= hi0; ++i)
-    for (int j = lo1; j <= hi1; ++j)
-      for (int k = lo2; k <= hi2; ++k)
-        if (gat(G, (uint32_t)i, (uint32_t)j, (uint32_t)k) == EMPTY) return true;
-  return false;
-}
-
-__device__ __forceinline__ uint32_t biased(uint64_t seed, uint32_t impact, uint64_t cand, int axis,
-                                           uint32_t n, uint32_t spreading) {
-  const uint32_t m = n / spreading;
-  uint32_t s = 0;
-  for (uint32_t j = 0; j < spreading; ++j) {
-    const uint64_t ctr = ((uint64_t)impact << 44) + (cand * 3u + (uint64_t)axis) * spreading + j;
-    s += (uint32_t)(vf_hash(seed, VF_STREAM_NEAR, ctr) >> 33) % m;
+struct ImpactView {
+  const vfk::ImpactGrid& G;
+  __device__ bool occupied(uint32_t x, uint32_t y, uint32_t z) const { return gat(G, x, y, z) != EMPTY; }
+  // RegularGrid::isBoundary(x, y, z, 1) (RegularGrid.cpp:543-559)
+  __device__ bool boundary(uint32_t x, uint32_t y, uint32_t z) const {
+    const int lo0 = max((int)x - 1, 0), lo1 = max((int)y - 1, 0), lo2 = max((int)z - 1, 0);
+    const int hi0 = min((int)x + 1, (int)G.X - 1), hi1 = min((int)y + 1, (int)G.Y - 1),
+              hi2 = min((int)z + 1, (int)G.Z - 1);
+    for (int i = lo0; i <= hi0; ++i)
+      for (int j = lo1; j <= hi1; ++j)
+        for (int k = lo2; k <= hi2; ++k)
+          if (gat(G, (uint32_t)i, (uint32_t)j, (uint32_t)k) == EMPTY) return true;
+    return false;
   }
-  return s;
-}
+};
 
-// status[0] = chosen count, status[1] = 0 or VF_ERR_SEED_SEARCH
+// status[0] = count placed, status[1] = 0 or VF_ERR_SEED_SEARCH
 __global__ void __launch_bounds__(256) k_near_seeds(vfk::ImpactGrid G, const uint32_t* frags,
                                                     uint32_t nfrags, uint32_t num_impacts,
                                                     uint32_t num_seeds, uint32_t spreading,
-                                                    uint64_t seed, uint32_t label0, uint32_t* chosen,
-                                                    uint32_t* out, uint32_t* status) {
-  __shared__ uint32_t cand[256][3];
-  __shared__ uint8_t ok[256];
-  __shared__ uint32_t s_nch, s_got, s_fail;
-  const uint32_t t = threadIdx.x;
-  if (t == 0) {
-    s_nch = 0;
-    s_fail = 0;
-  }
-  __syncthreads();
-  const uint32_t dims[3] = {G.X, G.Y, G.Z}, half[3] = {G.X / 2, G.Y / 2, G.Z / 2};
-  const uint32_t mind = min(G.X, min(G.Y, G.Z));
-  const float minDiv = (float)(mind / 2);
-  uint32_t pending = num_seeds;
-  for (uint32_t i = 0; i < num_impacts; ++i) {
-    const uint32_t fi = (uint32_t)__fmul_rn(vf_u01(vf_hash(seed, VF_STREAM_IMPACT, 2ull * i)), (float)nfrags);
-    const uint32_t* f = frags + 4 * (uint64_t)min(fi, nfrags - 1);
-    if (!pending) continue;
-    uint32_t want =
-        1u + (uint32_t)__fmul_rn(vf_u01(vf_hash(seed, VF_STREAM_IMPACT, 2ull * i + 1)), (float)pending);
-    if (want > pending) want = pending;
-    if (t == 0) s_got = 0;
-    __syncthreads();
-    for (uint64_t k0 = 0; k0 < VF_NEAR_MAX_CANDIDATES; k0 += 256) {
-      const uint64_t k = k0 + t;
-      uint32_t v[3];
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const int64_t off = (int64_t)half[a] - (int64_t)biased(seed, i, k, a, dims[a], spreading);
-        v[a] = (uint32_t)(((int64_t)f[a] + off + (int64_t)dims[a]) % (int64_t)dims[a]);
-      }
-      const float dx = __fsub_rn((float)f[0], (float)v[0]), dy = __fsub_rn((float)f[1], (float)v[1]),
-                  dz = __fsub_rn((float)f[2], (float)v[2]);
-      const float dist = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
-      bool good = k < VF_NEAR_MAX_CANDIDATES && !(dist > minDiv) && gat(G, v[0], v[1], v[2]) != EMPTY;
-      const uint32_t nprev = s_nch;
-      for (uint32_t c = 0; c < nprev && good; ++c)
-        good = !(chosen[3 * c] == v[0] && chosen[3 * c + 1] == v[1] && chosen[3 * c + 2] == v[2]);
-      if (good) good = is_boundary(G, (int)v[0], (int)v[1], (int)v[2]);
-      cand[t][0] = v[0];
-      cand[t][1] = v[1];
-      cand[t][2] = v[2];
-      ok[t] = good ? 1 : 0;
-      __syncthreads();
-      if (t == 0) {
-        // candidate order; a repeat within this round counts once
-        uint32_t nch = s_nch, got = s_got;
-        for (uint32_t j = 0; j < 256 && got < want; ++j) {
-          if (!ok[j]) continue;
-          bool dup = false;
-          for (uint32_t c = nprev; c < nch && !dup; ++c)
-            dup = chosen[3 * c] == cand[j][0] && chosen[3 * c + 1] == cand[j][1] &&
-                  chosen[3 * c + 2] == cand[j][2];
-          if (dup) continue;
-          chosen[3 * nch] = cand[j][0];
-          chosen[3 * nch + 1] = cand[j][1];
-          chosen[3 * nch + 2] = cand[j][2];
-          ++nch;
-          ++got;
-        }
-        s_nch = nch;
-        s_got = got;
-      }
-      __syncthreads();
-      if (s_got >= want) break;
-    }
-    if (s_got < want) {
-      if (t == 0) s_fail = 1;
-      break;
-    }
-    pending -= want;
-    __syncthreads();
-  }
-  __syncthreads();
-  const uint32_t nch = s_nch;
-  if (!s_fail) {
-    // rank in (x, y, z) order; chosen voxels are distinct
-    for (uint32_t c = t; c < nch; c += blockDim.x) {
-      const uint32_t x = chosen[3 * c], y = chosen[3 * c + 1], z = chosen[3 * c + 2];
-      uint32_t rank = 0;
-      for (uint32_t e = 0; e < nch; ++e) {
-        const uint32_t ex = chosen[3 * e], ey = chosen[3 * e + 1], ez = chosen[3 * e + 2];
-        rank += (ex < x || (ex == x && (ey < y || (ey == y && ez < z)))) ? 1u : 0u;
-      }
-      uint32_t* o = out + 4 * (uint64_t)rank;
-      o[0] = x;
-      o[1] = y;
-      o[2] = z;
-      o[3] = label0 + rank + 1;
-    }
-  }
-  if (t == 0) {
-    status[0] = nch;
-    status[1] = s_fail ? (uint32_t)VF_ERR_SEED_SEARCH : 0u;
+                                                    uint64_t seed, uint32_t label0, uint32_t* out,
+                                                    uint32_t* status) {
+  __shared__ unsigned long long cand[256];
+  __shared__ unsigned long long acc[4096];
+  __shared__ uint32_t cnt;
+  const int n = vfnear::place(ImpactView{G}, G.X, G.Y, G.Z, frags, nfrags, num_impacts, num_seeds,
+                              spreading, seed, label0, cand, acc, &cnt, out);
+  if (threadIdx.x == 0) {
+    status[0] = n < 0 ? 0u : (uint32_t)n;
+    status[1] = n < 0 ? (uint32_t)VF_ERR_SEED_SEARCH : 0u;
   }
 }
 
@@ -267,9 +175,9 @@ void ray_entry(cudaStream_t st, const ImpactGrid& G, const float* rays, uint32_t
 
 void near_seeds(cudaStream_t st, const ImpactGrid& G, const uint32_t* frags, uint32_t nfrags,
                 uint32_t num_impacts, uint32_t num_seeds, uint32_t spreading, uint64_t seed,
-                uint32_t label0, uint32_t* chosen, uint32_t* out, uint32_t* status) {
+                uint32_t label0, uint32_t* out, uint32_t* status) {
   k_near_seeds<<<1, 256, 0, st>>>(G, frags, nfrags, num_impacts, num_seeds, spreading, seed, label0,
-                                  chosen, out, status);
+                                  out, status);
 }
 
 }  // namespace vfk

@@ -121,12 +121,12 @@ struct ImpactGrid {
 void ray_entry(cudaStream_t st, const ImpactGrid& G, const float* rays, uint32_t n, uint32_t* out,
                int num_sms);
 // Seeder::nearSeeds: the new seeds (4 uint32 each, labels label0 + 1, ...)
-// in (x, y, z) order into out; chosen: 3 * num_seeds scratch; status[0] =
-// count, status[1] = 0 or VF_ERR_SEED_SEARCH.  Needs nfrags >= 1 and
+// in (x, y, z) order into out; status[0] = count, status[1] = 0 or
+// VF_ERR_SEED_SEARCH.  Needs nfrags >= 1, num_seeds <= 4095 and
 // 1 <= spreading <= min(dims) when num_impacts > 0.
 void near_seeds(cudaStream_t st, const ImpactGrid& G, const uint32_t* frags, uint32_t nfrags,
                 uint32_t num_impacts, uint32_t num_seeds, uint32_t spreading, uint64_t seed,
-                uint32_t label0, uint32_t* chosen, uint32_t* out, uint32_t* status);
+                uint32_t label0, uint32_t* out, uint32_t* status);
 
 // ---- point sampling of meshes (vf_sample.cu) ----
 struct SampleMeshes {
