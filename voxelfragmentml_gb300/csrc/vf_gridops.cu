@@ -384,7 +384,12 @@ __global__ void __launch_bounds__(256) k_perturb(const JobDesc* jobs, const uint
   // the thread's row of labels (34-u16 pitch: the u16 of one z from 32
   // threads falls on 32 distinct banks)
   __shared__ __align__(16) uint16_t vrows[256 * 34];
-  uint16_t* v = vrows + threadIdx.x * 34;
+  // the brick's labelled voxels (row << 5 | z), dealt to all threads: the
+  // labelled voxels of a thin wall are few and uneven per row
+  __shared__ uint16_t vq[256 * VF_BZ];
+  __shared__ uint32_t wq[8];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  uint16_t* v = vrows + t * 34;
   const uint32_t n = *count;
   for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
     const uint32_t b = list[it];
@@ -394,67 +399,77 @@ __global__ void __launch_bounds__(256) k_perturb(const JobDesc* jobs, const uint
     brick_coords(J, b, x0, y0, z0);
     const uint32_t P = J.noise_period;
     const float fp = (float)P;
-    __syncthreads();  // the previous brick's rows are done with the tables
-    if (threadIdx.x < VF_BZ) {
-      const uint32_t gz = z0 + threadIdx.x;
-      t2s[threadIdx.x] = __fdiv_rn((float)(gz % P), fp);
-      i2s[threadIdx.x] = gz / P;
+    __syncthreads();  // the previous brick is done with the tables, rows and queue
+    if (t < VF_BZ) {
+      const uint32_t gz = z0 + t;
+      t2s[t] = __fdiv_rn((float)(gz % P), fp);
+      i2s[t] = gz / P;
+    }
+    const uint32_t x = x0 + t / VF_BY, y = y0 + t % VF_BY;
+    const bool rowok = x < J.X && y < J.Y;
+    const uint16_t* src = J.grid;
+    uint32_t m = 0;  // labelled z of this row
+    if (rowok) {
+      const uint4* s4 = reinterpret_cast<const uint4*>(src + vf_gidx(J, x, y, z0));
+      const uint32_t nz = min((uint32_t)VF_BZ, J.Zp - z0);
+      uint32_t* v32 = reinterpret_cast<uint32_t*>(v);  // 4-byte aligned: 68-byte pitch
+#pragma unroll
+      for (int q = 0; q < VF_BZ / 8; ++q) {
+        const uint4 w = (q * 8 < (int)nz) ? s4[q] : make_uint4(0, 0, 0, 0);
+        v32[4 * q + 0] = w.x; v32[4 * q + 1] = w.y; v32[4 * q + 2] = w.z; v32[4 * q + 3] = w.w;
+      }
+#pragma unroll
+      for (int z = 0; z < VF_BZ; ++z) m |= (uint32_t)(v[z] > VOXEL_FREE) << z;
+    }
+    const uint32_t c = (uint32_t)__popc(m);
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+      if (lane >= o) incl += u;
+    }
+    if (lane == 31) wq[warp] = incl;
+    __syncthreads();
+    uint32_t base = incl - c, total = 0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) {
+      base += w < warp ? wq[w] : 0u;
+      total += wq[w];
+    }
+    while (m) {
+      const uint32_t z = (uint32_t)__ffs(m) - 1;
+      m &= m - 1;
+      vq[base++] = (uint16_t)((t << 5) | z);
     }
     __syncthreads();
-    const uint32_t x = x0 + threadIdx.x / VF_BY, y = y0 + threadIdx.x % VF_BY;
-    if (x >= J.X || y >= J.Y) continue;
-    const uint16_t* src = J.grid;
-    const uint4* s4 = reinterpret_cast<const uint4*>(src + vf_gidx(J, x, y, z0));
-    const uint32_t nz = min((uint32_t)VF_BZ, J.Zp - z0);
-    uint32_t* v32 = reinterpret_cast<uint32_t*>(v);  // 4-byte aligned: 68-byte pitch
-#pragma unroll
-    for (int q = 0; q < VF_BZ / 8; ++q) {
-      const uint4 w = (q * 8 < (int)nz) ? s4[q] : make_uint4(0, 0, 0, 0);
-      v32[4 * q + 0] = w.x; v32[4 * q + 1] = w.y; v32[4 * q + 2] = w.z; v32[4 * q + 3] = w.w;
-    }
     // Per labelled voxel: a 3-channel trilinear value noise n(v / P) from the
     // lattice (lerp along z, then y, then x, as the oracle), offset
     // floor(A * n + 0.5) per axis, and the label found there if it is labelled.
-    // The lattice cell of this row changes only every P voxels along z: its
-    // 8 corners x 3 channels stay in registers; t0, t1 are per row.
-    const float t0 = __fdiv_rn((float)(x % P), fp), t1 = __fdiv_rn((float)(y % P), fp);
     const uint32_t sy = J.lat_nz * 3, sx = J.lat_ny * sy;
-    const float* Lrow = J.lattice + (size_t)(x / P) * sx + (size_t)(y / P) * sy;
     const float amp = J.noise_amplitude;
-    float cn[3][8];
-    uint32_t cached = 0xFFFFFFFFu;
-#pragma unroll 1
-    for (int z = 0; z < VF_BZ; ++z) {
-      if (v[z] <= VOXEL_FREE) continue;
-      const uint32_t gz = z0 + z;
-      const uint32_t i2 = i2s[z];
-      if (i2 != cached) {
-        cached = i2;
-        const float* L = Lrow + (size_t)i2 * 3;
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) {
-          cn[ch][0] = L[ch];           cn[ch][1] = L[3 + ch];
-          cn[ch][2] = L[sy + ch];      cn[ch][3] = L[sy + 3 + ch];
-          cn[ch][4] = L[sx + ch];      cn[ch][5] = L[sx + 3 + ch];
-          cn[ch][6] = L[sx + sy + ch]; cn[ch][7] = L[sx + sy + 3 + ch];
-        }
-      }
+    for (uint32_t i = t; i < total; i += blockDim.x) {
+      const uint32_t e = vq[i], row = e >> 5, z = e & 31u;
+      const uint32_t xr = x0 + row / VF_BY, yr = y0 + row % VF_BY, gz = z0 + z;
+      const float t0 = __fdiv_rn((float)(xr % P), fp), t1 = __fdiv_rn((float)(yr % P), fp);
       const float t2 = t2s[z];
+      const float* L = J.lattice + (size_t)(xr / P) * sx + (size_t)(yr / P) * sy + (size_t)i2s[z] * 3;
       int o[3];
 #pragma unroll
       for (int ch = 0; ch < 3; ++ch) {
-        const float c00 = lerp_(cn[ch][0], cn[ch][1], t2), c01 = lerp_(cn[ch][2], cn[ch][3], t2);
-        const float c10 = lerp_(cn[ch][4], cn[ch][5], t2), c11 = lerp_(cn[ch][6], cn[ch][7], t2);
+        const float c00 = lerp_(L[ch], L[3 + ch], t2), c01 = lerp_(L[sy + ch], L[sy + 3 + ch], t2);
+        const float c10 = lerp_(L[sx + ch], L[sx + 3 + ch], t2),
+                    c11 = lerp_(L[sx + sy + ch], L[sx + sy + 3 + ch], t2);
         const float c0 = lerp_(c00, c01, t1), c1 = lerp_(c10, c11, t1);
-        const float nz = lerp_(c0, c1, t0);
-        o[ch] = (int)floorf(__fadd_rn(__fmul_rn(amp, nz), 0.5f));
+        const float nzv = lerp_(c0, c1, t0);
+        o[ch] = (int)floorf(__fadd_rn(__fmul_rn(amp, nzv), 0.5f));
       }
-      const long ux = (long)x + o[0], uy = (long)y + o[1], uz = (long)gz + o[2];
+      const long ux = (long)xr + o[0], uy = (long)yr + o[1], uz = (long)gz + o[2];
       if (ux < 0 || uy < 0 || uz < 0 || ux >= (long)J.X || uy >= (long)J.Y || uz >= (long)J.Z) continue;
       const uint16_t u = src[vf_gidx(J, (uint32_t)ux, (uint32_t)uy, (uint32_t)uz)];
-      if (u > VOXEL_FREE) v[z] = u;
+      if (u > VOXEL_FREE) vrows[row * 34 + z] = u;
     }
-    store_row(J, J.grid2, x, y, z0, v);
+    __syncthreads();
+    if (rowok) store_row(J, J.grid2, x, y, z0, v);
   }
 }
 
