@@ -487,60 +487,72 @@ __global__ void __launch_bounds__(256, 2) k_mc_temit(vfk::MeshGrid G, const unsi
         run += part[e];
       }
       __syncwarp();
-      for (uint32_t i = lane; i < nq; i += 32) {
-        const uint32_t j = S.qcell[w][i];
+      // one triangle per lane: triangle k of the step belongs to the last
+      // queued cell whose first triangle is <= k (cells without triangles
+      // share their successor's prefix), then to the fragment and case-table
+      // row found by counting the cell's triangles in order
+      const uint32_t ntot = __shfl_sync(FULL, incl, 31);
+      for (uint32_t k = lane; k < ntot; k += 32) {
+        uint32_t lo = 0, hi = nq;
+        while (hi - lo > 1) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (S.qtri[w][mid] <= k) lo = mid; else hi = mid;
+        }
+        const uint32_t j = S.qcell[w][lo];
         const int64_t c = (int64_t)c0 + j;
-        uint64_t tt = base + S.qtri[w][i];
+        uint32_t r = k - S.qtri[w][lo];  // triangle within the cell
+        const uint64_t tt = base + k;
         uint32_t v[8], raw0;
         staged_corners(S, w, j, v, raw0);
         const uint32_t wb = raw0 >> 15;  // bit 15 of the voxel at the cell's lattice point
         uint32_t fm = 0;  // corners that hold the first copy of a fragment label
 #pragma unroll
         for (int q = 0; q < 8; ++q) fm |= (uint32_t)first_of(v, q) << q;
+        uint32_t target = 0, conf = 0, nt = 0;
         while (fm) {
           const int i0 = __ffs(fm) - 1;
           fm &= fm - 1;
-          uint32_t target = 0;
+          target = 0;
 #pragma unroll
           for (int q = 0; q < 8; ++q)
             if (q == i0) target = v[q];
-          const uint32_t conf = config_of(v, target);
-          const uint32_t nt = S.T.ntri[conf];
-          const unsigned long long edges = S.T.tri[conf];
-          const uint16_t key = dense[target];
-          for (uint32_t q = 0; q < nt; ++q, ++tt) {
-            uint32_t id[3];
+          conf = config_of(v, target);
+          nt = S.T.ntri[conf];
+          if (r < nt) break;
+          r -= nt;
+        }
+        const unsigned long long edges = S.T.tri[conf];
+        const uint32_t q = r;
+        uint32_t id[3];
 #pragma unroll
-            for (int jj = 0; jj < 3; ++jj) {
-              const int slot = 3 * (int)q + (jj == 0 ? 0 : (jj == 1 ? 2 : 1));
-              const uint32_t e = (uint32_t)(edges >> (4 * slot)) & 15u;
-              // edge endpoints (VF_MC_EDGE); the owner is the end inside the fragment
-              const uint32_t pa = (uint32_t)(0x3210'7654'3210ull >> (4 * e)) & 15u;
-              const uint32_t pb = (uint32_t)(0x7654'4765'0321ull >> (4 * e)) & 15u;
-              const bool a_own = ((conf >> pa) & 1u) == 0u;
-              const uint32_t own = a_own ? pa : pb, oth = a_own ? pb : pa;
-              const uint32_t ob = corner_bits(own), tb = corner_bits(oth);
-              const int64_t ox = a - (int64_t)(ob & 1u), oy = b - 1 + (int64_t)((ob >> 1) & 1u),
-                            oz = c - 1 + (int64_t)((ob >> 2) & 1u);
-              const uint32_t diff = ob ^ tb;  // one bit: the axis
-              const uint32_t axis = diff == 1u ? 0u : (diff == 2u ? 1u : 2u);
-              // x: bit set = dx -1, so the other end lies at larger x when its bit is clear
-              const uint32_t up = axis == 0u ? ((tb & 1u) == 0u) : ((tb >> axis) & 1u);
-              const uint32_t d = 2u * axis + up;
-              const uint64_t lin = ((uint64_t)ox * G.Y + (uint64_t)oy) * G.Zp + (uint64_t)oz;
-              const uint32_t mk = mask[lin];
-              if ((mk >> d) & 1u) {
-                id[jj] = vbase[lin] + (uint32_t)__popc(mk & ((1u << d) - 1u));
-                if (wb) atomicOr(vflag + (id[jj] >> 5), 1u << (id[jj] & 31u));
-              } else {  // the owner's face mask must hold the edge's direction
-                atomicOr(err, 1u);
-                id[jj] = 0;
-              }
-            }
-            tkey[tt] = key;
-            tv[tt] = make_uint4(id[0], id[1], id[2], 0u);
+        for (int jj = 0; jj < 3; ++jj) {
+          const int slot = 3 * (int)q + (jj == 0 ? 0 : (jj == 1 ? 2 : 1));
+          const uint32_t e = (uint32_t)(edges >> (4 * slot)) & 15u;
+          // edge endpoints (VF_MC_EDGE); the owner is the end inside the fragment
+          const uint32_t pa = (uint32_t)(0x3210'7654'3210ull >> (4 * e)) & 15u;
+          const uint32_t pb = (uint32_t)(0x7654'4765'0321ull >> (4 * e)) & 15u;
+          const bool a_own = ((conf >> pa) & 1u) == 0u;
+          const uint32_t own = a_own ? pa : pb, oth = a_own ? pb : pa;
+          const uint32_t ob = corner_bits(own), tb = corner_bits(oth);
+          const int64_t ox = a - (int64_t)(ob & 1u), oy = b - 1 + (int64_t)((ob >> 1) & 1u),
+                        oz = c - 1 + (int64_t)((ob >> 2) & 1u);
+          const uint32_t diff = ob ^ tb;  // one bit: the axis
+          const uint32_t axis = diff == 1u ? 0u : (diff == 2u ? 1u : 2u);
+          // x: bit set = dx -1, so the other end lies at larger x when its bit is clear
+          const uint32_t up = axis == 0u ? ((tb & 1u) == 0u) : ((tb >> axis) & 1u);
+          const uint32_t d = 2u * axis + up;
+          const uint64_t lin = ((uint64_t)ox * G.Y + (uint64_t)oy) * G.Zp + (uint64_t)oz;
+          const uint32_t mk = mask[lin];
+          if ((mk >> d) & 1u) {
+            id[jj] = vbase[lin] + (uint32_t)__popc(mk & ((1u << d) - 1u));
+            if (wb) atomicOr(vflag + (id[jj] >> 5), 1u << (id[jj] & 31u));
+          } else {  // the owner's face mask must hold the edge's direction
+            atomicOr(err, 1u);
+            id[jj] = 0;
           }
         }
+        tkey[tt] = dense[target];
+        tv[tt] = make_uint4(id[0], id[1], id[2], 0u);
       }
       base += __shfl_sync(FULL, incl, 31);
     }
