@@ -172,3 +172,15 @@ def test_batch_and_plain_paths_with_impacts(vf, ctx):
     vf.plain_run(plain, ctx)
     for a, b in zip(plain, specs):
         assert np.array_equal(a.labels, b.labels)
+
+
+def test_ray_batches_walk_the_occupancy_bits(vf, ctx):
+    # 4096 rays or more read a packed occupancy bitmap; the answers stay the oracle's
+    labels, mn, mx = _case(CASES[1])
+    g = vf.RegularGrid(labels.shape, mn, mx, ctx)
+    g.upload(labels)
+    rays = _rays(mn, mx, 6000, 17)
+    got = g.rayEntryVoxels(rays)
+    assert np.array_equal(got, O.ray_entry_batch(labels, mn, mx, rays))
+    assert np.array_equal(got[:100], g.rayEntryVoxels(rays[:100]))  # the direct path agrees
+    g.close()

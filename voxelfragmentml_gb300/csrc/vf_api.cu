@@ -67,9 +67,9 @@ struct MeshState {
 
 // device scratch of the impact path (rays, nearSeeds)
 struct ImpactState {
-  vfr::DevBuf rays, hits, frags, out, status;
+  vfr::DevBuf rays, hits, frags, out, status, bits;
   void release(vfr::Ctx& c) {
-    for (vfr::DevBuf* b : {&rays, &hits, &frags, &out, &status}) c.free_buf(*b);
+    for (vfr::DevBuf* b : {&rays, &hits, &frags, &out, &status, &bits}) c.free_buf(*b);
   }
 };
 
@@ -792,10 +792,19 @@ vf_status vf_ray_entry_voxels(vf_grid* g, const float* rays, uint32_t n, uint32_
   ImpactState& I = g->impact;
   vf_status s;
   if ((s = c.alloc(I.rays, (size_t)n * 24)) || (s = c.alloc(I.hits, (size_t)n * 12))) return s;
+  // batches of rays walk a packed occupancy bitmap (built once per call);
+  // a few rays read the labels directly
+  const vfr::JobPlan& p = g->b.plans[0];
+  const size_t bitbytes = (size_t)p.X * p.Y * ((p.Z + 31) / 32) * 4;
+  uint32_t* bits = nullptr;
+  if (n >= 4096) {
+    if ((s = c.alloc(I.bits, bitbytes))) return s;
+    bits = static_cast<uint32_t*>(I.bits.p);
+  }
   cudaStream_t st = g->b.stream;
   VF_CK(cudaMemcpyAsync(I.rays.p, rays, (size_t)n * 24, cudaMemcpyHostToDevice, st));
   vfk::ray_entry(st, impact_grid(g), static_cast<const float*>(I.rays.p), n,
-                 static_cast<uint32_t*>(I.hits.p), c.num_sms);
+                 static_cast<uint32_t*>(I.hits.p), bits, c.num_sms);
   VF_CK(cudaMemcpyAsync(out, I.hits.p, (size_t)n * 12, cudaMemcpyDeviceToHost, st));
   VF_CK(cudaStreamSynchronize(st));
   VF_CK(cudaGetLastError());

@@ -5,6 +5,8 @@
 // CADScene::hit and CADScene::fractureModel use them (CADScene.cpp:508-520,
 // 629-645).
 //
+//   k_occ_bits    (batches of rays) the grid's occupancy packed 1 bit per
+//                 voxel, so the walks read an L2-resident bitmap
 //   k_ray_entry   one thread per ray: the reference's slab test and
 //                 Amanatides-Woo walk in its operation order (every float
 //                 step rounded as written); the walk is bounded by
@@ -65,7 +67,37 @@ __device__ bool ray_box(const float o[3], const float d[3], const float mn[3], c
   return tMin < FLT_MAX && tMax > 0.0f;
 }
 
-__global__ void __launch_bounds__(256) k_ray_entry(vfk::ImpactGrid G, const float* rays, uint32_t n,
+// occupancy bits (label != EMPTY) of grid row r: word r * Zw + z / 32
+__global__ void __launch_bounds__(256) k_occ_bits(vfk::ImpactGrid G, uint32_t Zw, uint32_t* bits) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t rows = (uint64_t)G.X * G.Y;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows; r += nw) {
+    const uint16_t* row = G.g + r * G.Zp;
+    for (uint32_t z0 = 0; z0 < G.Z; z0 += 32) {
+      const uint32_t z = z0 + lane;
+      const unsigned m = __ballot_sync(0xFFFFFFFFu, z < G.Z && row[z] != EMPTY);
+      if (lane == 0) bits[r * Zw + (z0 >> 5)] = m;
+    }
+  }
+}
+
+// Occupancy of a voxel: from the label grid, or (many rays) from the packed
+// bits, which stay in L2 while the rays walk.
+struct LabelOcc {
+  const vfk::ImpactGrid& G;
+  __device__ bool operator()(uint32_t x, uint32_t y, uint32_t z) const { return gat(G, x, y, z) != EMPTY; }
+};
+struct BitOcc {
+  const uint32_t* bits;
+  uint32_t Y, Zw;
+  __device__ bool operator()(uint32_t x, uint32_t y, uint32_t z) const {
+    return (__ldg(bits + ((uint64_t)x * Y + y) * Zw + (z >> 5)) >> (z & 31u)) & 1u;
+  }
+};
+
+template <typename Occ>
+__global__ void __launch_bounds__(256) k_ray_entry(vfk::ImpactGrid G, Occ occ, const float* rays, uint32_t n,
                                                    uint32_t* out) {
   for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
     const float o[3] = {rays[6 * r + 0], rays[6 * r + 1], rays[6 * r + 2]};
@@ -112,7 +144,7 @@ __global__ void __launch_bounds__(256) k_ray_entry(vfk::ImpactGrid G, const floa
         if (!(cur[0] <= dims[0] && cur[1] <= dims[1] && cur[2] <= dims[2] && cur[0] > 0 && cur[1] > 0 &&
               cur[2] > 0))
           break;
-        if (gat(G, cur[0] - 1, cur[1] - 1, cur[2] - 1) != EMPTY) {
+        if (occ(cur[0] - 1, cur[1] - 1, cur[2] - 1)) {
           res[0] = cur[0];
           res[1] = cur[1];
           res[2] = cur[2];
@@ -167,10 +199,18 @@ __global__ void __launch_bounds__(256) k_near_seeds(vfk::ImpactGrid G, const uin
 namespace vfk {
 
 void ray_entry(cudaStream_t st, const ImpactGrid& G, const float* rays, uint32_t n, uint32_t* out,
-               int num_sms) {
+               uint32_t* bits, int num_sms) {
   if (!n) return;
   const int blocks = (int)std::min<uint32_t>((n + 255) / 256, (uint32_t)num_sms * 8);
-  k_ray_entry<<<blocks, 256, 0, st>>>(G, rays, n, out);
+  if (bits) {
+    const uint32_t Zw = (G.Z + 31) / 32;
+    const uint64_t rows = (uint64_t)G.X * G.Y;
+    const int bb = (int)std::max<uint64_t>(1, std::min<uint64_t>((rows * 32 + 255) / 256, (uint64_t)num_sms * 8));
+    k_occ_bits<<<bb, 256, 0, st>>>(G, Zw, bits);
+    k_ray_entry<<<blocks, 256, 0, st>>>(G, BitOcc{bits, G.Y, Zw}, rays, n, out);
+  } else {
+    k_ray_entry<<<blocks, 256, 0, st>>>(G, LabelOcc{G}, rays, n, out);
+  }
 }
 
 void near_seeds(cudaStream_t st, const ImpactGrid& G, const uint32_t* frags, uint32_t nfrags,

@@ -117,9 +117,10 @@ struct ImpactGrid {
 };
 // per ray (origin xyz, direction xyz): the 1-based index of the first
 // occupied voxel, 0xFFFFFFFF x3 when none; zero directions are rejected by
-// the caller
+// the caller.  bits (X * Y * ceil(Z / 32) words, or NULL): scratch for the
+// packed occupancy the walks read instead of the labels
 void ray_entry(cudaStream_t st, const ImpactGrid& G, const float* rays, uint32_t n, uint32_t* out,
-               int num_sms);
+               uint32_t* bits, int num_sms);
 // Seeder::nearSeeds: the new seeds (4 uint32 each, labels label0 + 1, ...)
 // in (x, y, z) order into out; status[0] = count, status[1] = 0 or
 // VF_ERR_SEED_SEARCH.  Needs nfrags >= 1, num_seeds <= 4095 and
