@@ -853,44 +853,40 @@ __global__ void __launch_bounds__(256, 3) k_shell_flat(const JobDesc* jobs, cons
 __global__ void __launch_bounds__(256) k_combine(const JobDesc* jobs, const uint32_t* brick_job,
                                                  uint32_t total, uint8_t* live, int dual) {
   // One CTA per column of bricks along z (the CTA of the column's first
-  // brick; the others return at once), one thread per (x, y) row: the row's
-  // bit-plane words are contiguous, and the row is written whole.
+  // brick; the others skip it), a warp per (x, y) row with the lanes along z:
+  // the row's bit-plane words load coalesced, and each store instruction
+  // writes 32 consecutive 16-byte label units.
   __shared__ uint32_t colmask[4];  // bricks of the column with an occupied voxel (bit bz)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (uint32_t b = blockIdx.x; b < total; b += gridDim.x) {
     const JobDesc& J = jobs[brick_job[b]];
     const uint32_t lb = b - J.brick_base;
     const uint32_t bz = lb % J.nbz;
     if (bz != 0) continue;  // uniform across the CTA
     const uint32_t by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
-    const uint32_t x = bx * VF_BX + threadIdx.x / VF_BY, y = by * VF_BY + threadIdx.x % VF_BY;
-    const bool inside = x < J.X && y < J.Y;
     if (threadIdx.x < 4) colmask[threadIdx.x] = 0;
     __syncthreads();
-    const uint32_t nw = J.Zw;  // words per row = bricks per column (<= 128)
-    uint32_t m[4] = {0, 0, 0, 0};
-    if (inside) {
+    const uint32_t nw = J.Zw;      // words per row = bricks per column (<= 128)
+    const uint32_t nq = J.Zp / 8;  // 16-byte label units of the row
+    uint32_t m[4] = {0, 0, 0, 0};  // this warp's rows: bricks with an occupied voxel
+    for (uint32_t row = warp; row < VF_BX * VF_BY; row += 8) {
+      const uint32_t x = bx * VF_BX + row / VF_BY, y = by * VF_BY + row % VF_BY;
+      if (x >= J.X || y >= J.Y) continue;  // uniform across the warp
       const size_t w0 = ((size_t)x * J.Y + y) * nw;
       uint4* dst = reinterpret_cast<uint4*>(J.grid + vf_gidx(J, x, y, 0));
-      const uint32_t nq = J.Zp / 8;  // 16-byte label units of the row
-      // the row's words in chunks of 16, all loads of a chunk in flight
-      // before its label stores
-      for (uint32_t w0c = 0; w0c < nw; w0c += 16) {
-        uint32_t words[16];
+      for (uint32_t wb = 0; wb < nw; wb += 32) {
+        const uint32_t w = wb + lane;
+        const uint32_t word = w < nw ? (J.par[w0 + w] | J.shell[w0 + w]) : 0u;
+        m[wb >> 5] |= __ballot_sync(0xFFFFFFFFu, word != 0u);
+        // units q = 4 wb + 32 k + lane take byte (q & 3) of word q >> 2 (lane
+        // (8 k + lane / 4) of this group); bits at z >= Z are never set, so the
+        // row padding is written as 0
 #pragma unroll
-        for (uint32_t i = 0; i < 16; ++i)
-          words[i] = w0c + i < nw ? (J.par[w0 + w0c + i] | J.shell[w0 + w0c + i]) : 0u;
-#pragma unroll
-        for (uint32_t i = 0; i < 16; ++i) {
-          const uint32_t w = w0c + i;
-          if (w >= nw) break;
-          const uint32_t word = words[i];
-          if (word) m[w >> 5] |= 1u << (w & 31);
-          // bits at z >= Z are never set, so the row padding is written as 0
-#pragma unroll
-          for (uint32_t k = 0; k < 4; ++k) {
-            const uint32_t q = 4 * w + k;
-            if (q >= nq) break;
-            const uint32_t bits = word >> (8 * k);
+        for (uint32_t k = 0; k < 4; ++k) {
+          const uint32_t src = __shfl_sync(0xFFFFFFFFu, word, (int)(8 * k + (uint32_t)lane / 4));
+          const uint32_t q = 4 * wb + 32 * k + (uint32_t)lane;
+          if (q < nq) {
+            const uint32_t bits = src >> (8 * (lane & 3));
             uint4 v;
             v.x = (bits & 1u) | ((bits >> 1) & 1u) << 16;
             v.y = ((bits >> 2) & 1u) | ((bits >> 3) & 1u) << 16;
@@ -901,26 +897,24 @@ __global__ void __launch_bounds__(256) k_combine(const JobDesc* jobs, const uint
         }
       }
     }
+    if (lane == 0)
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const uint32_t r = __reduce_or_sync(0xFFFFFFFFu, m[i]);
-      if ((threadIdx.x & 31) == 0 && r) atomicOr(&colmask[i], r);
-    }
+      for (int i = 0; i < 4; ++i)
+        if (m[i]) atomicOr(&colmask[i], m[i]);
     __syncthreads();
     for (uint32_t w = threadIdx.x; w < J.nbz; w += blockDim.x)
       live[b + w] = (colmask[w >> 5] >> (w & 31)) & 1u;
-    if (dual && inside) {
+    if (dual) {
       // the second label buffer needs zeros in the bricks that are not live
       // (stencil tiles read their halo there); live bricks are written in
       // full by the first stage that targets it
-      uint4* dst2 = reinterpret_cast<uint4*>(J.grid2 + vf_gidx(J, x, y, 0));
-      const uint32_t nq = J.Zp / 8;
-      for (uint32_t w = 0; w < nw; ++w) {
-        if ((colmask[w >> 5] >> (w & 31)) & 1u) continue;
-#pragma unroll
-        for (uint32_t k = 0; k < 4; ++k) {
-          const uint32_t q = 4 * w + k;
-          if (q < nq) dst2[q] = make_uint4(0, 0, 0, 0);
+      for (uint32_t row = warp; row < VF_BX * VF_BY; row += 8) {
+        const uint32_t x = bx * VF_BX + row / VF_BY, y = by * VF_BY + row % VF_BY;
+        if (x >= J.X || y >= J.Y) continue;
+        uint4* dst2 = reinterpret_cast<uint4*>(J.grid2 + vf_gidx(J, x, y, 0));
+        for (uint32_t q = lane; q < nq; q += 32) {
+          const uint32_t w = q >> 2;  // the brick (word) of this unit
+          if (!((colmask[w >> 5] >> (w & 31)) & 1u)) dst2[q] = make_uint4(0, 0, 0, 0);
         }
       }
     }
