@@ -742,24 +742,32 @@ __global__ void __launch_bounds__(256) k_counts(const JobDesc* jobs, JobState* s
     hist[threadIdx.x] = 0;
     if (threadIdx.x == 0) occ = 0;
     __syncthreads();
-    const uint32_t x = x0 + threadIdx.x / VF_BY, y = y0 + threadIdx.x % VF_BY;
+    // four lanes per row, each 16 bytes (8 voxels) of the row's 64: a warp
+    // reads 8 rows as contiguous segments; 4 passes cover the brick's 256 rows
     uint32_t mine = 0, err = 0;
-    if (x < J.X && y < J.Y) {
-      const uint4* s4 = reinterpret_cast<const uint4*>(J.grid + vf_gidx(J, x, y, z0));
-      const uint32_t nz = min((uint32_t)VF_BZ, J.Zp - z0);
-      for (uint32_t q = 0; q < nz / 8; ++q) {
-        const uint4 w = s4[q];
-        const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
+    const uint32_t nz = min((uint32_t)VF_BZ, J.Zp - z0);
+    const uint32_t part = threadIdx.x & 3u;
+    uint4 wv[4];
 #pragma unroll
-        for (int h = 0; h < 8; ++h) {
-          const uint32_t g = (ww[h >> 1] >> (16 * (h & 1))) & 0xFFFFu;
-          if (g > VOXEL_FREE) {
-            const uint32_t val = g & 0x7FFFu;
-            ++mine;
-            if (val < 256) atomicAdd(&hist[val], 1u);
-            else if (val < J.ncounts) atomicAdd(&J.counts[val], 1u);
-            else err = 1;
-          }
+    for (int pass = 0; pass < 4; ++pass) {
+      const uint32_t row = (threadIdx.x >> 2) + 64u * pass;
+      const uint32_t x = x0 + row / VF_BY, y = y0 + row % VF_BY;
+      wv[pass] = make_uint4(0, 0, 0, 0);
+      if (x < J.X && y < J.Y && 8u * part < nz)
+        wv[pass] = *reinterpret_cast<const uint4*>(J.grid + vf_gidx(J, x, y, z0 + 8u * part));
+    }
+#pragma unroll
+    for (int pass = 0; pass < 4; ++pass) {
+      const uint32_t ww[4] = {wv[pass].x, wv[pass].y, wv[pass].z, wv[pass].w};
+#pragma unroll
+      for (int h = 0; h < 8; ++h) {
+        const uint32_t g = (ww[h >> 1] >> (16 * (h & 1))) & 0xFFFFu;
+        if (g > VOXEL_FREE) {
+          const uint32_t val = g & 0x7FFFu;
+          ++mine;
+          if (val < 256) atomicAdd(&hist[val], 1u);
+          else if (val < J.ncounts) atomicAdd(&J.counts[val], 1u);
+          else err = 1;
         }
       }
     }
