@@ -708,50 +708,46 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
 
 // ---------------------------------------------------------------------------
 // keys from the label grid: EMPTY -> 0, occupied -> 1 (unreached)
+//
+// Row kernels over live bricks (k_init_keys, k_finalize): one brick per CTA
+// iteration, eight lanes per (x, y) row with the lanes along z.  A lane
+// handles 4 voxels (8 bytes of labels, 16 bytes of keys), so one warp
+// instruction covers 4 rows of the brick with contiguous bytes per row.  A
+// thread takes rows r, r + 32, ... r + 224 and issues all 8 loads before
+// its stores.
+constexpr int ROW_UNITS = VF_BX * VF_BY * (VF_BZ / 4) / 256;
+
 __global__ void __launch_bounds__(256) k_init_keys(const JobDesc* jobs, const uint32_t* list,
                                                    const uint32_t* count, const uint32_t* brick_job) {
-  // IB live bricks per CTA and iteration, one row of each per thread: the
-  // label loads of all of them are in flight before the key stores
-  constexpr int IB = 2;
   const uint32_t n = *count;
-  for (uint32_t i0 = blockIdx.x * IB; i0 < n; i0 += gridDim.x * IB) {
-    uint4 a[IB][VF_BZ / 8];
-    uint4* d[IB];
-    uint32_t nq[IB];
+  const uint32_t q = threadIdx.x & 7, r0 = threadIdx.x >> 3;
+  for (uint32_t it = blockIdx.x; it < n; it += gridDim.x) {
+    const uint32_t b = list[it];
+    const JobDesc& J = jobs[brick_job[b]];
+    if (!J.active) continue;
+    const uint32_t lb = b - J.brick_base;
+    const uint32_t bz = lb % J.nbz, by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
+    const uint32_t z = bz * VF_BZ + 4 * q;
+    // Zk is a multiple of 4 and Zp >= Zk: the lane's 4 keys and 4 labels
+    // are inside the row when z < Zk
+    if (z >= J.Zk) continue;
+    uint2 a[ROW_UNITS];
+    bool ok[ROW_UNITS];
 #pragma unroll
-    for (int k = 0; k < IB; ++k) {
-      d[k] = nullptr;
-      nq[k] = 0;
-#pragma unroll
-      for (int q = 0; q < VF_BZ / 8; ++q) a[k][q] = make_uint4(0, 0, 0, 0);
-      if (i0 + k >= n) continue;
-      const uint32_t b = list[i0 + k];
-      const JobDesc& J = jobs[brick_job[b]];
-      if (!J.active) continue;
-      const uint32_t lb = b - J.brick_base;
-      const uint32_t bz = lb % J.nbz, by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
-      const uint32_t x = bx * VF_BX + threadIdx.x / VF_BY, y = by * VF_BY + threadIdx.x % VF_BY;
-      const uint32_t z0 = bz * VF_BZ;
-      if (x >= J.X || y >= J.Y) continue;
-      // 8 labels per 16-byte load (Zp >= Zk and Zp is a multiple of 8)
-      const uint4* g = reinterpret_cast<const uint4*>(J.grid + vf_gidx(J, x, y, z0));
-      d[k] = reinterpret_cast<uint4*>(J.keys + vf_kidx(J, x, y, z0));
-      nq[k] = min((uint32_t)VF_BZ, J.Zk - z0) / 4;
-#pragma unroll
-      for (uint32_t q = 0; q < VF_BZ / 8; ++q)
-        if (2 * q < nq[k]) a[k][q] = g[q];
+    for (int i = 0; i < ROW_UNITS; ++i) {
+      const uint32_t r = r0 + 32u * i;
+      const uint32_t x = bx * VF_BX + r / VF_BY, y = by * VF_BY + r % VF_BY;
+      ok[i] = x < J.X && y < J.Y;
+      a[i] = ok[i] ? *reinterpret_cast<const uint2*>(J.grid + vf_gidx(J, x, y, z)) : make_uint2(0, 0);
     }
 #pragma unroll
-    for (int k = 0; k < IB; ++k) {
-      if (!d[k]) continue;
-#pragma unroll
-      for (uint32_t q = 0; q < VF_BZ / 4; ++q) {
-        if (q >= nq[k]) break;
-        const uint4 w = a[k][q >> 1];
-        const uint32_t lo = (q & 1) ? w.z : w.x, hi = (q & 1) ? w.w : w.y;
-        __stcg(d[k] + q, make_uint4((lo & 0xFFFFu) ? 1u : 0u, (lo >> 16) ? 1u : 0u,
-                                    (hi & 0xFFFFu) ? 1u : 0u, (hi >> 16) ? 1u : 0u));
-      }
+    for (int i = 0; i < ROW_UNITS; ++i) {
+      if (!ok[i]) continue;
+      const uint32_t r = r0 + 32u * i;
+      const uint32_t x = bx * VF_BX + r / VF_BY, y = by * VF_BY + r % VF_BY;
+      __stcg(reinterpret_cast<uint4*>(J.keys + vf_kidx(J, x, y, z)),
+             make_uint4((a[i].x & 0xFFFFu) ? 1u : 0u, (a[i].x >> 16) ? 1u : 0u,
+                        (a[i].y & 0xFFFFu) ? 1u : 0u, (a[i].y >> 16) ? 1u : 0u));
     }
   }
 }
@@ -835,23 +831,27 @@ __global__ void __launch_bounds__(256) k_finalize(const JobDesc* jobs, const Job
       if (threadIdx.x == 0) cached = (int)j;
       __syncthreads();
     }
+    // rows as in k_init_keys: 8 lanes per row along z, 4 keys per lane
     const uint32_t lb = b - J.brick_base;
     const uint32_t bz = lb % J.nbz, by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
-    const uint32_t x = bx * VF_BX + threadIdx.x / VF_BY, y = by * VF_BY + threadIdx.x % VF_BY;
-    const uint32_t z0 = bz * VF_BZ;
-    if (x >= J.X || y >= J.Y) continue;
-    const uint4* kk = reinterpret_cast<const uint4*>(J.keys + vf_kidx(J, x, y, z0));
-    uint2* g = reinterpret_cast<uint2*>(J.grid + vf_gidx(J, x, y, z0));
-    const uint32_t nq = min((uint32_t)VF_BZ, J.Zk - z0) / 4;
-    // all key loads of the row first (the row's 8 loads in flight together),
-    // then the label lookups and the stores
-    uint4 k4[VF_BZ / 4];
+    const uint32_t z = bz * VF_BZ + 4 * (threadIdx.x & 7), r0 = threadIdx.x >> 3;
+    if (z >= J.Zk) continue;
+    uint4 k4[ROW_UNITS];
+    bool ok[ROW_UNITS];
 #pragma unroll
-    for (uint32_t q = 0; q < VF_BZ / 4; ++q) k4[q] = q < nq ? __ldcg(kk + q) : make_uint4(0, 0, 0, 0);
+    for (int i = 0; i < ROW_UNITS; ++i) {
+      const uint32_t r = r0 + 32u * i;
+      const uint32_t x = bx * VF_BX + r / VF_BY, y = by * VF_BY + r % VF_BY;
+      ok[i] = x < J.X && y < J.Y;
+      k4[i] = ok[i] ? __ldcg(reinterpret_cast<const uint4*>(J.keys + vf_kidx(J, x, y, z)))
+                    : make_uint4(0, 0, 0, 0);
+    }
 #pragma unroll
-    for (uint32_t q = 0; q < VF_BZ / 4; ++q) {
-      if (q >= nq) break;
-      const uint32_t ks[4] = {k4[q].x, k4[q].y, k4[q].z, k4[q].w};
+    for (int i = 0; i < ROW_UNITS; ++i) {
+      if (!ok[i]) continue;
+      const uint32_t r = r0 + 32u * i;
+      const uint32_t x = bx * VF_BX + r / VF_BY, y = by * VF_BY + r % VF_BY;
+      const uint32_t ks[4] = {k4[i].x, k4[i].y, k4[i].z, k4[i].w};
       uint32_t lv[4];
 #pragma unroll
       for (int h = 0; h < 4; ++h) {
@@ -859,7 +859,8 @@ __global__ void __launch_bounds__(256) k_finalize(const JobDesc* jobs, const Job
         // reached: the slot's label; else 0 EMPTY, 1 FREE
         lv[h] = key >= VF_KEY_MIN_REACHED ? (uint32_t)lab[(~key) & 0xFFFu] : key;
       }
-      g[q] = make_uint2(lv[0] | (lv[1] << 16), lv[2] | (lv[3] << 16));
+      *reinterpret_cast<uint2*>(J.grid + vf_gidx(J, x, y, z)) =
+          make_uint2(lv[0] | (lv[1] << 16), lv[2] | (lv[3] << 16));
     }
   }
 }
@@ -1006,7 +1007,7 @@ static inline int brick_grid(uint32_t max_count) {
 void flood_init_keys(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
                      const uint32_t* count, uint32_t max_count, const uint32_t* brick_job,
                      const uint8_t*) {
-  if (max_count) k_init_keys<<<brick_grid((max_count + 1) / 2), 256, 0, st>>>(dj, list, count, brick_job);
+  if (max_count) k_init_keys<<<brick_grid(max_count), 256, 0, st>>>(dj, list, count, brick_job);
 }
 
 void flood_seed_bricks(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs, uint8_t* live,
