@@ -552,26 +552,40 @@ __global__ void __launch_bounds__(256, 3) k_detect1(const JobDesc* jobs, const u
     __syncthreads();
     const bool self_only = J.boundary_size <= 0;  // uniform across the CTA
     if (!self_only) {
-      // phase 1: z-window extrema of every staged row, one u16 pair (z = 2p,
-      // 2p + 1) per thread: the window of the pair is (2p-1, 2p), (2p, 2p+1)
-      // and (2p+1, 2p+2), taken from three aligned u32 words by byte permutes
-      for (int i = threadIdx.x; i < D1_ROWS * D1_W; i += blockDim.x) {
-        const int r = i >> 4, p = i & (D1_W - 1);
-        const uint32_t* rw = reinterpret_cast<const uint32_t*>(tile + r * ZW + 8) + p;
-        const uint32_t w1 = rw[0];
-        const uint32_t wa = __byte_perm(rw[-1], w1, 0x5432), wc = __byte_perm(w1, rw[1], 0x5432);
-        // labelled halves keep u = w & 0x7FFF, the others become 0xFFFF (min) / 0 (max)
-        auto lo = [](uint32_t w) {
-          const uint32_t u = w & 0x7FFF7FFFu;
-          return u | ~__vcmpgtu2(u, 0x00010001u);
-        };
-        auto hi = [](uint32_t w) {
-          const uint32_t u = w & 0x7FFF7FFFu;
-          return u & __vcmpgtu2(u, 0x00010001u);
-        };
-        const int o = r * D1_W + (d1_swz(r, p >> 2) << 2) + (p & 3);
-        zmin[o] = __vminu2(__vminu2(lo(wa), lo(w1)), lo(wc));
-        zmax[o] = __vmaxu2(__vmaxu2(hi(wa), hi(w1)), hi(wc));
+      // phase 1: z-window extrema of every staged row.  A thread takes a
+      // quarter row (4 u32 words = u16 pairs p = 4c .. 4c + 3) and the words
+      // either side of it.  The window of pair p is (2p-1, 2p), (2p, 2p+1)
+      // and (2p+1, 2p+2); labelled halves keep u = w & 0x7FFF, the others
+      // become 0xFFFF (min) / 0 (max).  The masks act on each 16-bit half
+      // alone, so they are taken once per word and the shifted windows are
+      // byte permutes of the masked words.
+      auto lo = [](uint32_t w) {
+        const uint32_t u = w & 0x7FFF7FFFu;
+        return u | ~__vcmpgtu2(u, 0x00010001u);
+      };
+      auto hi = [](uint32_t w) {
+        const uint32_t u = w & 0x7FFF7FFFu;
+        return u & __vcmpgtu2(u, 0x00010001u);
+      };
+      for (int i = threadIdx.x; i < D1_ROWS * 4; i += blockDim.x) {
+        const int r = i >> 2, c = i & 3;
+        const uint32_t* rw = reinterpret_cast<const uint32_t*>(tile + r * ZW + 8) + 4 * c;
+        const uint4 m = *reinterpret_cast<const uint4*>(rw);
+        const uint32_t w[6] = {rw[-1], m.x, m.y, m.z, m.w, rw[4]};
+        uint32_t L[6], H[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) { L[k] = lo(w[k]); H[k] = hi(w[k]); }
+        uint32_t mn[4], mx[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          mn[k] = __vminu2(__vminu2(__byte_perm(L[k], L[k + 1], 0x5432), L[k + 1]),
+                           __byte_perm(L[k + 1], L[k + 2], 0x5432));
+          mx[k] = __vmaxu2(__vmaxu2(__byte_perm(H[k], H[k + 1], 0x5432), H[k + 1]),
+                           __byte_perm(H[k + 1], H[k + 2], 0x5432));
+        }
+        const int o = r * D1_W + (d1_swz(r, c) << 2);
+        *reinterpret_cast<uint4*>(zmin + o) = make_uint4(mn[0], mn[1], mn[2], mn[3]);
+        *reinterpret_cast<uint4*>(zmax + o) = make_uint4(mx[0], mx[1], mx[2], mx[3]);
       }
       __syncthreads();
     }
@@ -616,17 +630,18 @@ __global__ void __launch_bounds__(256, 3) k_detect1(const JobDesc* jobs, const u
           mx.x = __vmaxu2(mx.x, c.x); mx.y = __vmaxu2(mx.y, c.y);
           mx.z = __vmaxu2(mx.z, c.z); mx.w = __vmaxu2(mx.w, c.w);
         }
+        // per 16-bit half: marked when g > FREE, some labelled voxel is in
+        // the window (min != 0xFFFF) and the window is not uniformly g
         const uint32_t mns[4] = {mn.x, mn.y, mn.z, mn.w}, mxs[4] = {mx.x, mx.y, mx.z, mx.w};
+        uint32_t marked = 0;
 #pragma unroll
-        for (int h = 0; h < 8; ++h) {
-          const uint32_t lo = (mns[h >> 1] >> (16 * (h & 1))) & 0xFFFFu;
-          const uint32_t hi = (mxs[h >> 1] >> (16 * (h & 1))) & 0xFFFFu;
-          const uint16_t g = (uint16_t)(gw[h >> 1] >> (16 * (h & 1)));
-          const bool bd = g > VOXEL_FREE && lo != 0xFFFFu && (lo != g || hi != g);
-          const uint32_t o = bd ? (uint32_t)(g | 0x8000u) : (uint32_t)g;
-          if (h & 1) out[h >> 1] |= o << 16; else out[h >> 1] = o;
-          any |= bd;
+        for (int k = 0; k < 4; ++k) {
+          const uint32_t bd = __vcmpgtu2(gw[k], 0x00010001u) & __vcmpne2(mns[k], 0xFFFFFFFFu) &
+                              (__vcmpne2(mns[k], gw[k]) | __vcmpne2(mxs[k], gw[k]));
+          out[k] = gw[k] | (bd & 0x80008000u);
+          marked |= bd;
         }
+        any = marked != 0;
       }
       if (any) dst[q] = make_uint4(out[0], out[1], out[2], out[3]);
     }
