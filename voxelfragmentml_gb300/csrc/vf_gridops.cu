@@ -376,11 +376,10 @@ __device__ __forceinline__ float lerp_(float a, float b, float t) {
 
 __global__ void __launch_bounds__(256) k_perturb(const JobDesc* jobs, const uint32_t* list,
                                                  const uint32_t* count, const uint32_t* brick_job) {
-  // per brick: the lattice index and in-cell coordinate of its 32 z values
-  // (every row of the brick shares them), t = (z mod P) / P rounded as the
-  // oracle divides
-  __shared__ float t2s[VF_BZ];
-  __shared__ uint32_t i2s[VF_BZ];
+  // per brick: the lattice index and in-cell coordinate of its 16 x, 16 y
+  // and 32 z values, t = (c mod P) / P rounded as the oracle divides
+  __shared__ float t0s[VF_BX], t1s[VF_BY], t2s[VF_BZ];
+  __shared__ uint32_t i0s[VF_BX], i1s[VF_BY], i2s[VF_BZ];
   // the thread's row of labels (34-u16 pitch: the u16 of one z from 32
   // threads falls on 32 distinct banks)
   __shared__ __align__(16) uint16_t vrows[256 * 34];
@@ -404,20 +403,43 @@ __global__ void __launch_bounds__(256) k_perturb(const JobDesc* jobs, const uint
       const uint32_t gz = z0 + t;
       t2s[t] = __fdiv_rn((float)(gz % P), fp);
       i2s[t] = gz / P;
+    } else if (t < VF_BZ + VF_BX) {
+      const uint32_t gx = x0 + (t - VF_BZ);
+      t0s[t - VF_BZ] = __fdiv_rn((float)(gx % P), fp);
+      i0s[t - VF_BZ] = gx / P;
+    } else if (t < VF_BZ + VF_BX + VF_BY) {
+      const uint32_t gy = y0 + (t - VF_BZ - VF_BX);
+      t1s[t - VF_BZ - VF_BX] = __fdiv_rn((float)(gy % P), fp);
+      i1s[t - VF_BZ - VF_BX] = gy / P;
     }
     const uint32_t x = x0 + t / VF_BY, y = y0 + t % VF_BY;
     const bool rowok = x < J.X && y < J.Y;
     const uint16_t* src = J.grid;
+    // the brick's label rows into shared memory, 4 lanes per row along z (a
+    // warp instruction reads 8 whole 64-byte rows); chunks at or past Zp are
+    // zero
+    const uint32_t nz = min((uint32_t)VF_BZ, J.Zp - z0);
+    {
+      uint4 w[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const uint32_t u = i * 256 + t, row = u >> 2, q = u & 3;
+        const uint32_t xr = x0 + row / VF_BY, yr = y0 + row % VF_BY;
+        w[i] = (xr < J.X && yr < J.Y && 8 * q < nz)
+                   ? *reinterpret_cast<const uint4*>(src + vf_gidx(J, xr, yr, z0 + 8 * q))
+                   : make_uint4(0, 0, 0, 0);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const uint32_t u = i * 256 + t, row = u >> 2, q = u & 3;
+        // 4-byte aligned: 68-byte row pitch, 16-byte chunks
+        uint32_t* d = reinterpret_cast<uint32_t*>(vrows + row * 34 + 8 * q);
+        d[0] = w[i].x; d[1] = w[i].y; d[2] = w[i].z; d[3] = w[i].w;
+      }
+    }
+    __syncthreads();
     uint32_t m = 0;  // labelled z of this row
     if (rowok) {
-      const uint4* s4 = reinterpret_cast<const uint4*>(src + vf_gidx(J, x, y, z0));
-      const uint32_t nz = min((uint32_t)VF_BZ, J.Zp - z0);
-      uint32_t* v32 = reinterpret_cast<uint32_t*>(v);  // 4-byte aligned: 68-byte pitch
-#pragma unroll
-      for (int q = 0; q < VF_BZ / 8; ++q) {
-        const uint4 w = (q * 8 < (int)nz) ? s4[q] : make_uint4(0, 0, 0, 0);
-        v32[4 * q + 0] = w.x; v32[4 * q + 1] = w.y; v32[4 * q + 2] = w.z; v32[4 * q + 3] = w.w;
-      }
 #pragma unroll
       for (int z = 0; z < VF_BZ; ++z) m |= (uint32_t)(v[z] > VOXEL_FREE) << z;
     }
@@ -449,10 +471,10 @@ __global__ void __launch_bounds__(256) k_perturb(const JobDesc* jobs, const uint
     const float amp = J.noise_amplitude;
     for (uint32_t i = t; i < total; i += blockDim.x) {
       const uint32_t e = vq[i], row = e >> 5, z = e & 31u;
-      const uint32_t xr = x0 + row / VF_BY, yr = y0 + row % VF_BY, gz = z0 + z;
-      const float t0 = __fdiv_rn((float)(xr % P), fp), t1 = __fdiv_rn((float)(yr % P), fp);
-      const float t2 = t2s[z];
-      const float* L = J.lattice + (size_t)(xr / P) * sx + (size_t)(yr / P) * sy + (size_t)i2s[z] * 3;
+      const uint32_t lx = row / VF_BY, ly = row % VF_BY;
+      const uint32_t xr = x0 + lx, yr = y0 + ly, gz = z0 + z;
+      const float t0 = t0s[lx], t1 = t1s[ly], t2 = t2s[z];
+      const float* L = J.lattice + (size_t)i0s[lx] * sx + (size_t)i1s[ly] * sy + (size_t)i2s[z] * 3;
       int o[3];
 #pragma unroll
       for (int ch = 0; ch < 3; ++ch) {
@@ -469,7 +491,17 @@ __global__ void __launch_bounds__(256) k_perturb(const JobDesc* jobs, const uint
       if (u > VOXEL_FREE) vrows[row * 34 + z] = u;
     }
     __syncthreads();
-    if (rowok) store_row(J, J.grid2, x, y, z0, v);
+    // rows back out as they came in, 4 lanes per row
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const uint32_t u = i * 256 + t, row = u >> 2, q = u & 3;
+      const uint32_t xr = x0 + row / VF_BY, yr = y0 + row % VF_BY;
+      if (xr < J.X && yr < J.Y && 8 * q < nz) {
+        const uint32_t* r32 = reinterpret_cast<const uint32_t*>(vrows + row * 34 + 8 * q);
+        *reinterpret_cast<uint4*>(J.grid2 + vf_gidx(J, xr, yr, z0 + 8 * q)) =
+            make_uint4(r32[0], r32[1], r32[2], r32[3]);
+      }
+    }
   }
 }
 
