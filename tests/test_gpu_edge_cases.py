@@ -1,4 +1,4 @@
-"""GPU parity edge cases of the mesh, point-cloud and impact paths: grids
+"""GPU parity edge cases of the mesh, point-cloud, impact and grid-pass paths: grids
 touching every border, odd sizes, degenerate meshes, rays on the box faces
 and signed-zero directions, extreme nearSeeds settings.  Bit-exact against
 the oracle, as the main parity tests."""
@@ -98,4 +98,30 @@ def test_near_seeds_extreme_settings(vf, ctx, spread, nseeds):
     frags = O.seeder_uniform(g0, 3, 5, 1)
     got = vf.Seeder.nearSeeds(g, frags, 2, nseeds, spread, 13)
     assert np.array_equal(got, O.near_seeds(g0, frags, 2, nseeds, spread, 13))
+    g.close()
+
+
+# ---- grid passes on ragged grids: partial bricks in x, y and z ------------
+# (Z = 13, 45, 66: the last z brick holds fewer than 32 voxels, so the row
+# kernels' lanes past Zk / Zp must stay idle; X, Y are not multiples of 16)
+@pytest.mark.parametrize("shape,gseed", [((21, 17, 13), 3), ((37, 29, 45), 4), ((18, 40, 66), 5)])
+def test_grid_passes_on_ragged_grids(vf, ctx, shape, gseed):
+    rng = np.random.default_rng(gseed)
+    occ = (rng.random(shape) < 0.6).astype(np.uint16)
+    seeds = O.seeder_uniform(occ, 9, gseed, 2)
+    g = vf.RegularGrid(shape, None, None, ctx)
+    g.upload(occ)
+    fr = vf.FloodFracturer()
+    fr.setDistanceFunction(2)
+    fr.build(g, seeds)
+    lab, _ = O.flood(occ, seeds, 2)
+    assert np.array_equal(g.data(), lab)
+    for amp, period, seed in ((2.0, 5, 7), (1.3, 16, 8)):
+        g.upload(lab)
+        g.perturb(amp, period, seed)
+        assert np.array_equal(g.data(), O.perturb(lab, amp, period, seed))
+    for bs in (0, 1, 2):
+        g.upload(lab)
+        g.detectBoundaries(bs)
+        assert np.array_equal(g.data(), O.detect_boundaries(lab, bs))
     g.close()
