@@ -121,54 +121,74 @@ def _oracle_params(job, O):
     return p
 
 
-def cpu_sample(jobs, stride=16):
-    return [j for j in jobs if j["index"] % stride == 0]
+def cpu_sample(jobs, stride=16, offset=0):
+    return [j for j in jobs if j["index"] % stride == offset % stride]
 
 
-def run_cpu(jobs, meshes=None):
+def workload_config(jobs):
+    """The `config` object of both arms: the workload and its size."""
+    return {"workload": WORKLOAD, "jobs": len(jobs),
+            "voxels_per_step": int(sum(int(np.prod(j["dims"])) for j in jobs)),
+            "l2": "inputs larger than L2 (label grids 2.8 GB per step)"}
+
+
+def run_cpu(jobs, meshes=None, check=None):
     """Oracle (CPU restatement of the reference algorithm) over `jobs`;
-    returns (voxels, seconds)."""
+    returns (voxels, seconds, parity).  With `check` (job index -> JobSpec
+    holding the GPU's labels and counts of that job) every oracle result is
+    compared with the GPU's, outside the timed region; parity counts the
+    jobs, the label voxels that differ and the jobs whose counts differ."""
     import oracle as O
     from voxelfragmentml_gb300 import vessel as Vs, workloads as W
     O.build()
     vox, secs = 0, 0.0
+    par = {"jobs": 0, "voxels": 0, "label_mismatch_voxels": 0, "count_mismatches": 0}
     for j in jobs:
         v, f = meshes[j["index"]] if meshes else W.mesh_for(j)
         mn, mx = Vs.mesh_aabb(v)
         dims = j["dims"] or Vs.grid_dims(mn, mx, j["max_dim"])
         p = _oracle_params(j, O)
         t = time.perf_counter()
-        O.run_job(v, f, dims, mn, mx, p)
+        lab, cnt, _ = O.run_job(v, f, dims, mn, mx, p, ncounts=256)
         secs += time.perf_counter() - t
         vox += int(np.prod(dims))
-    return vox, secs
+        if check is not None and j["index"] in check:
+            spec = check[j["index"]]
+            par["jobs"] += 1
+            par["voxels"] += int(lab.size)
+            par["label_mismatch_voxels"] += int(np.count_nonzero(spec.labels != lab))
+            par["count_mismatches"] += int(not np.array_equal(spec.counts, cnt[:spec.counts.shape[0]]))
+    return vox, secs, par
 
 
 def reference_arm(args):
+    """The reference's algorithm on the host cores: the CPU oracle over all
+    jobs of the workload every timed step (the same jobs, metric and config
+    as the GPU arm); warm-up steps take every 16th job."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     from voxelfragmentml_gb300 import workloads as W
-    jobs = W.mixed(256)
+    jobs = W.mixed(args.jobs)
     sample = cpu_sample(jobs, args.ref_stride)
     meshes = {j["index"]: W.mesh_for(j) for j in sample}
-    for _ in range(args.warmup):
-        run_cpu(sample[:1], meshes)
+    for w in range(args.warmup):
+        run_cpu(cpu_sample(sample, 16, w), meshes)
     tot_v, tot_s = 0, 0.0
     for _ in range(args.steps):
-        v, s = run_cpu(sample, meshes)
+        v, s, _ = run_cpu(sample, meshes)
         tot_v += v
         tot_s += s
     value = tot_v / tot_s
     cores = os.cpu_count()
-    desc = (f"CPU oracle (restatement of the reference's flood/seed/voxelize/erode code; "
-            f"the reference is Windows+OpenGL only) on every {args.ref_stride}th job of "
-            f"mixed-256 ({len(sample)} jobs, {tot_v // args.steps} voxels) per step")
+    desc = (f"CPU oracle (restatement of the reference's voxelize/seed/flood/perturb/boundary/"
+            f"count code; the reference itself is Windows+OpenGL only), OpenMP on {cores} threads, "
+            f"{len(sample)} of {len(jobs)} mixed-256 jobs ({tot_v // args.steps} voxels) per step")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "voxels/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 * tot_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u16", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample": desc},
+            "config": workload_config(jobs),
             "cpu_baseline": {"value": value, "unit": "voxels/s", "cores": cores, "kind": "port",
                              "sample": desc},
             "e2e": {"value": value, "unit": "voxels/s", "h2d_bytes_per_step": 0,
@@ -194,9 +214,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--jobs", type=int, default=256)
     ap.add_argument("--plain-jobs", type=int, default=32)
-    ap.add_argument("--serve-rates", default="100,400,1000,2000",
+    ap.add_argument("--serve-rates", default="50,500,2000,4000,6000,8000",
                     help="Poisson arrival rates (jobs/s) of the serving sweep")
-    ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrivals per rate")
+    ap.add_argument("--serve-seconds", type=float, default=60.0,
+                    help="seconds of arrivals per rate")
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0,
+                    help="HBM budget of the server (GiB) that admission control keeps to")
     ap.add_argument("--configs", action="store_true",
                     help="single-instance configurations 1-3 (128^3, 256^3, 512^3 vessels): "
                          "one JSON line each with batched, plain and CPU times and a parity check")
@@ -211,8 +234,8 @@ def main():
     ap.add_argument("--rays", type=int, default=1 << 20, help="--impact: rays per step")
     ap.add_argument("--cpu-stride", type=int, default=2,
                     help="cpu_baseline sample: every n-th job of the workload (2: about 10-15 s)")
-    ap.add_argument("--ref-stride", type=int, default=4,
-                    help="--impl reference: every n-th job per step")
+    ap.add_argument("--ref-stride", type=int, default=1,
+                    help="--impl reference: every n-th job per step (1: the whole workload)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default settings)")
@@ -312,12 +335,19 @@ def main():
     R.barrier()
     t0 = time.perf_counter()
     res = []
+    submit_s, collect_s = 0.0, 0.0
     for k in range(args.steps):
         if len(pipe._inflight) == 2:
+            tc = time.perf_counter()
             res += pipe.collect()
+            collect_s += time.perf_counter() - tc
+        ts = time.perf_counter()
         pipe.submit(sets[k % 2])
+        submit_s += time.perf_counter() - ts
     while pipe._inflight:
+        tc = time.perf_counter()
         res += pipe.collect()
+        collect_s += time.perf_counter() - tc
     wall_pipe = time.perf_counter() - t0
     pipe.close()
     e2e_ms = R.max_over_ranks(1000.0 * wall_pipe)
@@ -344,6 +374,32 @@ def main():
     clk = clocks.stop()
     assert all(r.status == 0 for r in res)
 
+    # host link and placement of the pinned buffers (explains e2e - value)
+    h2d_gbs, d2h_gbs = ctx.copy_bandwidth(256 << 20)
+    L = V.lib()
+    buf_nodes = sorted({L.vf_host_numa_node(s.labels.ctypes.data) for s in specs[::16]})
+    host_link = {"h2d_gbs": h2d_gbs, "d2h_gbs": d2h_gbs,
+                 "probe": "best of 3 copies of 256 MB, pinned host <-> device, CUDA events",
+                 "gpu_host_numa_node": ctx.host_numa(), "label_buffer_numa_nodes": buf_nodes,
+                 "host_cpus": os.cpu_count()}
+
+    # ---- CPU baseline (oracle) on a bounded sample, and parity ----------
+    # The GPU's labels and counts of the sample's jobs (in `specs` from the
+    # last vf_batch_run above) are compared with the oracle's, job by job.
+    cpu, parity = None, None
+    if not args.no_cpu and rank == 0:
+        sample = cpu_sample(jobs, args.cpu_stride)
+        cv, cs, parity = run_cpu(sample, check={s.tag: s for s in specs})
+        cpu = {"value": cv / cs, "unit": "voxels/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"CPU oracle on every {args.cpu_stride}th job of mixed-256 "
+                         f"({len(sample)} jobs, {cv} voxels, {cs:.1f} s)"}
+        parity["compared"] = ("labels and per-fragment counts of the headline batch "
+                              "(vf_batch_run) against the oracle on the cpu_baseline jobs")
+        if parity["label_mismatch_voxels"] or parity["count_mismatches"]:
+            print(json.dumps({"parity": parity}), file=sys.stderr, flush=True)
+            raise SystemExit("GPU labels or counts differ from the oracle on the headline batch")
+    del specs2, sets
+
     # ---- plain per-job path (reference-shaped) on a subset ---------------
     plain = None
     if args.plain_jobs > 0:
@@ -366,19 +422,13 @@ def main():
     serving = None
     if not args.no_serve and args.serve_seconds > 0:
         rates = [float(r) for r in args.serve_rates.split(",") if r]
-        sweep = serve_sweep(V, ctx, jobs, rates, args.serve_seconds)
-        serving = {"sweep": sweep,
-                   "note": "Poisson arrivals of mixed-256 jobs (pool of 64 distinct jobs cycled) "
-                           "through vf_server_*: latency = submit to labels in host memory"}
-
-    # ---- CPU baseline (oracle) on a bounded sample -----------------------
-    cpu = None
-    if not args.no_cpu and rank == 0:
-        sample = cpu_sample(jobs, args.cpu_stride)
-        cv, cs = run_cpu(sample)
-        cpu = {"value": cv / cs, "unit": "voxels/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"CPU oracle on every {args.cpu_stride}th job of mixed-256 "
-                         f"({len(sample)} jobs, {cv} voxels, {cs:.1f} s)"}
+        budget = int(args.serve_budget_gb * (1 << 30))
+        sweep = serve_sweep(V, ctx, jobs, rates, args.serve_seconds, budget)
+        serving = {"sweep": sweep, "hbm_budget_bytes": budget,
+                   "note": f"Poisson arrivals drawn from the {len(jobs)} mixed-256 jobs through "
+                           "vf_server_* (continuous batching): latency = submit to labels in host "
+                           "memory; sustained = voxels of completed jobs / (last completion - "
+                           "first arrival)"}
 
     peak, peak_kind = _peaks()
     flood_launch_ms = flood_ms / args.steps
@@ -407,21 +457,23 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "jobs": len(specs), "voxels_per_step": voxels,
-                       "l2": "inputs larger than L2 (label grids 2.8 GB per step)",
-                       "parallelism": "replicas" if world > 1 else "single GPU",
-                       "path": "batched (one persistent brick-queue kernel per stage)",
-                       "cuda_graph": bool(getattr(rb, "graph", False)),
-                       "tuning": tuning},
+            "config": workload_config(jobs),
+            "setup": {"parallelism": "replicas" if world > 1 else "single GPU",
+                      "path": "batched (one persistent brick-queue kernel per stage)",
+                      "cuda_graph": bool(getattr(rb, "graph", False)),
+                      "tuning": tuning},
             "e2e": {"value": e2e_value, "unit": "voxels/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms / args.steps,
                     "path": "vf_pipeline_submit / vf_pipeline_collect, 2 batches in flight",
                     "timing": "host wall clock over the K steps, device idle at the start",
                     "stages_ms_last_step": {k: round(v, 3) for k, v in e2e_stages.items()},
+                    "host_ms_per_step": {"submit": 1000.0 * submit_s / args.steps,
+                                         "collect_wait": 1000.0 * collect_s / args.steps},
+                    "host_link": host_link,
                     "one_batch_at_a_time": {"path": "vf_batch_run", "value": sync_value,
                                             "ms_per_step": sync_ms / args.steps,
                                             "wall_ms_per_step": 1000.0 * wall_sync / args.steps}},
-            "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+            "roofline": roof, "cpu_baseline": cpu, "parity": parity, "clocks": clk,
             "gpu_launches": launches, "plain": plain, "serving": serving,
             "stages_ms_per_step": {k: v / args.steps for k, v in stage_tot.items()}}
     if rank == 0:
@@ -431,48 +483,61 @@ def main():
     return 0
 
 
-def serve_sweep(V, ctx, jobs, rates, seconds, pool=64, copies=4):
-    """Poisson arrivals of mixed-256 jobs at each rate (jobs/s) for `seconds`."""
+def serve_sweep(V, ctx, jobs, rates, seconds, budget, copies=2):
+    """Poisson arrivals at each rate (jobs/s) for `seconds`; each arrival is
+    a job drawn uniformly from `jobs`.  Every job has `copies` pinned label
+    buffers used in turn, so a job that is in flight twice writes to two
+    buffers."""
     from voxelfragmentml_gb300 import workloads as W
-    base = [W.to_spec(j, V, want_labels=False, ncounts=256, pinned=True) for j in jobs[:pool]]
+    base = [W.to_spec(j, V, want_labels=False, ncounts=256, pinned=True) for j in jobs]
     outs = {}
     for k in range(copies):
         for i, s in enumerate(base):
             outs[(i, k)] = V.pinned_array(s.dims, np.uint16)
     sweep = []
     for rate in rates:
-        srv = V.Server(ctx, max_inflight=3, max_batch=32)
+        srv = V.Server(ctx, hbm_budget=budget, max_inflight=3, max_batch=32)
         rng = np.random.default_rng(7)
-        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * seconds * 2) + 16))
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * seconds * 1.5) + 64))
         arrivals = arrivals[arrivals < seconds]
+        pick = rng.integers(0, len(base), size=len(arrivals))
+        uses = np.zeros(len(base), np.int64)
         results = []
+        vox_of = {}
         t0 = time.perf_counter()
-        vox = 0
         for n, at in enumerate(arrivals):
             now = time.perf_counter() - t0
             if at > now:
                 time.sleep(at - now)
-            i = n % pool
+            i = int(pick[n])
             s = base[i]
-            s.labels = outs[(i, (n // pool) % copies)]
+            s.labels = outs[(i, int(uses[i]) % copies)]
+            uses[i] += 1
             s.tag = n
+            vox_of[n] = int(np.prod(s.dims))
             srv.submit(s)
-            vox += int(np.prod(s.dims))
             results += srv.poll(256, 0)
         offered = time.perf_counter() - t0
-        deadline = time.perf_counter() + 120
+        deadline = time.perf_counter() + 300
         while len(results) < len(arrivals) and time.perf_counter() < deadline:
             results += srv.poll(256, 50)
-        span = time.perf_counter() - t0
         srv.close()
-        lat = sorted(r.done_ms - r.submit_ms for r in results)
-        ok = sum(1 for r in results if r.status == 0)
+        lat = np.array(sorted(r.done_ms - r.submit_ms for r in results))
+        ok = [r for r in results if r.status == 0]
+        done_vox = sum(vox_of[int(r.user_tag)] for r in ok)
+        span_ms = max(r.done_ms for r in results) - min(r.submit_ms for r in results) \
+            if results else 0.0
+        offered_vox = sum(vox_of.values()) / max(offered, 1e-9)
         sweep.append({"rate_jobs_per_s": rate, "seconds": seconds, "submitted": int(len(arrivals)),
                       "achieved_arrival_rate": len(arrivals) / max(offered, 1e-9),
-                      "completed_ok": ok,
-                      "p50_ms": float(np.percentile(lat, 50)) if lat else None,
-                      "p99_ms": float(np.percentile(lat, 99)) if lat else None,
-                      "sustained_voxels_per_s": vox / span})
+                      "completed_ok": len(ok),
+                      "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
+                      "p90_ms": float(np.percentile(lat, 90)) if len(lat) else None,
+                      "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+                      "offered_voxels_per_s": offered_vox,
+                      "sustained_voxels_per_s": done_vox / max(span_ms / 1000.0, 1e-9),
+                      "sustained_over_offered": (done_vox / max(span_ms / 1000.0, 1e-9)) /
+                      max(offered_vox, 1e-9)})
     return sweep
 
 
@@ -559,7 +624,7 @@ def single_configs(args):
 
 
 # ncu DRAM bytes (read + write) of one non-boundary k_lap_gather launch on the
-# 512^3 mesh workload (profiles/mesh_kernels_512.md)
+# 512^3 mesh workload (one GB300, --clock-control none)
 K_LAP_GATHER_NB_DRAM_BYTES_512 = 125.624576e6 + 17.66e6
 
 MESH_JOBS = {

@@ -114,9 +114,22 @@ vf_status vf_ctx_destroy(vf_ctx* ctx);
 vf_status vf_ctx_synchronize(vf_ctx* ctx);
 /* bytes currently held by grids and scratch */
 size_t vf_ctx_bytes_in_use(const vf_ctx* ctx);
-/* pinned host memory for fast uploads/downloads (cudaMallocHost) */
+/* pinned host memory for fast uploads/downloads.  Buffers of 1 MiB or more
+ * are placed on the host NUMA node closest to the current device (preferred
+ * policy, then cudaHostRegister, mapped); smaller ones, or hosts without a
+ * NUMA node for the device, come from cudaMallocHost.  Free with
+ * vf_host_free. */
 void* vf_host_alloc(size_t bytes);
 void vf_host_free(void* p);
+/* NUMA node of the host page holding p (-1 unknown); no reference
+ * counterpart, for placement checks */
+int vf_host_numa_node(const void* p);
+/* host NUMA node closest to the context's device (cudaDevAttrHostNumaId;
+ * -1 when the system reports none) */
+vf_status vf_ctx_host_numa(vf_ctx* ctx, int* node);
+/* host link probe: best of 3 copies of `bytes` between a vf_host_alloc
+ * buffer and device memory on the context's stream, GB/s each way */
+vf_status vf_ctx_copy_bandwidth(vf_ctx* ctx, size_t bytes, float* h2d_gbs, float* d2h_gbs);
 
 /* ---- grid (RegularGrid) --------------------------------------------------
  * RegularGrid(aabb, subdivisions) + setAABB (RegularGrid.cpp:21-27, 426-441):
@@ -387,9 +400,16 @@ vf_status vf_pipeline_destroy(vf_pipeline* p);
  * file-scope device array of 32 MiB inside the library, held by every GPU
  * that loads it until exit; grids needing more (about 5 million voxels)
  * return VF_ERR_RANGE.  Calls share that array: calls that overlap on the
- * GPU race.  The first call on a device looks up the array's address; make
- * it before any stream capture.  Runs on `stream` (a cudaStream_t, NULL =
- * default stream) and returns when the labels are written. */
+ * GPU race.  The flood inside is a cooperative launch with a grid-wide
+ * barrier, so a call must not overlap a context's batched flood
+ * (vf_batch_run, vf_pipeline_*, vf_server_*) on another stream either (the
+ * barrier's bounded wait could run out: VF_ERR_TIMEOUT).  The first call on
+ * a device looks up the array's address; make it before any stream capture.
+ * Runs on `stream` (a cudaStream_t, NULL = default stream) and returns when
+ * the labels are written.  nseeds = 0 labels every occupied voxel FREE (1).
+ * On an error (VF_ERR_INVALID for a seed outside the grid or a label that is
+ * not 2..255 in its low byte or carries a sub-seed prefix) the contents of
+ * d_labels are unspecified. */
 vf_status vf_flood_noalloc(const uint16_t* d_grid, uint16_t* d_labels, uint32_t X, uint32_t Y,
                            uint32_t Z, const uint32_t* d_seeds_xyzw, uint32_t nseeds,
                            int distance, void* stream);
@@ -439,6 +459,12 @@ vf_status vf_ctx_last_graph(vf_ctx* ctx, int* replayed);
  * (BFS waves a brick advances per pass before it re-queues itself),
  * [3] flood CTAs per SM (0: as many as fit).  Results never depend on them. */
 vf_status vf_ctx_set_tuning(vf_ctx* ctx, const int32_t* values, uint32_t n);
+/* Spin limit of the flood relaxation's pass barrier on this context (polls
+ * of about 64 ns each; 0 restores the default 2^26, about 4 s).  When the
+ * limit runs out the kernel sets its error word and returns, and the call
+ * fails with VF_ERR_TIMEOUT; the context stays usable.  A small limit makes
+ * the bounded device wait run out on purpose (tests of the error path). */
+vf_status vf_ctx_set_flood_wait_limit(vf_ctx* ctx, uint32_t spins);
 vf_status vf_ctx_get_tuning(vf_ctx* ctx, int32_t* values, uint32_t n);
 /* Autotuner: prepares `jobs` as a resident batch (as vf_batch_prepare, which
  * it replaces) and runs it under candidate settings, one knob at a time,

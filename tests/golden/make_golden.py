@@ -85,7 +85,9 @@ def case_inputs(name):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: make_golden.py <root of the reference checkout>")
+    ref_root = sys.argv[1]
     index = {}
     for name in CASES:
         v, f, mn, mx, dims, p, kw = case_inputs(name)

@@ -65,4 +65,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: make_mc_table_fixture.py <root of the reference checkout>")
+    main(sys.argv[1])

@@ -20,19 +20,20 @@ from voxelfragmentml_gb300 import vessel as Vs
 pytestmark = pytest.mark.gpu
 
 
-def _device_call(vf, occ, seeds, dfunc):
+def _device_call(vf, occ, seeds, dfunc, expect=0):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
-    g = torch.from_numpy(occ.astype(np.int16)).cuda()
+    g = torch.from_numpy(occ.astype(np.uint16).view(np.int16)).cuda()
     out = torch.full(occ.shape, -1, dtype=torch.int16, device="cuda")
-    s = torch.from_numpy(seeds.astype(np.int32)).cuda()
+    s = torch.from_numpy(seeds.astype(np.uint32).view(np.int32).reshape(-1, 4)).cuda() \
+        if len(seeds) else None
     torch.cuda.synchronize()
     X, Y, Z = occ.shape
     st = vf.lib().vf_flood_noalloc(C.c_void_p(g.data_ptr()), C.c_void_p(out.data_ptr()),
-                                   X, Y, Z, C.c_void_p(s.data_ptr()), seeds.shape[0], dfunc,
-                                   None)
-    assert st == 0, vf.lib().vf_last_error()
+                                   X, Y, Z, C.c_void_p(s.data_ptr()) if s is not None else None,
+                                   len(seeds), dfunc, None)
+    assert st == expect, vf.lib().vf_last_error()
     torch.cuda.synchronize()
     return out.cpu().numpy().view(np.uint16)
 
@@ -56,6 +57,36 @@ def test_flood_noalloc_matches_regular_entry_point_twice(vf, ctx, oracle_lib):
         got = _device_call(vf, occ, seeds, dfunc)
         exp = _regular(vf, ctx, occ, seeds, dfunc)
         assert np.array_equal(got, exp)
+        assert np.array_equal(got, O.flood(occ, seeds, dfunc)[0])
+
+
+def test_flood_noalloc_edge_cases(vf, ctx, oracle_lib):
+    rng = np.random.default_rng(11)
+    # no seeds: occupied voxels come out FREE (1), empty ones EMPTY (0)
+    occ = (rng.random((20, 17, 9)) < 0.6).astype(np.uint16)
+    got = _device_call(vf, occ, np.zeros((0, 4), np.uint32), 1)
+    assert np.array_equal(got, O.flood(occ, np.zeros((0, 4), np.uint32), 1)[0])
+    assert np.array_equal(got, (occ != 0).astype(np.uint16))
+    # grids one voxel wide along each axis
+    for shape in ((1, 23, 40), (31, 1, 18), (12, 26, 1)):
+        occ = (rng.random(shape) < 0.7).astype(np.uint16)
+        seeds = O.seeder_uniform(occ, 3, 5, 2)
+        for dfunc in (1, 2):
+            got = _device_call(vf, occ, seeds, dfunc)
+            assert np.array_equal(got, O.flood(occ, seeds, dfunc)[0]), shape
+
+
+def test_flood_noalloc_rejects_bad_seeds(vf, ctx):
+    occ = np.ones((16, 16, 16), np.uint16)
+    # a seed outside the grid, and a label with a sub-seed prefix (> 255)
+    outside = np.array([[3, 3, 3, 2], [3, 16, 3, 3]], np.uint32)
+    _device_call(vf, occ, outside, 1, expect=vf.ERR_INVALID)
+    prefixed = np.array([[3, 3, 3, 2], [9, 9, 9, 2 | (1 << 8)]], np.uint32)
+    _device_call(vf, occ, prefixed, 2, expect=vf.ERR_INVALID)
+    # the next valid call is unaffected by the failed ones
+    seeds = np.array([[1, 2, 3, 2], [12, 12, 12, 3]], np.uint32)
+    got = _device_call(vf, occ, seeds, 1)
+    assert np.array_equal(got, O.flood(occ, seeds, 1)[0])
 
 
 def test_flood_noalloc_rejects_oversize(vf, ctx):

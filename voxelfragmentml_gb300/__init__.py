@@ -102,6 +102,9 @@ EXPORTS = {
     "vf_ctx_bytes_in_use": (C.c_size_t, [C.c_void_p]),
     "vf_host_alloc": (C.c_void_p, [C.c_size_t]),
     "vf_host_free": (None, [C.c_void_p]),
+    "vf_host_numa_node": (C.c_int, [C.c_void_p]),
+    "vf_ctx_host_numa": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "vf_ctx_copy_bandwidth": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]),
     "vf_grid_create": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
                                  C.c_void_p, C.c_void_p, C.c_void_p]),
     "vf_grid_destroy": (C.c_int, [C.c_void_p]),
@@ -151,6 +154,7 @@ EXPORTS = {
     "vf_grid_mesh_counters": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_ctx_set_tuning": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "vf_ctx_get_tuning": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "vf_ctx_set_flood_wait_limit": (C.c_int, [C.c_void_p, C.c_uint32]),
     "vf_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
     "vf_server_create": (C.c_int, [C.c_void_p, C.c_size_t, C.c_uint32, C.c_uint32, C.c_void_p]),
     "vf_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -259,6 +263,18 @@ class Context:
         _check(lib().vf_ctx_flood_pass_sizes(self.h, a, 256))
         return [v for v in a if v]
 
+    def host_numa(self) -> int:
+        """Host NUMA node closest to the device (-1: none reported)."""
+        n = C.c_int(-1)
+        _check(lib().vf_ctx_host_numa(self.h, C.byref(n)))
+        return n.value
+
+    def copy_bandwidth(self, nbytes: int = 256 << 20):
+        """(H2D, D2H) GB/s between pinned host memory and the device."""
+        a, b = C.c_float(), C.c_float()
+        _check(lib().vf_ctx_copy_bandwidth(self.h, nbytes, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def last_stats(self):
         la, vis, by = C.c_uint64(), C.c_uint64(), C.c_uint64()
         ms = C.c_float()
@@ -272,6 +288,7 @@ class Context:
                 "flood_maxit_hits": mh.value, "flood_active_row_sweeps": cn[6],
                 "flood_busy_warp_sweeps": cn[2],
                 "flood_key_changes": cn[7],
+                "flood_barrier_timeouts": cn[3],
                 # first out-of-range access the relaxation skipped (0: none)
                 "flood_anomaly": (cn[8], cn[9], cn[10]),
                 "flood_empty_visits": cn[16],

@@ -11,8 +11,13 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <mutex>
 #include <thread>
+
+#include <sys/mman.h>
+#include <sys/syscall.h>
+#include <unistd.h>
 
 #include "vf_runtime.h"
 
@@ -22,6 +27,23 @@ void dims_for_aabb(const float mn[3], const float mx[3], uint32_t maxv, uint32_t
 }  // namespace vfr
 
 using vfr::fail;
+
+namespace {
+std::mutex g_host_mu;
+std::map<void*, size_t> g_host_mapped;  // vf_host_alloc buffers placed by mbind
+constexpr int kMpolPreferred = 1;       // MPOL_PREFERRED (linux/mempolicy.h)
+
+// host NUMA node closest to the current device, or -1
+int device_host_numa() {
+  int dev = 0, node = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&node, cudaDevAttrHostNumaId, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  return node;
+}
+}  // namespace
 
 #define VF_CK(call)                                                                  \
   do {                                                                               \
@@ -200,13 +222,109 @@ vf_status vf_ctx_synchronize(vf_ctx* ctx) {
 
 size_t vf_ctx_bytes_in_use(const vf_ctx* ctx) { return ctx ? ctx->c.in_use : 0; }
 
+// Pinned host memory.  Buffers of 1 MiB and more are placed on the host NUMA
+// node closest to the current device (cudaDevAttrHostNumaId): anonymous
+// pages with a preferred-node policy (mbind), then page-locked and mapped
+// with cudaHostRegister.  On a host with several CPU sockets the copy
+// engines and the direct-write pack kernels then move labels over the
+// GPU's own host link instead of crossing the socket interconnect.  Smaller
+// buffers, and hosts that report no NUMA node, use cudaMallocHost.
 void* vf_host_alloc(size_t bytes) {
+  const int node = device_host_numa();
+  if (node >= 0 && node < 64 && bytes >= ((size_t)1 << 20)) {
+    const size_t pg = (size_t)sysconf(_SC_PAGESIZE);
+    const size_t len = (bytes + pg - 1) / pg * pg;
+    void* p = mmap(nullptr, len, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+    if (p != MAP_FAILED) {
+      const unsigned long mask = 1ul << node;
+      if (syscall(SYS_mbind, p, len, kMpolPreferred, &mask, 8 * sizeof(mask) + 1, 0) == 0 &&
+          cudaHostRegister(p, len, cudaHostRegisterPortable | cudaHostRegisterMapped) ==
+              cudaSuccess) {
+        std::lock_guard<std::mutex> lk(g_host_mu);
+        g_host_mapped[p] = len;
+        return p;
+      }
+      cudaGetLastError();  // a failed registration leaves no sticky error
+      munmap(p, len);
+    }
+  }
   void* p = nullptr;
   if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
   return p;
 }
 void vf_host_free(void* p) {
-  if (p) cudaFreeHost(p);
+  if (!p) return;
+  size_t len = 0;
+  {
+    std::lock_guard<std::mutex> lk(g_host_mu);
+    auto it = g_host_mapped.find(p);
+    if (it != g_host_mapped.end()) {
+      len = it->second;
+      g_host_mapped.erase(it);
+    }
+  }
+  if (len) {
+    cudaHostUnregister(p);
+    munmap(p, len);
+  } else {
+    cudaFreeHost(p);
+  }
+}
+
+int vf_host_numa_node(const void* p) {
+  if (!p) return -1;
+  const uintptr_t pg = (uintptr_t)sysconf(_SC_PAGESIZE);
+  void* pages[1] = {reinterpret_cast<void*>(reinterpret_cast<uintptr_t>(p) & ~(pg - 1))};
+  int status[1] = {-1};
+  if (syscall(SYS_move_pages, 0, 1ul, pages, nullptr, status, 0) != 0) return -1;
+  return status[0] >= 0 ? status[0] : -1;
+}
+
+vf_status vf_ctx_host_numa(vf_ctx* ctx, int* node) {
+  if (!ctx || !node) return fail(VF_ERR_INVALID, "NULL argument");
+  *node = -1;
+  int v = -1;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrHostNumaId, ctx->c.device) == cudaSuccess) *node = v;
+  cudaGetLastError();
+  return VF_OK;
+}
+
+vf_status vf_ctx_copy_bandwidth(vf_ctx* ctx, size_t bytes, float* h2d_gbs, float* d2h_gbs) {
+  if (!ctx || !h2d_gbs || !d2h_gbs || bytes == 0) return fail(VF_ERR_INVALID, "bad argument");
+  VF_CK(cudaSetDevice(ctx->c.device));
+  void* h = vf_host_alloc(bytes);
+  if (!h) return fail(VF_ERR_OOM, "pinned host allocation failed");
+  std::memset(h, 1, bytes);
+  void* d = nullptr;
+  if (cudaMalloc(&d, bytes) != cudaSuccess) {
+    vf_host_free(h);
+    return fail(VF_ERR_OOM, "device allocation for the copy probe failed");
+  }
+  cudaStream_t st = ctx->c.stream;
+  cudaEvent_t e[3];
+  for (auto& x : e) cudaEventCreate(&x);
+  float best_h2d = 0.f, best_d2h = 0.f;
+  cudaError_t err = cudaSuccess;
+  for (int rep = 0; rep < 3 && err == cudaSuccess; ++rep) {
+    cudaEventRecord(e[0], st);
+    cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, st);
+    cudaEventRecord(e[1], st);
+    cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, st);
+    cudaEventRecord(e[2], st);
+    err = cudaEventSynchronize(e[2]);
+    float a = 0.f, b = 0.f;
+    cudaEventElapsedTime(&a, e[0], e[1]);
+    cudaEventElapsedTime(&b, e[1], e[2]);
+    if (a > 0.f) best_h2d = std::max(best_h2d, (float)(bytes / (a * 1e6)));
+    if (b > 0.f) best_d2h = std::max(best_d2h, (float)(bytes / (b * 1e6)));
+  }
+  for (auto& x : e) cudaEventDestroy(x);
+  cudaFree(d);
+  vf_host_free(h);
+  if (err != cudaSuccess) return fail(VF_ERR_CUDA, std::string("copy probe: ") + cudaGetErrorString(err));
+  *h2d_gbs = best_h2d;
+  *d2h_gbs = best_d2h;
+  return VF_OK;
 }
 
 vf_status vf_dims_for_aabb(const float aabb_min[3], const float aabb_max[3], uint32_t max_voxels,
@@ -1148,6 +1266,13 @@ static vf_status set_tuning(vfr::Ctx& c, const int32_t* v, uint32_t n) {
 vf_status vf_ctx_set_tuning(vf_ctx* ctx, const int32_t* values, uint32_t n) {
   if (!ctx || (n && !values)) return fail(VF_ERR_INVALID, "NULL argument");
   return set_tuning(ctx->c, values, n);
+}
+
+vf_status vf_ctx_set_flood_wait_limit(vf_ctx* ctx, uint32_t spins) {
+  if (!ctx) return fail(VF_ERR_INVALID, "ctx is NULL");
+  ctx->c.tune.flood_wait_spins = spins;
+  ctx->c.batch.drop_graphs();  // captured chains hold the old limit
+  return VF_OK;
 }
 
 vf_status vf_ctx_get_tuning(vf_ctx* ctx, int32_t* values, uint32_t n) {

@@ -64,6 +64,7 @@ struct FloodArgs {
   uint32_t* fdir;        // [nbricks][FLOOD_FDIR] change record (read and cleared by each visit)
   uint32_t nbricks;      // bricks of the batch (queue entries and brick ids are below)
   uint32_t njobs;        // jobs of the batch
+  uint32_t wait_spins;   // spins of the pass barrier before it gives up
 };
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
@@ -84,8 +85,10 @@ __device__ __noinline__ void flood_anomaly(const FloodArgs& a, uint32_t code, ui
   }
 }
 
-// software grid barrier with a bounded spin (~4 s); false on timeout
-__device__ bool grid_sync(uint32_t* bar, uint32_t nblocks, uint32_t* err, uint32_t* stats) {
+// software grid barrier with a bounded spin (wait_spins polls, 2^26 or about
+// 4 s by default); false on timeout
+__device__ bool grid_sync(uint32_t* bar, uint32_t nblocks, uint32_t* err, uint32_t* stats,
+                          uint32_t wait_spins) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -100,7 +103,7 @@ __device__ bool grid_sync(uint32_t* bar, uint32_t nblocks, uint32_t* err, uint32
     } else {
       uint32_t spins = 0;
       while (ld_acquire(bar + 1) == gen) {
-        if (++spins > (1u << 26) || ld_acquire(err) != 0) {
+        if (++spins > wait_spins || ld_acquire(err) != 0) {
           atomicOr(err, 2u);
           atomicAdd(stats + 3, 1u);
           ok = 0;
@@ -681,7 +684,7 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
       ++visits;
     }
     if (threadIdx.x == 0 && visits) atomicAdd(&a.stats[0], visits);
-    const bool synced = grid_sync(a.bar, gridDim.x, a.err, a.stats);
+    const bool synced = grid_sync(a.bar, gridDim.x, a.err, a.stats, a.wait_spins);
     if (threadIdx.x == 0) {
       // phase cycles: [0] claim, [1] staging, [2] sweeps, [3] write-back +
       // enqueue, [4] from the failed claim through the pass barrier; added to
@@ -1028,14 +1031,16 @@ void flood_seed(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs,
 }
 
 static int relax_blocks(int num_sms) {
-  static int per_sm = -1;
-  if (per_sm < 0) {
+  static int per_sm[64] = {};  // per device: the attribute is set on each device
+  const int dv = cur_dev();
+  if (per_sm[dv] < 1) {
+    int n = 0;
     cudaFuncSetAttribute(k_relax, cudaFuncAttributeMaxDynamicSharedMemorySize, TILE_BYTES);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_relax, 256, TILE_BYTES) != cudaSuccess)
-      per_sm = 1;
-    if (per_sm < 1) per_sm = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_relax, 256, TILE_BYTES) != cudaSuccess)
+      n = 1;
+    per_sm[dv] = n < 1 ? 1 : n;
   }
-  return per_sm * num_sms;
+  return per_sm[dv] * num_sms;
 }
 
 void flood_prepare(int num_sms) { (void)relax_blocks(num_sms); }
@@ -1063,6 +1068,7 @@ cudaError_t flood_relax(cudaStream_t st, const JobDesc* dj, JobState* ds,
   a.fdir = fs.fdir;
   a.nbricks = fs.total_bricks;
   a.njobs = fs.njobs;
+  a.wait_spins = fs.wait_spins ? fs.wait_spins : (1u << 26);
   int blocks = relax_blocks(num_sms);
   if (fs.ctas_per_sm > 0 && fs.ctas_per_sm * num_sms < blocks) blocks = fs.ctas_per_sm * num_sms;
   if (blocks_used) *blocks_used = blocks;

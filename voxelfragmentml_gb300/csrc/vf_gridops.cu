@@ -930,10 +930,11 @@ static inline int brick_grid(uint32_t max_count) {
 }
 
 void sample_seeds(cudaStream_t st, const JobDesc* dj, JobState* ds, int njobs) {
-  static bool attr = false;
-  if (!attr) {
+  static bool attr[64] = {};  // per device
+  const int dv = cur_dev();
+  if (!attr[dv]) {
     cudaFuncSetAttribute(k_seeds, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SeedSmem));
-    attr = true;
+    attr[dv] = true;
   }
   if (njobs > 0) k_seeds<<<njobs, 1024, sizeof(SeedSmem), st>>>(dj, ds);
 }
@@ -954,10 +955,11 @@ void perturb(cudaStream_t st, const JobDesc* dj, const uint32_t* list, const uin
 template <int H>
 static void detect_h(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
                      const uint32_t* count, uint32_t max_count, const uint32_t* brick_job) {
-  static bool attr = false;
-  if (!attr) {
+  static bool attr[64] = {};  // per device
+  const int dv = cur_dev();
+  if (!attr[dv]) {
     cudaFuncSetAttribute(k_detect<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, Tile<H>::BYTES);
-    attr = true;
+    attr[dv] = true;
   }
   k_detect<H><<<brick_grid(max_count), 256, Tile<H>::BYTES, st>>>(dj, list, count, brick_job);
 }
@@ -965,10 +967,11 @@ void detect_boundaries(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
                        const uint32_t* count, uint32_t max_count, const uint32_t* brick_job) {
   // boundary sizes 0..1 (the default): window extrema; 2..3: detect_boundaries_wide
   if (!max_count) return;
-  static bool attr = false;
-  if (!attr) {
+  static bool attr[64] = {};  // per device
+  const int dv = cur_dev();
+  if (!attr[dv]) {
     cudaFuncSetAttribute(k_detect1, cudaFuncAttributeMaxDynamicSharedMemorySize, D1_BYTES);
-    attr = true;
+    attr[dv] = true;
   }
   k_detect1<<<brick_grid(max_count), 256, D1_BYTES, st>>>(dj, list, count, brick_job);
 }
@@ -981,11 +984,12 @@ void detect_boundaries_wide(cudaStream_t st, const JobDesc* dj, const uint32_t* 
 template <int H>
 static void erode_h(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
                     const uint32_t* count, uint32_t max_count, const uint32_t* brick_job) {
-  static bool attr = false;
+  static bool attr[64] = {};  // per device
+  const int dv = cur_dev();
   const int bytes = Tile<H>::BYTES + 343 * 4;
-  if (!attr) {
+  if (!attr[dv]) {
     cudaFuncSetAttribute(k_erode<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    attr = true;
+    attr[dv] = true;
   }
   k_erode<H><<<brick_grid(max_count), 256, bytes, st>>>(dj, list, count, brick_job);
 }
@@ -996,10 +1000,11 @@ void erode(cudaStream_t st, const JobDesc* dj, const uint32_t* list, const uint3
 }
 void remove_isolated(cudaStream_t st, const JobDesc* dj, const uint32_t* list,
                      const uint32_t* count, uint32_t max_count, const uint32_t* brick_job) {
-  static bool attr = false;
-  if (!attr) {
+  static bool attr[64] = {};  // per device
+  const int dv = cur_dev();
+  if (!attr[dv]) {
     cudaFuncSetAttribute(k_isolated, cudaFuncAttributeMaxDynamicSharedMemorySize, Tile<1>::BYTES);
-    attr = true;
+    attr[dv] = true;
   }
   if (max_count)
     k_isolated<<<brick_grid(max_count), 256, Tile<1>::BYTES, st>>>(dj, list, count, brick_job);

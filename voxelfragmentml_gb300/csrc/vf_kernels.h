@@ -188,6 +188,14 @@ void count_values(cudaStream_t st, const JobDesc* dj, JobState* ds, const uint32
 // [9..16] rows whose key at z0+32 changed (bit t & 31 of word t >> 5, row
 // t = x * 16 + y within the brick).
 constexpr uint32_t FLOOD_FDIR = 17;
+// the current device, as an index into per-device caches of launch
+// attributes (a kernel's shared-memory limit is set once per device)
+inline int cur_dev() {
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess) d = 0;
+  return d & 63;
+}
+
 struct FloodScratch {
   uint32_t* queue[3];    // brick ids, capacity total_bricks each (rotating)
   uint32_t* qcount;      // [3]
@@ -202,6 +210,7 @@ struct FloodScratch {
   uint32_t njobs = 1;    // job descriptors in the table
   int max_sweeps = 0;    // tuning: sweeps per brick visit (0: default cap)
   int ctas_per_sm = 0;   // tuning: resident CTAs per SM (0: as many as fit)
+  uint32_t wait_spins = 0;  // spins of the pass barrier before it gives up (0: 2^26, ~4 s)
   uint32_t* pass_sizes = nullptr;  // statistics: bricks queued per pass (256)
 };
 void flood_init_keys(cudaStream_t st, const JobDesc* dj, const uint32_t* list,

@@ -15,7 +15,12 @@
 //   - every call on a device shares it and it keeps the contents of the last
 //     call; each call clears what must start at zero before using it;
 //   - calls whose work overlaps on the GPU (two host threads, or two streams
-//     without ordering between them) race on it and give wrong results.
+//     without ordering between them) race on it and give wrong results;
+//   - its flood relaxation is a cooperative launch with a grid-wide barrier
+//     that expects the whole GPU: a call must not overlap a vf_ctx's batched
+//     flood (vf_batch_run, vf_pipeline_*, a vf_server) on another stream
+//     either, or the barrier wait may run out (VF_ERR_TIMEOUT).
+// When the call returns an error the contents of d_labels are unspecified.
 //
 // Host code cannot use the name g_scratch as a device address (on the host
 // it is only a stand-in symbol).  The first call on each device, with that
@@ -42,6 +47,7 @@ __global__ void k_noalloc_init(JobDesc d, JobDesc* dst, JobState* st, uint32_t* 
 
 std::mutex g_mu;
 void* g_addr[64] = {};  // resolved scratch address per device
+int g_sms[64] = {};     // multiprocessor count per device
 
 size_t up(size_t v) { return (v + 255) & ~(size_t)255; }
 
@@ -73,7 +79,13 @@ extern "C" vf_status vf_flood_noalloc(const uint16_t* d_grid, uint16_t* d_labels
       }
     }
     base = g_addr[dev];
+    if (!g_sms[dev] &&
+        cudaDeviceGetAttribute(&g_sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+      g_sms[dev] = 0;
+      return fail(VF_ERR_CUDA, "vf_flood_noalloc: device query failed");
+    }
   }
+  const int num_sms = g_sms[dev];
   // layout of the scratch array
   const uint32_t Zp = vf_roundup(Z, 8), Zk = vf_roundup(Z, 4);
   const uint32_t nbx = (X + VF_BX - 1) / VF_BX, nby = (Y + VF_BY - 1) / VF_BY,
@@ -124,9 +136,6 @@ extern "C" vf_status vf_flood_noalloc(const uint16_t* d_grid, uint16_t* d_labels
   d.active = 1;
 
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  cudaDeviceProp prop;
-  if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess)
-    return fail(VF_ERR_CUDA, "vf_flood_noalloc: device query failed");
 #define NA_CK(call)                                                                         \
   do {                                                                                      \
     cudaError_t e_ = (call);                                                                \
@@ -141,7 +150,9 @@ extern "C" vf_status vf_flood_noalloc(const uint16_t* d_grid, uint16_t* d_labels
   NA_CK(cudaMemsetAsync(bj, 0, nb * 4, st));  // every brick belongs to job 0
   vfk::mark_live(st, ddesc, bj, (uint32_t)nb, live);
   vfk::compact_live(st, live, (uint32_t)nb, list, lcount);
-  vfk::sample_seeds(st, ddesc, dstate, 1);  // seeds given: count + prefix flag
+  // Without seeds nothing is claimed: occupied voxels come out FREE (1), as
+  // FloodFracturer::build leaves them after homogenize (keys 1 -> label 1).
+  if (nseeds) vfk::sample_seeds(st, ddesc, dstate, 1);  // seeds given: count + prefix flag
   vfk::FloodScratch fs;
   fs.queue[0] = reinterpret_cast<uint32_t*>(S + o_q0);
   fs.queue[1] = reinterpret_cast<uint32_t*>(S + o_q1);
@@ -156,11 +167,13 @@ extern "C" vf_status vf_flood_noalloc(const uint16_t* d_grid, uint16_t* d_labels
   fs.max_passes = 1u << 20;
   fs.total_bricks = (uint32_t)nb;
   fs.njobs = 1;
-  vfk::flood_seed_bricks(st, ddesc, dstate, 1, live, list, lcount);
+  if (nseeds) vfk::flood_seed_bricks(st, ddesc, dstate, 1, live, list, lcount);
   vfk::flood_init_keys(st, ddesc, list, lcount, (uint32_t)nb, bj, live);
-  vfk::flood_seed(st, ddesc, dstate, 1, fs, live);
-  int blocks = 0;
-  NA_CK(vfk::flood_relax(st, ddesc, dstate, bj, live, fs, prop.multiProcessorCount, &blocks));
+  if (nseeds) {
+    vfk::flood_seed(st, ddesc, dstate, 1, fs, live);
+    int blocks = 0;
+    NA_CK(vfk::flood_relax(st, ddesc, dstate, bj, live, fs, num_sms, &blocks));
+  }
   vfk::flood_finalize(st, ddesc, dstate, list, lcount, (uint32_t)nb, bj, 0);
   NA_CK(cudaMemcpy2DAsync(d_labels, (size_t)Z * 2, grid, (size_t)Zp * 2, (size_t)Z * 2,
                           (size_t)X * Y, cudaMemcpyDeviceToDevice, st));

@@ -626,6 +626,7 @@ static vfk::FloodScratch flood_scratch(Batch& B) {
   fs.njobs = (uint32_t)B.jobs.size();
   fs.max_sweeps = B.ctx->tune.flood_sweeps;
   fs.ctas_per_sm = B.ctx->tune.flood_ctas;
+  fs.wait_spins = B.ctx->tune.flood_wait_spins;
   fs.pass_sizes = sc + 128;  // [256]
   return fs;
 }

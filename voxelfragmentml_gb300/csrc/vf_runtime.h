@@ -129,6 +129,7 @@ struct Tuning {
   int32_t shell_grid = 12;    // k_shell_flat CTAs per SM
   int32_t flood_sweeps = 96;  // relaxation sweeps per brick visit (waves per pass)
   int32_t flood_ctas = 0;     // k_relax resident CTAs per SM (0: as many as fit)
+  uint32_t flood_wait_spins = 0;  // grid-barrier spin limit of k_relax (0: the default)
 };
 
 struct Ctx {
