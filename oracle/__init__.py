@@ -33,6 +33,51 @@ def build(force: bool = False) -> str:
     return _LIB_PATH
 
 
+_REF_LIB = os.path.join(_HERE, "_ref", "libvfref.so")
+_ref = None
+
+
+def build_ref(ref_root: str | None = None) -> str | None:
+    """Compile the reference pin (`make ref`: the reference's own tri-box,
+    NaiveFracturer::buildCPU and Seeder::mergeSeeds, unchanged, against the
+    stand-ins in oracle/ref_shim/) when the reference checkout is present;
+    None when it is not."""
+    src = ref_root or os.environ.get("VF_REFERENCE_SOURCE", "")
+    if not src:
+        for cand in (os.path.join(_HERE, "..", "..", "reference", "MeshFragments", "Source"),):
+            if os.path.isdir(cand):
+                src = cand
+    if not src or not os.path.isdir(src):
+        return _REF_LIB if os.path.exists(_REF_LIB) else None
+    r = subprocess.run(["make", "-s", "-C", _HERE, "ref", f"REF={os.path.abspath(src)}"],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference pin build failed:\n" + r.stderr[-4000:])
+    return _REF_LIB
+
+
+def ref_lib():
+    """The compiled reference pin (vfr_tri_box, vfr_tri_box_batch, vfr_naive,
+    vfr_merge_seeds), or None when it cannot be built here."""
+    global _ref
+    if _ref is None:
+        path = build_ref()
+        if not path or not os.path.exists(path):
+            return None
+        L = C.CDLL(path)
+        P, u32, i32 = C.c_void_p, C.c_uint32, C.c_int
+        L.vfr_tri_box.restype = i32
+        L.vfr_tri_box.argtypes = [P, P, P, P, P]
+        L.vfr_tri_box_batch.restype = None
+        L.vfr_tri_box_batch.argtypes = [P, P, u32, P]
+        L.vfr_naive.restype = i32
+        L.vfr_naive.argtypes = [P, u32, u32, u32, P, u32, i32]
+        L.vfr_merge_seeds.restype = i32
+        L.vfr_merge_seeds.argtypes = [P, u32, P, u32, i32]
+        _ref = L
+    return _ref
+
+
 class Params(C.Structure):
     _fields_ = [("algorithm", C.c_int32), ("distance", C.c_int32),
                 ("num_seeds", C.c_int32), ("num_extra_seeds", C.c_int32),

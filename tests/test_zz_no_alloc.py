@@ -67,10 +67,13 @@ def test_flood_noalloc_edge_cases(vf, ctx, oracle_lib):
     got = _device_call(vf, occ, np.zeros((0, 4), np.uint32), 1)
     assert np.array_equal(got, O.flood(occ, np.zeros((0, 4), np.uint32), 1)[0])
     assert np.array_equal(got, (occ != 0).astype(np.uint16))
-    # grids one voxel wide along each axis
+    # grids one voxel wide along each axis (seeds picked directly: the
+    # seeder needs two layers per axis)
     for shape in ((1, 23, 40), (31, 1, 18), (12, 26, 1)):
         occ = (rng.random(shape) < 0.7).astype(np.uint16)
-        seeds = O.seeder_uniform(occ, 3, 5, 2)
+        occv = np.argwhere(occ != 0)
+        pick = occv[rng.choice(len(occv), 3, replace=False)]
+        seeds = np.concatenate([pick, np.arange(2, 5)[:, None]], axis=1).astype(np.uint32)
         for dfunc in (1, 2):
             got = _device_call(vf, occ, seeds, dfunc)
             assert np.array_equal(got, O.flood(occ, seeds, dfunc)[0]), shape
