@@ -443,7 +443,8 @@ vf_status vf_ctx_flood_stats(vf_ctx* ctx, uint64_t* passes, uint64_t* sweeps,
  * a brick, [12] staging its keys, [13] sweeps, [14] write-back and enqueue of
  * neighbours, [15] from the last claim of a pass through the pass barrier,
  * [16] visits that found no change around the brick and staged nothing
- * (included in [0]).  n <= 17 are filled, the rest zeroed. */
+ * (included in [0]), [17] visits that staged their brick but changed no key.
+ * n <= 20 are filled, the rest zeroed. */
 vf_status vf_ctx_flood_counters(vf_ctx* ctx, uint64_t* out, uint32_t n);
 /* bricks queued for each pass of the last batched flood (first 256 passes;
  * zero beyond the pass count). */

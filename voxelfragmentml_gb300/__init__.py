@@ -281,8 +281,8 @@ class Context:
         _check(lib().vf_ctx_last_stats(self.h, C.byref(la), C.byref(ms), C.byref(by), C.byref(vis)))
         pa, sw, mh = C.c_uint64(), C.c_uint64(), C.c_uint64()
         _check(lib().vf_ctx_flood_stats(self.h, C.byref(pa), C.byref(sw), C.byref(mh)))
-        cn = (C.c_uint64 * 17)()
-        _check(lib().vf_ctx_flood_counters(self.h, cn, 17))
+        cn = (C.c_uint64 * 20)()
+        _check(lib().vf_ctx_flood_counters(self.h, cn, 20))
         return {"launches": la.value, "flood_ms": ms.value, "flood_bytes": by.value,
                 "flood_visits": vis.value, "flood_passes": pa.value, "flood_sweeps": sw.value,
                 "flood_maxit_hits": mh.value, "flood_active_row_sweeps": cn[6],
@@ -292,6 +292,7 @@ class Context:
                 # first out-of-range access the relaxation skipped (0: none)
                 "flood_anomaly": (cn[8], cn[9], cn[10]),
                 "flood_empty_visits": cn[16],
+                "flood_visits_no_change": cn[17],
                 # SM cycles summed over the relaxation CTAs, per phase of their work
                 "flood_phase_cycles": {k: 256 * cn[11 + i] for i, k in enumerate(
                     ("claim", "staging", "sweeps", "writeback_enqueue", "pass_barrier"))}}

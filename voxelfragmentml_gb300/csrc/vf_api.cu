@@ -1351,8 +1351,8 @@ vf_status vf_ctx_last_graph(vf_ctx* ctx, int* replayed) {
 
 vf_status vf_ctx_flood_counters(vf_ctx* ctx, uint64_t* out, uint32_t n) {
   if (!ctx || (n && !out)) return fail(VF_ERR_INVALID, "NULL argument");
-  for (uint32_t i = 0; i < n && i < 17; ++i) out[i] = ctx->c.last_flood_counters[i];
-  for (uint32_t i = 17; i < n; ++i) out[i] = 0;
+  for (uint32_t i = 0; i < n && i < VF_FLOOD_NCOUNTERS; ++i) out[i] = ctx->c.last_flood_counters[i];
+  for (uint32_t i = VF_FLOOD_NCOUNTERS; i < n; ++i) out[i] = 0;
   return VF_OK;
 }
 

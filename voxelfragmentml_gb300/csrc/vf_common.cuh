@@ -43,6 +43,7 @@
 #define VF_JERR_INVALID 16u
 
 #define VF_MAX_TRIES 1000000u   // Seeder.h:48
+#define VF_FLOOD_NCOUNTERS 20    // raw flood relaxation counters (vf_ctx_flood_counters)
 #define VF_NOISE_BUFFER 1000000u // RegularGrid.cpp:124
 
 struct JobDesc {

@@ -30,6 +30,11 @@
 // connected component of one fragment the lowest prefix wins; per fragment
 // only voxels with the fragment's minimum prefix survive; the rest is
 // re-flooded from all survivors (ties to the lowest label value).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
 #include "vf_kernels.h"
 
 namespace {
@@ -40,6 +45,7 @@ constexpr int KP = 36;                 // smem row pitch (u32): conflict-free 16
 constexpr int KNX = VF_BX + 2, KNY = VF_BY + 2;
 constexpr int KROWS = KNX * KNY;
 constexpr int TILE_BYTES = KROWS * KP * 4;
+constexpr int TILE_SMEM = TILE_BYTES + 128;  // dynamic shared memory: the tile, aligned to 128
 constexpr int MAXIT = 96;              // default cap of relaxation sweeps per brick visit
 
 struct FloodArgs {
@@ -57,7 +63,8 @@ struct FloodArgs {
                      // [5] visits at the sweep cap, [6] active row-sweeps, [7] key changes,
                      // [8..10] first out-of-range access (code, two values),
                      // [11..15] SM cycles / 256 per phase of the CTAs' work,
-                     // [16] visits that found nothing new and staged nothing
+                     // [16] visits that found nothing new and staged nothing,
+                     // [17] visits that staged their brick but changed no key
   uint32_t max_passes;
   int max_sweeps;    // sweeps per brick visit before the brick re-queues itself
   uint32_t* pass_sizes;  // bricks queued for each of the first 256 passes (or null)
@@ -65,7 +72,48 @@ struct FloodArgs {
   uint32_t nbricks;      // bricks of the batch (queue entries and brick ids are below)
   uint32_t njobs;        // jobs of the batch
   uint32_t wait_spins;   // spins of the pass barrier before it gives up
+  const unsigned char* tmaps;  // [njobs] keys tensor maps (KEYS_MAP_BYTES each)
 };
+
+// ---- TMA tile loads (cp.async.bulk.tensor) with mbarrier completion -------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok) : "r"(mbar), "r"(phase) : "memory");
+  return ok != 0;
+}
+// bounded wait for the phase `phase` of the mbarrier to complete
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
+  for (uint32_t i = 0; i < (1u << 22); ++i)
+    if (mbar_try_wait(mbar, phase)) return true;
+  return false;
+}
+// the same box into L2 only (a hint: no completion, no shared memory)
+__device__ __forceinline__ void tma_prefetch_3d(const void* map, int c0, int c1, int c2) {
+  asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];"
+               ::"l"(map), "r"(c0), "r"(c1), "r"(c2) : "memory");
+}
+// box of the 3-D tensor `map` at (c0 innermost, c1, c2) into shared memory,
+// completion counted in bytes on the mbarrier
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const void* map, int c0, int c1, int c2,
+                                            uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(dst), "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(mbar) : "memory");
+}
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
   uint32_t v;
@@ -153,6 +201,15 @@ __device__ __forceinline__ uint32_t step_from(uint32_t m) {
 __device__ __forceinline__ uint32_t relax(uint32_t kk, uint32_t m) {
   return kk ? max(kk, step_from(m)) : 0u;
 }
+// One step of an in-row chain: relax(kk, max(w, prev)) with the part that
+// does not depend on prev, a = relax(kk, w), computed ahead of the chain.
+// step_from is monotone, so relax(kk, max(w, prev)) = kk ? max(a, step_from(
+// prev)) : 0, and a = 0 when kk = 0: on the chain there is one select (the
+// step, taken only for occupied voxels) and one max.
+__device__ __forceinline__ uint32_t chain_step(uint32_t a, bool occ, uint32_t prev) {
+  const uint32_t s = (occ && prev >= 2u * VF_KEY_STEP) ? prev - VF_KEY_STEP : 0u;
+  return max(a, s);
+}
 // a key at the largest distance the key format holds (its neighbours would
 // overflow the distance field)
 __device__ __forceinline__ bool at_limit(uint32_t m) {
@@ -168,12 +225,26 @@ __device__ __forceinline__ uint4 lds4(const uint32_t* p) {
 // Shared state of the sweeps of one brick visit.
 struct SweepShared {
   uint32_t rfw[16];      // [2][8] rows that changed in the previous sweep (bit per row)
-  uint32_t wcnt[8];      // active rows per warp in this sweep
+  uint32_t wmask[8];     // active rows of each warp in this sweep (bit per lane)
   uint32_t hl[256];      // per row: z halo candidate below the brick (z0-1)
   uint32_t hh[256];      //          z halo candidate above the brick (z0+32)
   uint32_t rowchg[256];  // per row: z positions changed during the visit
-  uint16_t rlist[256];   // rows to run in this sweep
 };
+
+// position of the k-th (from 0) set bit of m; k < popc(m)
+__device__ __forceinline__ int nth_set_bit(uint32_t m, uint32_t k) {
+  int pos = 0;
+#pragma unroll
+  for (int w = 16; w >= 1; w >>= 1) {
+    const uint32_t lo = (uint32_t)__popc(m & ((1u << w) - 1u));
+    if (k >= lo) {
+      k -= lo;
+      m >>= w;
+      pos += w;
+    }
+  }
+  return pos;
+}
 
 // Relaxes one row of the staged tile (own_row) in place: the forward pass
 // (cross-row candidates fused with the increasing-z pass) and the backward
@@ -205,10 +276,12 @@ __device__ __forceinline__ uint32_t relax_row(uint32_t* own_row, uint32_t hlo, u
       const uint32_t w[4] = {max(cp, max(C.x, C.y)), max(C.x, max(C.y, C.z)),
                              max(C.y, max(C.z, C.w)), max(C.z, max(C.w, Cn.x))};
       const uint32_t kk[4] = {kv.x, kv.y, kv.z, kv.w};
-      uint32_t f[4];
+      uint32_t f[4], av[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) av[j] = relax(kk[j], w[j]);  // off the chain
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
-        f[j] = relax(kk[j], max(w[j], prev));
+        f[j] = chain_step(av[j], kk[j] != 0u, prev);
         prev = f[j];
         if (f[j] != kk[j]) chg |= 1u << (4 * q + j);
       }
@@ -224,10 +297,12 @@ __device__ __forceinline__ uint32_t relax_row(uint32_t* own_row, uint32_t hlo, u
       const uint4 kv = lds4(own_row + 4 + 4 * q);
       const uint32_t w[4] = {M.x, M.y, M.z, M.w};
       const uint32_t kk[4] = {kv.x, kv.y, kv.z, kv.w};
-      uint32_t f[4];
+      uint32_t f[4], av[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) av[j] = relax(kk[j], w[j]);  // off the chain
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
-        f[j] = relax(kk[j], max(w[j], prev));
+        f[j] = chain_step(av[j], kk[j] != 0u, prev);
         prev = f[j];
         if (f[j] != kk[j]) chg |= 1u << (4 * q + j);
       }
@@ -253,7 +328,7 @@ __device__ __forceinline__ uint32_t relax_row(uint32_t* own_row, uint32_t hlo, u
     uint32_t cq = 0;
 #pragma unroll
     for (int j = 3; j >= 0; --j) {
-      f[j] = relax(kk[j], prev);
+      f[j] = chain_step(kk[j], kk[j] != 0u, prev);
       prev = f[j];
       if (f[j] != kk[j]) cq |= 1u << j;
     }
@@ -267,11 +342,14 @@ __device__ __forceinline__ uint32_t relax_row(uint32_t* own_row, uint32_t hlo, u
   return chg;
 }
 
+// One visit of brick b.  False when its tile load did not complete in
+// time (the error word is set; the kernel stops).
 template <int CONN>
-__device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, uint32_t b,
+__device__ bool relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, uint32_t b,
                             uint32_t pass, uint32_t* tile, uint32_t* live27, uint32_t* dirs,
                             int* reenq, SweepShared& sw, uint32_t* fbits,
-                            unsigned long long* ph, uint32_t i, uint32_t qn, uint32_t* pre) {
+                            unsigned long long* ph, uint32_t i, uint32_t qn, uint32_t* pre,
+                            uint32_t mbar, uint32_t& phase) {
   // ph (thread 0): SM cycles of [1] live map + staging, [2] sweeps, [3] write-back + enqueue
   long long c0 = 0;
   if (threadIdx.x == 0) c0 = clock64();
@@ -303,91 +381,99 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
   if (t == 0) { *dirs = 0; *reenq = 0; scnt[0] = 0; scnt[1] = 0; scnt[2] = 0; }
   if (!__syncthreads_or(fv != 0)) {  // nothing new around the brick
     if (t == 0) atomicAdd(a.stats + 16, 1u);
-    return;
+    return true;
   }
-  // stage keys: rows [x0-1, x0+17) x [y0-1, y0+17), keys z0 .. z0+31 (8 chunks
-  // of 4) and the halo keys z0-1, z0+32, by warps 0-6: each thread keeps SU
-  // 16-byte loads in flight before it stores them.  Keys outside the grid or
-  // in a brick without occupied voxels are zero (EMPTY).  Warp 7 meanwhile
-  // claims this CTA's next brick of the pass (while much of the pass is
-  // left), so the next visit starts without a claim round trip.
-  constexpr int NST = 224;  // staging threads
-  if (t >= NST) {
-    const int lane = t - NST;
-    uint32_t nx = 0xFFFFFFFFu;
-    if (lane == 0 && i + 2u * gridDim.x < qn) {
-      const uint32_t c = atomicAdd(&a.qhead[pass % 3u], 1u);
-      if (c < qn) nx = c;
-    }
-    nx = __shfl_sync(0xFFFFFFFFu, nx, 0);
-    if (nx != 0xFFFFFFFFu && lane == 0) *pre = nx;
-  } else {
-    constexpr int SU = 6;
-    const size_t nk = (size_t)J.X * J.Y * J.Zk;
-    bool bad = false;
-    // halo keys first (their loads overlap the chunk loads): row q >> 1;
-    // side 0: key z0-1 -> [3], 1: key z0+32 -> [0]
-    uint32_t h[3];
+  // Stage the keys of the brick and its one-voxel halo.  One TMA load (a
+  // 3-D box of 36 x 18 x 18 keys at z0-4, y0-1, x0-1 of the job's keys
+  // tensor) fills the 18 x 18 rows [x0-1, x0+17) x [y0-1, y0+17) with the
+  // keys z0-4 .. z0+31: [3] holds z0-1 and [4 + z] the key z0 + z; keys
+  // outside the grid arrive as zero (EMPTY).  The keys z0+32 (slot [0]) are
+  // loaded by the threads meanwhile.  Keys of neighbour bricks without
+  // occupied voxels are never initialised, so their parts of the tile are
+  // cleared once the load has landed.  Thread 224 also claims this CTA's
+  // next brick of the pass (while much of the pass is left), so the next
+  // visit starts without a claim round trip.
+  if (t == 0) {
+    // the neighbours' key writes acquired with the change record, and this
+    // CTA's own accesses to the tile, ordered before the async-proxy copy
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_arrive_expect_tx(mbar, (uint32_t)TILE_BYTES);
+    tma_load_3d(smem_u32(tile), a.tmaps + (size_t)jid * vfk::KEYS_MAP_BYTES, z0 - 4, y0 - 1,
+                x0 - 1, mbar);
+  }
+  uint32_t htop[2];
+  bool bad = false;
 #pragma unroll
-    for (int u = 0; u < 3; ++u) {
-      const int q = t + u * NST;
-      h[u] = 0;
-      if (q < KROWS * 2) {
-        const int row = q >> 1, side = q & 1;
-        const int lx = row / KNY - 1, ly = row % KNY - 1;
-        const int x = x0 + lx, y = y0 + ly, z = side ? z0 + VF_BZ : z0 - 1;
-        if (x >= 0 && y >= 0 && z >= 0 && x < (int)J.X && y < (int)J.Y && z < (int)J.Zk) {
-          const int dx = lx < 0 ? 0 : (lx >= VF_BX ? 2 : 1);
-          const int dy = ly < 0 ? 0 : (ly >= VF_BY ? 2 : 1);
-          if (live27[dx * 9 + dy * 3 + (side ? 2 : 0)]) {
-            const size_t ki = vf_kidx(J, x, y, z);
-            if (ki < nk) h[u] = __ldcg(J.keys + ki);
-            else bad = true;
-          }
+  for (int u = 0; u < 2; ++u) {
+    const int q = t + u * 256;
+    htop[u] = 0;
+    if (q < KROWS) {
+      const int lx = q / KNY - 1, ly = q % KNY - 1;
+      const int x = x0 + lx, y = y0 + ly, z = z0 + VF_BZ;
+      if (x >= 0 && y >= 0 && x < (int)J.X && y < (int)J.Y && z < (int)J.Zk) {
+        const int dx = lx < 0 ? 0 : (lx >= VF_BX ? 2 : 1);
+        const int dy = ly < 0 ? 0 : (ly >= VF_BY ? 2 : 1);
+        if (live27[dx * 9 + dy * 3 + 2]) {
+          const size_t ki = vf_kidx(J, x, y, z);
+          if (ki < (size_t)J.X * J.Y * J.Zk) htop[u] = __ldcg(J.keys + ki);
+          else bad = true;
         }
       }
     }
-#pragma unroll 1
-    for (int base = t; base < KROWS * 8; base += SU * NST) {
-      uint4 v[SU];
+  }
+  if (t == 224 && i + 2u * gridDim.x < qn) {
+    const uint32_t c = atomicAdd(&a.qhead[pass % 3u], 1u);
+    if (c < qn) *pre = c;
+  }
+  if (bad) flood_anomaly(a, 3u, b, (uint32_t)t);
+  const bool landed = mbar_wait(mbar, phase);
+  if (__syncthreads_or(!landed)) {
+    // the copy did not complete in time: report it, give it one more bounded
+    // wait so that nothing is in flight into this CTA's tile, and stop
+    if (t == 0) atomicOr(a.err, 16u);
+    mbar_wait(mbar, phase);
+    return false;
+  }
+  phase ^= 1u;
+  // clear the parts of bricks without occupied voxels, place the keys z0+32
 #pragma unroll
-      for (int u = 0; u < SU; ++u) {
-        const int q = base + u * NST;
-        v[u] = make_uint4(0, 0, 0, 0);
-        if (q < KROWS * 8) {
-          const int row = q >> 3, part = q & 7;
-          const int lx = row / KNY - 1, ly = row % KNY - 1;
-          const int x = x0 + lx, y = y0 + ly, z = z0 + 4 * part;
-          if (x >= 0 && y >= 0 && x < (int)J.X && y < (int)J.Y && z < (int)J.Zk) {
-            const int dx = lx < 0 ? 0 : (lx >= VF_BX ? 2 : 1);
-            const int dy = ly < 0 ? 0 : (ly >= VF_BY ? 2 : 1);
-            if (live27[dx * 9 + dy * 3 + 1]) {
-              const size_t ki = vf_kidx(J, x, y, z);
-              const uint32_t* src = J.keys + ki;
-              if (ki + 4 <= nk && (reinterpret_cast<uintptr_t>(src) & 15u) == 0)
-                v[u] = __ldcg(reinterpret_cast<const uint4*>(src));
-              else
-                bad = true;
-            }
-          }
-        }
+  for (int u = 0; u < 2; ++u) {
+    const int q = t + u * 256;
+    if (q < KROWS) {
+      uint32_t* row = tile + q * KP;
+      const int lx = q / KNY, ly = q % KNY;
+      const int dx = lx == 0 ? 0 : (lx == KNX - 1 ? 2 : 1);
+      const int dy = ly == 0 ? 0 : (ly == KNY - 1 ? 2 : 1);
+      if (!live27[dx * 9 + dy * 3 + 1]) {
+#pragma unroll
+        for (int c = 0; c < VF_BZ / 4; ++c)
+          *reinterpret_cast<uint4*>(row + 4 + 4 * c) = make_uint4(0, 0, 0, 0);
       }
-#pragma unroll
-      for (int u = 0; u < SU; ++u) {
-        const int q = base + u * NST;
-        if (q < KROWS * 8) *reinterpret_cast<uint4*>(tile + (q >> 3) * KP + 4 + 4 * (q & 7)) = v[u];
-      }
+      if (!live27[dx * 9 + dy * 3 + 0]) row[3] = 0u;
+      row[0] = htop[u];
     }
-#pragma unroll
-    for (int u = 0; u < 3; ++u) {
-      const int q = t + u * NST;
-      if (q < KROWS * 2) tile[(q >> 1) * KP + ((q & 1) ? 0 : 3)] = h[u];
-    }
-    if (bad) flood_anomaly(a, 3u, b, (uint32_t)t);
   }
   __syncthreads();
   long long c1 = 0;
   if (t == 0) { c1 = clock64(); ph[1] += c1 - c0; }
+  // The tile of the brick this CTA claimed next goes into L2 while this one
+  // relaxes (thread 255 rarely has a row to run), so its staging reads L2.
+  if (t == 255) {
+    const uint32_t ni = *pre;
+    if (ni != 0xFFFFFFFFu && ni < qn) {
+      const uint32_t nb = a.queue[pass % 3u][ni];
+      const uint32_t nj = nb < a.nbricks ? a.brick_job[nb] : 0xFFFFFFFFu;
+      if (nj < a.njobs) {
+        const JobDesc& N = a.jobs[nj];
+        const uint32_t nl = nb - N.brick_base;
+        const int nz = nl % N.nbz, ny = (nl / N.nbz) % N.nby, nx = nl / (N.nbz * N.nby);
+        tma_prefetch_3d(a.tmaps + (size_t)nj * vfk::KEYS_MAP_BYTES, nz * VF_BZ - 4,
+                        ny * VF_BY - 1, nx * VF_BX - 1);
+      }
+    }
+  }
   const int tx = t / VF_BY, ty = t % VF_BY;
   uint32_t* own_row = tile + ((tx + 1) * KNY + (ty + 1)) * KP;
   // Row layout (KP u32): [0] key z0+32, [3] key z0-1, [4 + z] key z0 + z.  The
@@ -423,14 +509,9 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
 #pragma unroll
       for (int dy = 0; dy < 3; ++dy)
         if ((dxm >> dx) & (dym >> dy) & 1u) hit |= (d >> (dx * 9 + dy * 3)) & 7u;
+    // the z neighbours name exactly the rows whose end voxel they improve
     const uint32_t zc = (((fbits[1 + (tx >> 1)] | fbits[9 + (tx >> 1)]) >> ((tx & 1) * 16)) & 0xFFFFu);
-    if (CONN == 26) {
-      const uint32_t zl = tx > 0 ? (((fbits[1 + ((tx - 1) >> 1)] | fbits[9 + ((tx - 1) >> 1)]) >> (((tx - 1) & 1) * 16)) & 0xFFFFu) : 0u;
-      const uint32_t zr = tx < VF_BX - 1 ? (((fbits[1 + ((tx + 1) >> 1)] | fbits[9 + ((tx + 1) >> 1)]) >> (((tx + 1) & 1) * 16)) & 0xFFFFu) : 0u;
-      hit |= (((zl | zc | zr) << 1) >> ty) & 7u;
-    } else {
-      hit |= (zc >> ty) & 1u;
-    }
+    hit |= (zc >> ty) & 1u;
     act0 = hit != 0;
   }
   // Sweeps.  The rows to run are compacted onto the lowest threads (one list
@@ -457,21 +538,24 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
         active = ((((m0 | m2) >> ty) & 1u) | ((m1 << 1) & (5u << ty))) != 0;
     }
     const unsigned bal = __ballot_sync(0xFFFFFFFFu, active);
-    if (lane == 0) sw.wcnt[wid] = (uint32_t)__popc(bal);
+    if (lane == 0) sw.wmask[wid] = bal;
     if (t < 8) sw.rfw[(cur ^ 1) * 8 + t] = 0u;  // filled by this sweep's changes
     __syncthreads();
-    uint32_t base = 0, n = 0;
+    // thread t takes the t-th active row: the k-th active lane of warp ws
+    uint32_t n = 0, k = 0;
+    int ws = 0;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-      const uint32_t c = sw.wcnt[i];
-      base += i < wid ? c : 0u;
+      const uint32_t c = (uint32_t)__popc(sw.wmask[i]);
+      if ((uint32_t)t >= n && (uint32_t)t < n + c) {
+        ws = i;
+        k = (uint32_t)t - n;
+      }
       n += c;
     }
-    if (active) sw.rlist[base + __popc(bal & ((1u << lane) - 1u))] = (uint16_t)t;
-    __syncthreads();
     uint32_t chg = 0;
     if (t < (int)n) {
-      const int row = sw.rlist[t];
+      const int row = 32 * ws + nth_set_bit(sw.wmask[ws], k);
       uint32_t* rr = tile + (((row >> 4) + 1) * KNY + ((row & 15) + 1)) * KP;
       chg = relax_row<CONN>(rr, sw.hl[row], sw.hh[row], it == 0);
       if (chg) {
@@ -543,39 +627,131 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     }
   }
   if (overflow) atomicOr(&a.st[jid].err, VF_JERR_DIST_OVERFLOW);
-  // neighbour bricks touched by changed boundary voxels
-  if (changed) {
-    uint32_t dm = 0;
-    const int lastz = min(VF_BZ, (int)J.Z - z0) - 1;
-    const bool zl = (changed & 1u) != 0, zh = lastz >= 0 && (changed >> lastz) & 1u;
-    const bool xl = tx == 0, xh = tx == VF_BX - 1 || x == (int)J.X - 1;
-    const bool yl = ty == 0, yh = ty == VF_BY - 1 || y == (int)J.Y - 1;
-    if (CONN == 6) {
-      if (xl) dm |= 1u << (0 * 9 + 1 * 3 + 1);
-      if (xh) dm |= 1u << (2 * 9 + 1 * 3 + 1);
-      if (yl) dm |= 1u << (1 * 9 + 0 * 3 + 1);
-      if (yh) dm |= 1u << (1 * 9 + 2 * 3 + 1);
-      if (zl) dm |= 1u << (1 * 9 + 1 * 3 + 0);
-      if (zh) dm |= 1u << (1 * 9 + 1 * 3 + 2);
-    } else {
-      for (int dx = 0; dx < 3; ++dx) {
-        if ((dx == 0 && !xl) || (dx == 2 && !xh)) continue;
-        for (int dy = 0; dy < 3; ++dy) {
-          if ((dy == 0 && !yl) || (dy == 2 && !yh)) continue;
-          for (int dz = 0; dz < 3; ++dz) {
-            if ((dz == 0 && !zl) || (dz == 2 && !zh)) continue;
-            dm |= 1u << (dx * 9 + dy * 3 + dz);
-          }
+  // Notifications.  A neighbour brick is queued (and its change record set)
+  // only when a voxel this visit changed can improve one of its voxels,
+  // judged against the neighbour's keys staged in the halo.  Staged keys can
+  // only be lower than the neighbour's current ones (keys never decrease),
+  // so a halo voxel that no changed voxel improves here cannot be improved
+  // in the neighbour either: skipping it loses nothing.  This drops the
+  // visits a front would otherwise send back to the brick it came from.
+  // changed key of interior row r (brick coordinates) at z, or 0
+  auto chg_key = [&](int rx, int ry, int z) -> uint32_t {
+    const uint32_t c = sw.rowchg[rx * VF_BY + ry];
+    return ((c >> z) & 1u) ? tile[((rx + 1) * KNY + (ry + 1)) * KP + 4 + z] : 0u;
+  };
+  // (a) the z faces, per interior row: the halo voxels below (z0-1) and
+  //     above (z0+32) the row, against the changed keys of the window rows
+  //     at z0 and z0+31 (26: the interior rows of the 3x3 around; 6: the row)
+  bool lo_imp = false, hi_imp = false;
+  {
+    const uint32_t klo = own_row[3], khi = own_row[0];
+    if (klo | khi) {
+      uint32_t mlo = 0, mhi = 0;
+      if (CONN == 26) {
+#pragma unroll
+        for (int r = 0; r < 9; ++r) {
+          const int rx = tx + r / 3 - 1, ry = ty + r % 3 - 1;
+          if (rx < 0 || ry < 0 || rx >= VF_BX || ry >= VF_BY) continue;
+          mlo = max(mlo, chg_key(rx, ry, 0));
+          mhi = max(mhi, chg_key(rx, ry, VF_BZ - 1));
         }
+      } else {
+        mlo = chg_key(tx, ty, 0);
+        mhi = chg_key(tx, ty, VF_BZ - 1);
+      }
+      lo_imp = klo != 0u && step_from(mlo) > klo;
+      hi_imp = khi != 0u && step_from(mhi) > khi;
+    }
+  }
+  // (b) the x/y faces, edges and corners: one thread per halo row of the
+  //     tile's perimeter.  C(z) = the largest changed key at z among the
+  //     interior rows next to the halo row; a halo voxel at z is improvable
+  //     when step(max of C over its z window) beats its key.  Chunks of four
+  //     keys with one chunk of look-ahead, as in relax_row.
+  if (t < 2 * KNY + 2 * VF_BX) {
+    const int lx = t < KNY ? 0 : t < 2 * KNY ? KNX - 1 : 1 + (t - 2 * KNY) % VF_BX;
+    const int ly = t < KNY ? t : t < 2 * KNY ? t - KNY : (t < 2 * KNY + VF_BX ? 0 : KNY - 1);
+    const uint32_t* hr = tile + (lx * KNY + ly) * KP;
+    // Interior rows next to this halo row, as a line of up to three rows
+    // (brick coordinates): the halo row's inward neighbour (ix, iy) and, for
+    // 26, its two neighbours along the halo edge (dx, dy) when inside.  A
+    // corner halo row has one (26) or none (6).  Rows outside get a zero mask.
+    const bool xs = lx == 0 || lx == KNX - 1, ys = ly == 0 || ly == KNY - 1;
+    const int ix = lx == 0 ? 0 : (lx == KNX - 1 ? VF_BX - 1 : lx - 1);
+    const int iy = ly == 0 ? 0 : (ly == KNY - 1 ? VF_BY - 1 : ly - 1);
+    const int ex = xs ? 0 : 1, ey = xs ? 1 : 0;  // direction along the edge
+    uint32_t cm[3] = {0u, 0u, 0u};
+    int base_row = (ix + 1) * KNY + (iy + 1);    // tile row of the middle row
+    const int stride_row = ex * KNY + ey;        // tile rows between the three
+    if (CONN == 26 || xs != ys) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int rx = ix + (k - 1) * ex, ry = iy + (k - 1) * ey;
+        const bool in = (CONN == 26 || k == 1) && rx >= 0 && ry >= 0 && rx < VF_BX && ry < VF_BY &&
+                        !(xs && ys && k != 1);
+        cm[k] = in ? sw.rowchg[rx * VF_BY + ry] : 0u;
       }
     }
-    dm &= ~(1u << 13);  // self
-    if (dm) atomicOr(dirs, dm);
+    const uint32_t u = cm[0] | cm[1] | cm[2];
+    if (u) {
+      // changed keys of the adjacent rows at chunk q, column maximum
+      auto chunkC = [&](int q) -> uint4 {
+        uint4 c = make_uint4(0, 0, 0, 0);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const uint32_t m = cm[k] >> (4 * q);
+          if (!(m & 0xFu)) continue;
+          const uint4 v = lds4(tile + (base_row + (k - 1) * stride_row) * KP + 4 + 4 * q);
+          c.x = max(c.x, (m & 1u) ? v.x : 0u);
+          c.y = max(c.y, (m & 2u) ? v.y : 0u);
+          c.z = max(c.z, (m & 4u) ? v.z : 0u);
+          c.w = max(c.w, (m & 8u) ? v.w : 0u);
+        }
+        return c;
+      };
+      auto imp = [](uint32_t w, uint32_t kh) { return kh != 0u && step_from(w) > kh; };
+      bool face = false, below = false, above = false;
+      uint4 Cc = chunkC(0);
+      uint32_t cprev = 0;
+      if (CONN == 26) below = imp(Cc.x, hr[3]);  // z0-1 reads C(z0)
+#pragma unroll 1
+      for (int q = 0; q < 8; ++q) {
+        // changed keys at z = 4q-1 .. 4q+4 reach this chunk's halo voxels
+        const uint32_t win = q == 0 ? (u & 0x1Fu) : ((u >> (4 * q - 1)) & 0x3Fu);
+        if (win) {
+          const uint4 Cn = (CONN == 26 && q < 7) ? chunkC(q + 1) : make_uint4(0, 0, 0, 0);
+          const uint4 kh = lds4(hr + 4 + 4 * q);
+          uint32_t w0, w1, w2, w3;
+          if (CONN == 26) {
+            w0 = max(cprev, max(Cc.x, Cc.y));
+            w1 = max(Cc.x, max(Cc.y, Cc.z));
+            w2 = max(Cc.y, max(Cc.z, Cc.w));
+            w3 = max(Cc.z, max(Cc.w, Cn.x));
+          } else {
+            w0 = Cc.x; w1 = Cc.y; w2 = Cc.z; w3 = Cc.w;
+          }
+          face |= imp(w0, kh.x) | imp(w1, kh.y) | imp(w2, kh.z) | imp(w3, kh.w);
+          cprev = Cc.w;
+          Cc = CONN == 26 ? Cn : (q < 7 ? chunkC(q + 1) : Cc);
+        } else {
+          cprev = 0u;
+          Cc = q < 7 ? chunkC(q + 1) : Cc;
+        }
+      }
+      if (CONN == 26) above = imp(cprev, hr[0]);  // z0+32 reads C(z0+31)
+      const int sx = lx == 0 ? 0 : (lx == KNX - 1 ? 2 : 1);
+      const int sy = ly == 0 ? 0 : (ly == KNY - 1 ? 2 : 1);
+      const uint32_t dmh = (below ? 1u << (sx * 9 + sy * 3 + 0) : 0u) |
+                           (face ? 1u << (sx * 9 + sy * 3 + 1) : 0u) |
+                           (above ? 1u << (sx * 9 + sy * 3 + 2) : 0u);
+      if (dmh) atomicOr(dirs, dmh);
+    }
   }
-  // rows whose bottom / top key layer changed (the z neighbours' halo keys)
-  const int lastz_all = min(VF_BZ, (int)J.Z - z0) - 1;
-  const unsigned zlo = __ballot_sync(0xFFFFFFFFu, (changed & 1u) != 0);
-  const unsigned zhi = __ballot_sync(0xFFFFFFFFu, lastz_all >= 0 && ((changed >> lastz_all) & 1u));
+  // rows of the z neighbours that read an improvable key (exact row masks)
+  const unsigned zlo = __ballot_sync(0xFFFFFFFFu, lo_imp);
+  const unsigned zhi = __ballot_sync(0xFFFFFFFFu, hi_imp);
+  if ((t & 31) == 0 && (zlo | zhi))
+    atomicOr(dirs, (zlo ? 1u << (1 * 9 + 1 * 3 + 0) : 0u) | (zhi ? 1u << (1 * 9 + 1 * 3 + 2) : 0u));
   // statistics: active row-sweeps and key changes (block sums in shared memory)
   if (nact) atomicAdd(&scnt[0], nact);
   if (nchg) atomicAdd(&scnt[1], nchg);
@@ -590,6 +766,7 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     atomicAdd(a.stats + 6, scnt[0]);
     atomicAdd(a.stats + 7, scnt[1]);
     atomicAdd(a.stats + 2, scnt[2]);
+    if (scnt[1] == 0) atomicAdd(a.stats + 17, 1u);  // staged, but no key changed
   }
   // change records of the neighbours, after the key writes above (fence), then
   // the neighbours go on the next pass's queue
@@ -624,6 +801,7 @@ __device__ void relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     enqueue(a, nb, pass + 1, want);
   }
   if (t == 0) ph[3] += clock64() - c2;
+  return true;
 }
 
 __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
@@ -633,8 +811,10 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
   __shared__ FloodArgs a;
   if (threadIdx.x == 0) a = args;
   __syncthreads();
+  // the tile, a TMA destination: 128-byte aligned inside the dynamic shared
+  // memory (TILE_SMEM = TILE_BYTES + 128)
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  uint32_t* tile = reinterpret_cast<uint32_t*>(smem_raw);
+  uint32_t* tile = reinterpret_cast<uint32_t*>(smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u));
   __shared__ uint32_t live27[27];
   __shared__ uint32_t dirs;
   __shared__ int reenq;
@@ -643,8 +823,16 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
   __shared__ SweepShared sw;
   __shared__ uint32_t fbits[FLOOD_FDIR];
   __shared__ unsigned long long ph[5];  // thread 0: SM cycles per phase (see flush below)
+  __shared__ __align__(8) unsigned long long tile_bar;  // completion of the tile loads
+  const uint32_t mbar = smem_u32(&tile_bar);
+  uint32_t phase = 0;  // parity of the tile load in flight (uniform across the CTA)
   if (threadIdx.x < 5) ph[threadIdx.x] = 0;
-  if (threadIdx.x == 0) pre = 0xFFFFFFFFu;
+  if (threadIdx.x == 0) {
+    pre = 0xFFFFFFFFu;
+    mbar_init(mbar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
   for (uint32_t p = 0; p < a.max_passes; ++p) {
     const uint32_t cur = p % 3u;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -678,8 +866,12 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
       const JobDesc& J = a.jobs[jid];
       const int conn6 = J.distance == 1;
       if (threadIdx.x == 0) ph[0] += clock64() - c_claim;
-      if (conn6) relax_brick<6>(a, J, jid, b, p, tile, live27, &dirs, &reenq, sw, fbits, ph, i, qn, &pre);
-      else relax_brick<26>(a, J, jid, b, p, tile, live27, &dirs, &reenq, sw, fbits, ph, i, qn, &pre);
+      const bool ok =
+          conn6 ? relax_brick<6>(a, J, jid, b, p, tile, live27, &dirs, &reenq, sw, fbits, ph, i,
+                                 qn, &pre, mbar, phase)
+                : relax_brick<26>(a, J, jid, b, p, tile, live27, &dirs, &reenq, sw, fbits, ph, i,
+                                  qn, &pre, mbar, phase);
+      if (!ok) return;  // tile load timed out (error word set; the others stop at the barrier)
       if (threadIdx.x == 0) atomicMax(&a.st[jid].passes, p + 1);
       ++visits;
     }
@@ -1002,6 +1194,43 @@ __global__ void k_enqueue_pass2(const JobDesc* jobs, const JobState* st, const u
 
 namespace vfk {
 
+namespace {
+PFN_cuTensorMapEncodeTiled_v12000 g_encode_tiled = nullptr;
+std::once_flag g_encode_once;
+}  // namespace
+
+bool encode_keys_map(void* map128, const uint32_t* keys, uint32_t X, uint32_t Y, uint32_t Zk,
+                     std::string* err) {
+  std::call_once(g_encode_once, [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_encode_tiled = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    cudaGetLastError();
+  });
+  if (!g_encode_tiled) {
+    if (err) *err = "cuTensorMapEncodeTiled is not available from the CUDA driver";
+    return false;
+  }
+  // dims innermost first: z (Zk, a multiple of 4: 16-byte row strides), y, x
+  const cuuint64_t dims[3] = {Zk, Y, X};
+  const cuuint64_t strides[2] = {(cuuint64_t)Zk * 4u, (cuuint64_t)Zk * 4u * Y};
+  const cuuint32_t box[3] = {(cuuint32_t)KP, (cuuint32_t)KNY, (cuuint32_t)KNX};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = g_encode_tiled(
+      static_cast<CUtensorMap*>(map128), CU_TENSOR_MAP_DATA_TYPE_UINT32, 3,
+      const_cast<uint32_t*>(keys), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+      CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    if (err) *err = "cuTensorMapEncodeTiled failed (CUresult " + std::to_string((int)r) + ")";
+    return false;
+  }
+  return true;
+}
+
 static inline int brick_grid(uint32_t max_count) {
   uint32_t g = max_count ? max_count : 1;
   return (int)(g > (1u << 20) ? (1u << 20) : g);
@@ -1035,8 +1264,8 @@ static int relax_blocks(int num_sms) {
   const int dv = cur_dev();
   if (per_sm[dv] < 1) {
     int n = 0;
-    cudaFuncSetAttribute(k_relax, cudaFuncAttributeMaxDynamicSharedMemorySize, TILE_BYTES);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_relax, 256, TILE_BYTES) != cudaSuccess)
+    cudaFuncSetAttribute(k_relax, cudaFuncAttributeMaxDynamicSharedMemorySize, TILE_SMEM);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_relax, 256, TILE_SMEM) != cudaSuccess)
       n = 1;
     per_sm[dv] = n < 1 ? 1 : n;
   }
@@ -1069,12 +1298,14 @@ cudaError_t flood_relax(cudaStream_t st, const JobDesc* dj, JobState* ds,
   a.nbricks = fs.total_bricks;
   a.njobs = fs.njobs;
   a.wait_spins = fs.wait_spins ? fs.wait_spins : (1u << 26);
+  a.tmaps = static_cast<const unsigned char*>(fs.tmaps);
+  if (!a.tmaps) return cudaErrorInvalidValue;
   int blocks = relax_blocks(num_sms);
   if (fs.ctas_per_sm > 0 && fs.ctas_per_sm * num_sms < blocks) blocks = fs.ctas_per_sm * num_sms;
   if (blocks_used) *blocks_used = blocks;
   void* args[] = {&a};
   return cudaLaunchCooperativeKernel((const void*)k_relax, dim3(blocks), dim3(256), args,
-                                     TILE_BYTES, st);
+                                     TILE_SMEM, st);
 }
 
 void flood_finalize(cudaStream_t st, const JobDesc* dj, const JobState* ds, const uint32_t* list,

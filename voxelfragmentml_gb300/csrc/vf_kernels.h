@@ -4,6 +4,7 @@
 // vf_runtime.cu) plus the per-job JobState array, and enqueues on `st`.
 // Brick-parallel stages take the list of live bricks and brick_job map.
 #pragma once
+#include <string>
 #include "vf_common.cuh"
 
 namespace vfk {
@@ -196,6 +197,14 @@ inline int cur_dev() {
   return d & 63;
 }
 
+// TMA descriptor (CUtensorMap, 128 bytes, 64-byte aligned) of one job's
+// flood keys uint32 [X][Y][Zk], encoded on the host for k_relax's tile
+// loads: boxes of 36 x 18 x 18 keys (z, y, x), zeros outside the grid.
+constexpr size_t KEYS_MAP_BYTES = 128;
+// false (message in *err) when the driver cannot encode the map
+bool encode_keys_map(void* map128, const uint32_t* keys, uint32_t X, uint32_t Y, uint32_t Zk,
+                     std::string* err);
+
 struct FloodScratch {
   uint32_t* queue[3];    // brick ids, capacity total_bricks each (rotating)
   uint32_t* qcount;      // [3]
@@ -211,6 +220,7 @@ struct FloodScratch {
   int max_sweeps = 0;    // tuning: sweeps per brick visit (0: default cap)
   int ctas_per_sm = 0;   // tuning: resident CTAs per SM (0: as many as fit)
   uint32_t wait_spins = 0;  // spins of the pass barrier before it gives up (0: 2^26, ~4 s)
+  const void* tmaps = nullptr;  // [njobs] keys tensor maps (KEYS_MAP_BYTES each, device)
   uint32_t* pass_sizes = nullptr;  // statistics: bricks queued per pass (256)
 };
 void flood_init_keys(cudaStream_t st, const JobDesc* dj, const uint32_t* list,

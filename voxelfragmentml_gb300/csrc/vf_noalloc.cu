@@ -38,8 +38,16 @@ static __device__ __align__(256) unsigned char g_scratch[VF_NOALLOC_SCRATCH_BYTE
 
 namespace {
 
-__global__ void k_noalloc_init(JobDesc d, JobDesc* dst, JobState* st, uint32_t* scal) {
+// the keys tensor map, passed by value into the scratch array
+struct KeysMap {
+  alignas(64) unsigned char b[vfk::KEYS_MAP_BYTES];
+};
+
+__global__ void k_noalloc_init(JobDesc d, JobDesc* dst, JobState* st, uint32_t* scal, KeysMap m,
+                               KeysMap* mdst) {
   if (threadIdx.x == 0) *dst = d;
+  if (threadIdx.x < vfk::KEYS_MAP_BYTES / 4)
+    reinterpret_cast<uint32_t*>(mdst->b)[threadIdx.x] = reinterpret_cast<const uint32_t*>(m.b)[threadIdx.x];
   unsigned char* s = reinterpret_cast<unsigned char*>(st);
   for (uint32_t i = threadIdx.x; i < sizeof(JobState); i += blockDim.x) s[i] = 0;
   for (uint32_t i = threadIdx.x; i < 1024; i += blockDim.x) scal[i] = 0;
@@ -95,6 +103,7 @@ extern "C" vf_status vf_flood_noalloc(const uint16_t* d_grid, uint16_t* d_labels
   const size_t o_desc = off; off += up(sizeof(JobDesc));
   const size_t o_state = off; off += up(sizeof(JobState));
   const size_t o_scal = off; off += up(4096);
+  const size_t o_map = off; off += up(sizeof(KeysMap));
   const size_t o_bj = off; off += up(nb * 4);
   const size_t o_live = off; off += up(nb);
   const size_t o_list = off; off += up(nb * 4);
@@ -142,7 +151,15 @@ extern "C" vf_status vf_flood_noalloc(const uint16_t* d_grid, uint16_t* d_labels
     if (e_ != cudaSuccess)                                                                  \
       return fail(VF_ERR_CUDA, std::string("vf_flood_noalloc: ") + cudaGetErrorString(e_)); \
   } while (0)
-  k_noalloc_init<<<1, 256, 0, st>>>(d, ddesc, dstate, scal);
+  KeysMap km;
+  std::memset(&km, 0, sizeof(km));
+  {
+    std::string why;
+    if (!vfk::encode_keys_map(km.b, keys, X, Y, Zk, &why))
+      return fail(VF_ERR_CUDA, "vf_flood_noalloc: " + why);
+  }
+  KeysMap* dmap = reinterpret_cast<KeysMap*>(S + o_map);
+  k_noalloc_init<<<1, 256, 0, st>>>(d, ddesc, dstate, scal, km, dmap);
   // padded copy of the caller's grid (padding z >= Z is zero)
   NA_CK(cudaMemsetAsync(grid, 0, (size_t)X * Y * Zp * 2, st));
   NA_CK(cudaMemcpy2DAsync(grid, (size_t)Zp * 2, d_grid, (size_t)Z * 2, (size_t)Z * 2,
@@ -167,6 +184,7 @@ extern "C" vf_status vf_flood_noalloc(const uint16_t* d_grid, uint16_t* d_labels
   fs.max_passes = 1u << 20;
   fs.total_bricks = (uint32_t)nb;
   fs.njobs = 1;
+  fs.tmaps = dmap;
   if (nseeds) vfk::flood_seed_bricks(st, ddesc, dstate, 1, live, list, lcount);
   vfk::flood_init_keys(st, ddesc, list, lcount, (uint32_t)nb, bj, live);
   if (nseeds) {

@@ -137,7 +137,7 @@ void Batch::release() {
                     &verts, &faces, &emask, &etab, &tables, &state, &brick_job, &live, &list, &lcount,
                     &q[0], &q[1], &q[2], &scal, &epoch, &fdir, &front[0], &front[1], &pcnt, &pbase,
                     &psums, &srec, &stage_out, &rle_cnt, &rle_base, &rle_sums, &rle_tot, &rle_starts,
-                    &rle_rec})
+                    &rle_rec, &tmaps})
     ctx->free_buf(*b);
   if (h_tables) cudaFreeHost(h_tables);
   if (h_state) cudaFreeHost(h_state);
@@ -387,8 +387,12 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
   ALLOC(psums, ((nf + 1023) / 1024 + 1) * 8);
   ALLOC(srec, nf * 96);
   if (sz.out) ALLOC(stage_out, sz.out * 2);
+  ALLOC(tmaps, vfk::KEYS_MAP_BYTES * std::max<size_t>(n, 1));
 #undef ALLOC
-  const size_t tbytes = sizeof(JobDesc) * ntables * std::max<size_t>(n, 1) + sz.emask * 4 + 256;
+  // pinned staging: stage tables, erosion masks, then the keys tensor maps
+  // (128-byte aligned, as CUtensorMap requires 64)
+  tmap_off = align_up(sizeof(JobDesc) * ntables * std::max<size_t>(n, 1) + sz.emask * 4, 128);
+  const size_t tbytes = tmap_off + vfk::KEYS_MAP_BYTES * std::max<size_t>(n, 1) + 256;
   if (tbytes > h_tables_cap) {
     if (h_tables) cudaFreeHost(h_tables);
     h_tables_cap = align_up(tbytes * 2, 1 << 16);
@@ -416,6 +420,13 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
     uint16_t* g0 = static_cast<uint16_t*>(grid0.p) + p.o_grid;
     uint16_t* g1 = static_cast<uint16_t*>(grid1.p) + p.o_grid;
     d.keys = static_cast<uint32_t*>(keys.p) + p.o_keys;
+    {
+      void* map = static_cast<char*>(h_tables) + tmap_off + vfk::KEYS_MAP_BYTES * i;
+      std::memset(map, 0, vfk::KEYS_MAP_BYTES);
+      std::string why;
+      if (j.params.algorithm == VF_FLOOD && !vfk::encode_keys_map(map, d.keys, p.X, p.Y, p.Zk, &why))
+        return fail(VF_ERR_CUDA, "job " + std::to_string(i) + ": " + why);
+    }
     d.par = static_cast<uint32_t*>(par.p) + p.o_par;
     d.shell = static_cast<uint32_t*>(par.p) + sz.par + p.o_par;
     d.verts = static_cast<float*>(verts.p) + p.o_verts;
@@ -551,6 +562,8 @@ static vf_status upload_inputs_impl(Batch& B) {
   if (B.sz.emask)
     VF_CK(cudaMemcpyAsync(B.emask.p, static_cast<char*>(B.h_tables) + tb, B.sz.emask * 4,
                           cudaMemcpyHostToDevice, st));
+  VF_CK(cudaMemcpyAsync(B.tmaps.p, static_cast<char*>(B.h_tables) + B.tmap_off,
+                        vfk::KEYS_MAP_BYTES * n, cudaMemcpyHostToDevice, st));
   return VF_OK;
 }
 
@@ -614,7 +627,7 @@ static vfk::FloodScratch flood_scratch(Batch& B) {
   fs.qhead = sc + 4;     // [3]
   fs.barrier = sc + 8;   // [2]
   fs.err = sc + 12;      // [1]
-  fs.stats = sc + 16;    // [17]: visits, passes, busy warp-sweeps, timeouts, sweeps,
+  fs.stats = sc + 16;    // [VF_FLOOD_NCOUNTERS]: visits, passes, busy warp-sweeps, timeouts, sweeps,
                          // sweep-cap hits, active row-sweeps, changed voxels, the
                          // first out-of-range access (code, two values), the SM
                          // cycles / 256 of five phases of the relaxation CTAs and
@@ -627,6 +640,7 @@ static vfk::FloodScratch flood_scratch(Batch& B) {
   fs.max_sweeps = B.ctx->tune.flood_sweeps;
   fs.ctas_per_sm = B.ctx->tune.flood_ctas;
   fs.wait_spins = B.ctx->tune.flood_wait_spins;
+  fs.tmaps = B.tmaps.p;
   fs.pass_sizes = sc + 128;  // [256]
   return fs;
 }
@@ -844,10 +858,10 @@ vf_status Batch::finish(vf_job_result* res) {
     ctx->last_flood_passes = h_scal[17];
     ctx->last_flood_sweeps = h_scal[20];
     ctx->last_flood_maxit = h_scal[21];
-    for (int i = 0; i < 17; ++i) ctx->last_flood_counters[i] = h_scal[16 + i];
+    for (int i = 0; i < VF_FLOOD_NCOUNTERS; ++i) ctx->last_flood_counters[i] = h_scal[16 + i];
     for (int i = 0; i < 256; ++i) ctx->last_pass_sizes[i] = h_scal[128 + i];
   } else {
-    for (int i = 0; i < 17; ++i) ctx->last_flood_counters[i] = 0;
+    for (int i = 0; i < VF_FLOOD_NCOUNTERS; ++i) ctx->last_flood_counters[i] = 0;
     ctx->last_flood_ms = 0.f;
     ctx->last_flood_visits = 0;
     ctx->last_flood_passes = 0;

@@ -67,6 +67,8 @@ struct Batch {
   DevBuf tables, state, brick_job, live, list, lcount, q[3], scal, epoch, fdir, front[2];
   DevBuf pcnt, pbase, psums, srec;  // flattened per-face work lists, shell setup
   DevBuf stage_out;  // packed labels of the DMA download
+  DevBuf tmaps;      // [jobs] TMA descriptors of the flood keys (vfk::KEYS_MAP_BYTES each)
+  size_t tmap_off = 0;  // their host copy inside h_tables
   // download by DMA: labels are copied to out_labels by the copy engine, from
   // the label grid when its rows have no padding, else packed first into a
   // device staging buffer (no kernel writes host memory, so the download of
@@ -161,7 +163,7 @@ struct Ctx {
   uint64_t last_flood_visits = 0;
   uint64_t last_flood_passes = 0;
   uint64_t last_flood_sweeps = 0;
-  uint64_t last_flood_counters[17] = {};  // raw flood counters of the last batched run
+  uint64_t last_flood_counters[VF_FLOOD_NCOUNTERS] = {};  // raw flood counters of the last batched run
   uint32_t last_pass_sizes[256] = {};    // bricks queued per flood pass (first 256)
   uint64_t last_flood_maxit = 0;
   vf_status alloc(DevBuf& b, size_t bytes);
