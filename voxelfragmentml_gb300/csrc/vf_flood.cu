@@ -100,11 +100,6 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
     if (mbar_try_wait(mbar, phase)) return true;
   return false;
 }
-// the same box into L2 only (a hint: no completion, no shared memory)
-__device__ __forceinline__ void tma_prefetch_3d(const void* map, int c0, int c1, int c2) {
-  asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];"
-               ::"l"(map), "r"(c0), "r"(c1), "r"(c2) : "memory");
-}
 // box of the 3-D tensor `map` at (c0 innermost, c1, c2) into shared memory,
 // completion counted in bytes on the mbarrier
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const void* map, int c0, int c1, int c2,
@@ -458,22 +453,6 @@ __device__ bool relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
   __syncthreads();
   long long c1 = 0;
   if (t == 0) { c1 = clock64(); ph[1] += c1 - c0; }
-  // The tile of the brick this CTA claimed next goes into L2 while this one
-  // relaxes (thread 255 rarely has a row to run), so its staging reads L2.
-  if (t == 255) {
-    const uint32_t ni = *pre;
-    if (ni != 0xFFFFFFFFu && ni < qn) {
-      const uint32_t nb = a.queue[pass % 3u][ni];
-      const uint32_t nj = nb < a.nbricks ? a.brick_job[nb] : 0xFFFFFFFFu;
-      if (nj < a.njobs) {
-        const JobDesc& N = a.jobs[nj];
-        const uint32_t nl = nb - N.brick_base;
-        const int nz = nl % N.nbz, ny = (nl / N.nbz) % N.nby, nx = nl / (N.nbz * N.nby);
-        tma_prefetch_3d(a.tmaps + (size_t)nj * vfk::KEYS_MAP_BYTES, nz * VF_BZ - 4,
-                        ny * VF_BY - 1, nx * VF_BX - 1);
-      }
-    }
-  }
   const int tx = t / VF_BY, ty = t % VF_BY;
   uint32_t* own_row = tile + ((tx + 1) * KNY + (ty + 1)) * KP;
   // Row layout (KP u32): [0] key z0+32, [3] key z0-1, [4 + z] key z0 + z.  The
