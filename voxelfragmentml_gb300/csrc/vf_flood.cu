@@ -337,6 +337,22 @@ __device__ __forceinline__ uint32_t relax_row(uint32_t* own_row, uint32_t hlo, u
   return chg;
 }
 
+// The values of a visit that the code after the sweeps needs.  Thread 0
+// keeps them in shared memory, and the code after the sweeps reads them back
+// there: held in registers across the sweeps they cost spills at 64
+// registers per thread (4 CTAs per SM).
+struct VisitInfo {
+  const JobDesc* J;
+  uint32_t b, jid, pass;
+  int bx, by, bz;
+  int sweeps;  // sweeps run (the loop counter at its end)
+};
+
+template <int CONN>
+__device__ bool visit_tail(const FloodArgs& a, uint32_t* tile, uint32_t* live27, uint32_t* dirs,
+                           int* reenq, SweepShared& sw, unsigned long long* ph, uint32_t* scnt,
+                           const VisitInfo* vi);
+
 // One visit of brick b.  False when its tile load did not complete in
 // time (the error word is set; the kernel stops).
 template <int CONN>
@@ -344,10 +360,11 @@ __device__ bool relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
                             uint32_t pass, uint32_t* tile, uint32_t* live27, uint32_t* dirs,
                             int* reenq, SweepShared& sw, uint32_t* fbits,
                             unsigned long long* ph, uint32_t i, uint32_t qn, uint32_t* pre,
-                            uint32_t mbar, uint32_t& phase) {
+                            uint32_t mbar, uint32_t& phase, uint32_t* scnt, VisitInfo* vi) {
   // ph (thread 0): SM cycles of [1] live map + staging, [2] sweeps, [3] write-back + enqueue
-  long long c0 = 0;
-  if (threadIdx.x == 0) c0 = clock64();
+  // phase timing (thread 0): ph[k] += cycles since the last mark, kept in
+  // shared memory so no 64-bit clock lives in registers across the sweeps
+  if (threadIdx.x == 0) ph[5] = clock64();
   const uint32_t lb = b - J.brick_base;
   const int bz = lb % J.nbz, by = (lb / J.nbz) % J.nby, bx = lb / (J.nbz * J.nby);
   const int x0 = bx * VF_BX, y0 = by * VF_BY, z0 = bz * VF_BZ;
@@ -372,8 +389,11 @@ __device__ bool relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
       l = a.live[brick_id(J, nx, ny, nz)];
     live27[n] = l;
   }
-  __shared__ uint32_t scnt[3];
-  if (t == 0) { *dirs = 0; *reenq = 0; scnt[0] = 0; scnt[1] = 0; scnt[2] = 0; }
+  if (t == 0) {
+    *dirs = 0; *reenq = 0; scnt[0] = 0; scnt[1] = 0; scnt[2] = 0;
+    vi->J = &J; vi->b = b; vi->jid = jid; vi->pass = pass;
+    vi->bx = bx; vi->by = by; vi->bz = bz;
+  }
   if (!__syncthreads_or(fv != 0)) {  // nothing new around the brick
     if (t == 0) atomicAdd(a.stats + 16, 1u);
     return true;
@@ -451,8 +471,7 @@ __device__ bool relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     }
   }
   __syncthreads();
-  long long c1 = 0;
-  if (t == 0) { c1 = clock64(); ph[1] += c1 - c0; }
+  if (t == 0) { const unsigned long long now = clock64(); ph[1] += now - ph[5]; ph[5] = now; }
   const int tx = t / VF_BY, ty = t % VF_BY;
   uint32_t* own_row = tile + ((tx + 1) * KNY + (ty + 1)) * KP;
   // Row layout (KP u32): [0] key z0+32, [3] key z0-1, [4 + z] key z0 + z.  The
@@ -470,7 +489,7 @@ __device__ bool relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     hlo = own_row[3];
     hhi = own_row[0];
   }
-  uint32_t overflow = 0, nact = 0, nchg = 0, nwarp = 0;
+  // scnt: [0] active row-sweeps, [2] busy warp-sweeps (thread 0), [1] key changes
   sw.hl[t] = hlo;
   sw.hh[t] = hhi;
   sw.rowchg[t] = 0;
@@ -543,10 +562,28 @@ __device__ bool relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
       }
     }
     cur ^= 1;
-    if (t == 0) { nact += n; nwarp += (n + 31) / 32; }
-    nchg += __popc(chg);
+    if (t == 0) { scnt[0] += n; scnt[2] += (n + 31) / 32; }
+    if (chg) atomicAdd(&scnt[1], (uint32_t)__popc(chg));
     if (!__syncthreads_or(chg != 0)) break;
   }
+  if (t == 0) vi->sweeps = it;
+  return visit_tail<CONN>(a, tile, live27, dirs, reenq, sw, ph, scnt, vi);
+}
+
+// The rest of a visit, after the sweeps: the distance limit, write-back,
+// notifications and statistics.
+template <int CONN>
+__device__ bool visit_tail(const FloodArgs& a, uint32_t* tile, uint32_t* live27, uint32_t* dirs,
+                           int* reenq, SweepShared& sw, unsigned long long* ph, uint32_t* scnt,
+                           const VisitInfo* vi) {
+  const int t = threadIdx.x;
+  const JobDesc& J = *vi->J;
+  const uint32_t b = vi->b, jid = vi->jid, pass = vi->pass;
+  const int bx = vi->bx, by = vi->by, bz = vi->bz;
+  const int x0 = bx * VF_BX, y0 = by * VF_BY, z0 = bz * VF_BZ;
+  const int tx = t / VF_BY, ty = t % VF_BY;
+  uint32_t* own_row = tile + ((tx + 1) * KNY + (ty + 1)) * KP;
+  uint32_t overflow = 0;
   const uint32_t changed = sw.rowchg[t];
   // Distance limit: an unreached voxel next to a key at the largest distance
   // the key format holds.  Checked on the converged tile, and only when some
@@ -589,8 +626,7 @@ __device__ bool relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
       }
     }
   }
-  long long c2 = 0;
-  if (t == 0) { c2 = clock64(); ph[2] += c2 - c1; }
+  if (t == 0) { const unsigned long long now = clock64(); ph[2] += now - ph[5]; ph[5] = now; }
   const int x = x0 + tx, y = y0 + ty;
   if (changed && x < (int)J.X && y < (int)J.Y) {
     // write back the changed 32-byte sectors of the row
@@ -732,10 +768,8 @@ __device__ bool relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
   if ((t & 31) == 0 && (zlo | zhi))
     atomicOr(dirs, (zlo ? 1u << (1 * 9 + 1 * 3 + 0) : 0u) | (zhi ? 1u << (1 * 9 + 1 * 3 + 2) : 0u));
   // statistics: active row-sweeps and key changes (block sums in shared memory)
-  if (nact) atomicAdd(&scnt[0], nact);
-  if (nchg) atomicAdd(&scnt[1], nchg);
-  if ((t & 31) == 0 && nwarp) atomicAdd(&scnt[2], nwarp);
   if (t == 0) {
+    const int it = vi->sweeps;
     if (it == a.max_sweeps) *reenq = 1;
     atomicAdd(a.stats + 4, (uint32_t)it + 1u);  // sweeps (statistics)
     if (it == a.max_sweeps) atomicAdd(a.stats + 5, 1u);
@@ -779,7 +813,7 @@ __device__ bool relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     }
     enqueue(a, nb, pass + 1, want);
   }
-  if (t == 0) ph[3] += clock64() - c2;
+  if (t == 0) ph[3] += clock64() - ph[5];
   return true;
 }
 
@@ -801,7 +835,11 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
   __shared__ uint32_t pre;  // queue index of the next brick, claimed ahead (~0: none)
   __shared__ SweepShared sw;
   __shared__ uint32_t fbits[FLOOD_FDIR];
-  __shared__ unsigned long long ph[5];  // thread 0: SM cycles per phase (see flush below)
+  // thread 0: SM cycles per phase (see flush below); [5] the phase mark of a
+  // visit, [6] the clock at the last claim
+  __shared__ unsigned long long ph[7];
+  __shared__ uint32_t scnt[3];   // per visit: active row-sweeps, key changes, busy warp-sweeps
+  __shared__ VisitInfo vinfo;
   __shared__ __align__(8) unsigned long long tile_bar;  // completion of the tile loads
   const uint32_t mbar = smem_u32(&tile_bar);
   uint32_t phase = 0;  // parity of the tile load in flight (uniform across the CTA)
@@ -821,11 +859,10 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
     const uint32_t qn = ld_acquire(&a.qcount[cur]);
     if (a.pass_sizes && blockIdx.x == 0 && threadIdx.x == 0 && p < 256) a.pass_sizes[p] = qn;
     uint32_t visits = 0;
-    long long c_claim = 0;
     for (;;) {
       __syncthreads();
       if (threadIdx.x == 0) {
-        c_claim = clock64();
+        ph[6] = clock64();
         item = pre != 0xFFFFFFFFu ? pre : atomicAdd(&a.qhead[cur], 1u);
         pre = 0xFFFFFFFFu;
       }
@@ -844,12 +881,12 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
       }
       const JobDesc& J = a.jobs[jid];
       const int conn6 = J.distance == 1;
-      if (threadIdx.x == 0) ph[0] += clock64() - c_claim;
+      if (threadIdx.x == 0) ph[0] += clock64() - ph[6];
       const bool ok =
           conn6 ? relax_brick<6>(a, J, jid, b, p, tile, live27, &dirs, &reenq, sw, fbits, ph, i,
-                                 qn, &pre, mbar, phase)
+                                 qn, &pre, mbar, phase, scnt, &vinfo)
                 : relax_brick<26>(a, J, jid, b, p, tile, live27, &dirs, &reenq, sw, fbits, ph, i,
-                                  qn, &pre, mbar, phase);
+                                  qn, &pre, mbar, phase, scnt, &vinfo);
       if (!ok) return;  // tile load timed out (error word set; the others stop at the barrier)
       if (threadIdx.x == 0) atomicMax(&a.st[jid].passes, p + 1);
       ++visits;
@@ -860,7 +897,7 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
       // phase cycles: [0] claim, [1] staging, [2] sweeps, [3] write-back +
       // enqueue, [4] from the failed claim through the pass barrier; added to
       // stats[11..15] in units of 256 cycles
-      ph[4] += clock64() - c_claim;
+      ph[4] += clock64() - ph[6];
       for (int i = 0; i < 5; ++i) {
         const uint32_t c = (uint32_t)(ph[i] >> 8);
         if (c) atomicAdd(a.stats + 11 + i, c);
