@@ -256,18 +256,19 @@ __device__ __forceinline__ uint32_t relax_row(uint32_t* own_row, uint32_t hlo, u
 #pragma unroll
     for (int r = 0; r < 9; ++r)
       C = max4(C, lds4(own_row + ((r / 3 - 1) * KNY + (r % 3 - 1)) * KP + 4));
-    uint4 kv = lds4(own_row + 4);
     uint32_t cp = hlo;  // window maximum at z-1 of the chunk
 #pragma unroll 1
     for (int q = 0; q < 8; ++q) {
-      uint4 Cn = make_uint4(hhi, 0, 0, 0), kn = make_uint4(0, 0, 0, 0);
+      // the next chunk's column maximum (its first key closes this chunk's
+      // window); the own keys load here, not a chunk ahead (registers)
+      uint4 Cn = make_uint4(hhi, 0, 0, 0);
       if (q + 1 < 8) {
         Cn = make_uint4(0, 0, 0, 0);
 #pragma unroll
         for (int r = 0; r < 9; ++r)
           Cn = max4(Cn, lds4(own_row + ((r / 3 - 1) * KNY + (r % 3 - 1)) * KP + 8 + 4 * q));
-        kn = lds4(own_row + 8 + 4 * q);
       }
+      const uint4 kv = lds4(own_row + 4 + 4 * q);
       const uint32_t w[4] = {max(cp, max(C.x, C.y)), max(C.x, max(C.y, C.z)),
                              max(C.y, max(C.z, C.w)), max(C.z, max(C.w, Cn.x))};
       const uint32_t kk[4] = {kv.x, kv.y, kv.z, kv.w};
@@ -282,7 +283,7 @@ __device__ __forceinline__ uint32_t relax_row(uint32_t* own_row, uint32_t hlo, u
       }
       if ((chg >> (4 * q)) & 0xFu)
         *reinterpret_cast<uint4*>(own_row + 4 + 4 * q) = make_uint4(f[0], f[1], f[2], f[3]);
-      cp = C.w; C = Cn; kv = kn;
+      cp = C.w; C = Cn;
     }
   } else {
 #pragma unroll 1
@@ -390,6 +391,7 @@ __device__ bool relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     live27[n] = l;
   }
   if (t == 0) {
+    atomicMax(&a.st[jid].passes, pass + 1);
     *dirs = 0; *reenq = 0; scnt[0] = 0; scnt[1] = 0; scnt[2] = 0;
     vi->J = &J; vi->b = b; vi->jid = jid; vi->pass = pass;
     vi->bx = bx; vi->by = by; vi->bz = bz;
@@ -840,34 +842,41 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
   __shared__ unsigned long long ph[7];
   __shared__ uint32_t scnt[3];   // per visit: active row-sweeps, key changes, busy warp-sweeps
   __shared__ VisitInfo vinfo;
+  // the pass, its queue length and its visits: read back from shared memory
+  // around each visit (registers held across a visit cost spills)
+  __shared__ uint32_t pass_p, pass_qn, pass_visits;
   __shared__ __align__(8) unsigned long long tile_bar;  // completion of the tile loads
   const uint32_t mbar = smem_u32(&tile_bar);
   uint32_t phase = 0;  // parity of the tile load in flight (uniform across the CTA)
   if (threadIdx.x < 5) ph[threadIdx.x] = 0;
   if (threadIdx.x == 0) {
     pre = 0xFFFFFFFFu;
+    pass_p = 0;
     mbar_init(mbar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  for (uint32_t p = 0; p < a.max_passes; ++p) {
-    const uint32_t cur = p % 3u;
+  for (;;) {
+    const uint32_t p0 = pass_p;
+    if (p0 >= a.max_passes) break;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-      a.qcount[(p + 2) % 3] = 0;
-      a.qhead[(p + 2) % 3] = 0;
+      a.qcount[(p0 + 2) % 3] = 0;
+      a.qhead[(p0 + 2) % 3] = 0;
     }
-    const uint32_t qn = ld_acquire(&a.qcount[cur]);
-    if (a.pass_sizes && blockIdx.x == 0 && threadIdx.x == 0 && p < 256) a.pass_sizes[p] = qn;
-    uint32_t visits = 0;
+    if (threadIdx.x == 0) {
+      pass_qn = ld_acquire(&a.qcount[p0 % 3u]);
+      pass_visits = 0;
+      if (a.pass_sizes && blockIdx.x == 0 && p0 < 256) a.pass_sizes[p0] = pass_qn;
+    }
     for (;;) {
       __syncthreads();
       if (threadIdx.x == 0) {
         ph[6] = clock64();
-        item = pre != 0xFFFFFFFFu ? pre : atomicAdd(&a.qhead[cur], 1u);
+        item = pre != 0xFFFFFFFFu ? pre : atomicAdd(&a.qhead[pass_p % 3u], 1u);
         pre = 0xFFFFFFFFu;
       }
       __syncthreads();
-      const uint32_t i = item;
+      const uint32_t i = item, p = pass_p, qn = pass_qn, cur = p % 3u;
       if (i >= qn) break;
       const uint32_t b = a.queue[cur][i];
       if (b >= a.nbricks) {
@@ -888,10 +897,10 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
                 : relax_brick<26>(a, J, jid, b, p, tile, live27, &dirs, &reenq, sw, fbits, ph, i,
                                   qn, &pre, mbar, phase, scnt, &vinfo);
       if (!ok) return;  // tile load timed out (error word set; the others stop at the barrier)
-      if (threadIdx.x == 0) atomicMax(&a.st[jid].passes, p + 1);
-      ++visits;
+      if (threadIdx.x == 0) ++pass_visits;
     }
-    if (threadIdx.x == 0 && visits) atomicAdd(&a.stats[0], visits);
+    const uint32_t p = pass_p;
+    if (threadIdx.x == 0 && pass_visits) atomicAdd(&a.stats[0], pass_visits);
     const bool synced = grid_sync(a.bar, gridDim.x, a.err, a.stats, a.wait_spins);
     if (threadIdx.x == 0) {
       // phase cycles: [0] claim, [1] staging, [2] sweeps, [3] write-back +
@@ -910,6 +919,8 @@ __global__ void __launch_bounds__(256, 4) k_relax(FloodArgs args) {
       if (blockIdx.x == 0 && threadIdx.x == 0) a.stats[1] = p + 1;
       return;
     }
+    if (threadIdx.x == 0) pass_p = p + 1;
+    __syncthreads();
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     a.stats[1] = a.max_passes;
