@@ -224,6 +224,7 @@ struct SweepShared {
   uint32_t hl[256];      // per row: z halo candidate below the brick (z0-1)
   uint32_t hh[256];      //          z halo candidate above the brick (z0+32)
   uint32_t rowchg[256];  // per row: z positions changed during the visit
+  uint8_t occ8[256];     // per row: bit q set when its keys 4q .. 4q+3 hold an occupied voxel
 };
 
 // position of the k-th (from 0) set bit of m; k < popc(m)
@@ -241,32 +242,67 @@ __device__ __forceinline__ int nth_set_bit(uint32_t m, uint32_t k) {
   return pos;
 }
 
-// Relaxes one row of the staged tile (own_row) in place: the forward pass
-// (cross-row candidates fused with the increasing-z pass) and the backward
-// pass, both starting from the row's z halo candidates hlo / hhi.  Returns the
-// z positions whose key changed.
+// Column maximum of the 3 x 3 rows around own_row at row slot s (one z).
+__device__ __forceinline__ uint32_t colmax1(const uint32_t* own_row, int s) {
+  uint32_t m = 0;
+#pragma unroll
+  for (int r = 0; r < 9; ++r) m = max(m, own_row[((r / 3 - 1) * KNY + (r % 3 - 1)) * KP + s]);
+  return m;
+}
+// Column maxima of the 3 x 3 rows around own_row at row slots s .. s+3.
+__device__ __forceinline__ uint4 colmax4(const uint32_t* own_row, int s) {
+  uint4 C = make_uint4(0, 0, 0, 0);
+#pragma unroll
+  for (int r = 0; r < 9; ++r) C = max4(C, lds4(own_row + ((r / 3 - 1) * KNY + (r % 3 - 1)) * KP + s));
+  return C;
+}
+
+// Relaxes one row of the staged tile (own_row) in place, on a pair of
+// adjacent lanes: lane h = 0 takes the chunks 0..3 (z 0..15), h = 1 the
+// chunks 4..7 (z 16..31).  A row update is a forward pass (cross-row
+// candidates fused with the increasing-z in-row chain) and a backward pass
+// (the decreasing-z chain), both starting from the row's z halo candidates
+// hlo / hhi.  occ8 has bit q set when the row's 4-key chunk q holds an
+// occupied voxel: empty chunks keep their zero keys and break the in-row
+// chain, so both passes skip them (a thin wall crosses a row in a few
+// chunks).
+// Each lane runs both chains over its half from a lower bound of the chain
+// value at the boundary (a key as read: keys only grow), then takes the
+// exact boundary value from the other lane by a shuffle.  Along an occupied
+// run the chain is max-plus linear: the value a chain carries in from the
+// boundary adds step^d(P) at distance d, so the lane raises its keys from
+// the boundary while step^d(P) exceeds them (past the first key it does not
+// exceed, none it reaches can be exceeded; an empty voxel ends the run).
+// The result equals one lane's sequential pass over the whole row for the
+// same reads.  All lanes of pair_mask call this (two shuffles each).
+// Returns the lane's changed z positions.
 template <int CONN>
-__device__ __forceinline__ uint32_t relax_row(uint32_t* own_row, uint32_t hlo, uint32_t hhi,
-                                              bool full_backward) {
+__device__ __forceinline__ uint32_t relax_half(uint32_t* own_row, int h, uint32_t hlo,
+                                               uint32_t hhi, uint32_t occ8, bool full_backward,
+                                               unsigned pair_mask) {
+  const int q0 = 4 * h, q1 = q0 + 4;
+  const uint32_t om = (occ8 >> q0) & 0xFu;
   uint32_t chg = 0;
-  // forward: cross-row candidates fused with the increasing-z pass
-  uint32_t prev = hlo;
+  // forward: lane 0 from the halo candidate hlo, lane 1 from the key at z 15
+  uint32_t prev = h == 0 ? hlo : own_row[4 + 15];
+  int last = q0 - 2;  // the chunk relaxed last
   if (CONN == 26) {
     uint4 C = make_uint4(0, 0, 0, 0);
-#pragma unroll
-    for (int r = 0; r < 9; ++r)
-      C = max4(C, lds4(own_row + ((r / 3 - 1) * KNY + (r % 3 - 1)) * KP + 4));
-    uint32_t cp = hlo;  // window maximum at z-1 of the chunk
+    uint32_t cp = hlo;
 #pragma unroll 1
-    for (int q = 0; q < 8; ++q) {
-      // the next chunk's column maximum (its first key closes this chunk's
-      // window); the own keys load here, not a chunk ahead (registers)
+    for (uint32_t m = om; m; m &= m - 1u) {
+      const int q = q0 + __ffs(m) - 1;
+      if (q != last + 1) {
+        C = colmax4(own_row, 4 + 4 * q);
+        if (q > 0) {
+          cp = colmax1(own_row, 3 + 4 * q);
+          if (q != q0) prev = 0u;  // after an empty chunk
+        }
+      }
       uint4 Cn = make_uint4(hhi, 0, 0, 0);
       if (q + 1 < 8) {
-        Cn = make_uint4(0, 0, 0, 0);
-#pragma unroll
-        for (int r = 0; r < 9; ++r)
-          Cn = max4(Cn, lds4(own_row + ((r / 3 - 1) * KNY + (r % 3 - 1)) * KP + 8 + 4 * q));
+        if (q + 1 < q1 && ((om >> (q + 1 - q0)) & 1u)) Cn = colmax4(own_row, 8 + 4 * q);
+        else Cn.x = colmax1(own_row, 8 + 4 * q);
       }
       const uint4 kv = lds4(own_row + 4 + 4 * q);
       const uint32_t w[4] = {max(cp, max(C.x, C.y)), max(C.x, max(C.y, C.z)),
@@ -283,11 +319,13 @@ __device__ __forceinline__ uint32_t relax_row(uint32_t* own_row, uint32_t hlo, u
       }
       if ((chg >> (4 * q)) & 0xFu)
         *reinterpret_cast<uint4*>(own_row + 4 + 4 * q) = make_uint4(f[0], f[1], f[2], f[3]);
-      cp = C.w; C = Cn;
+      cp = C.w; C = Cn; last = q;
     }
   } else {
 #pragma unroll 1
-    for (int q = 0; q < 8; ++q) {
+    for (uint32_t m = om; m; m &= m - 1u) {
+      const int q = q0 + __ffs(m) - 1;
+      if (q != last + 1 && q != q0) prev = 0u;  // after an empty chunk
       const uint4 M = max4(max4(lds4(own_row - KNY * KP + 4 + 4 * q), lds4(own_row + KNY * KP + 4 + 4 * q)),
                            max4(lds4(own_row - KP + 4 + 4 * q), lds4(own_row + KP + 4 + 4 * q)));
       const uint4 kv = lds4(own_row + 4 + 4 * q);
@@ -304,35 +342,71 @@ __device__ __forceinline__ uint32_t relax_row(uint32_t* own_row, uint32_t hlo, u
       }
       if ((chg >> (4 * q)) & 0xFu)
         *reinterpret_cast<uint4*>(own_row + 4 + 4 * q) = make_uint4(f[0], f[1], f[2], f[3]);
+      last = q;
     }
   }
-  // Backward in-row pass.  A row that is already consistent along z with its
-  // (unchanged) halo key above needs it only from the highest chunk the
-  // forward pass changed, and only down to where nothing changes and no
-  // forward change lies below; full_backward: the whole row from the halo.
-  int q = 7;
-  if (!full_backward) {
-    if (!chg) return 0u;
+  // lane 1 takes lane 0's exact chain value at z 15 (zero when chunk 3 is empty)
+  const uint32_t P = __shfl_xor_sync(pair_mask, last == 3 ? prev : 0u, 1);
+  if (h == 1) {
+    uint32_t v = P;
+#pragma unroll 1
+    for (int z = 16; z < 32; ++z) {
+      const uint32_t k = own_row[4 + z];
+      v = (k != 0u && v >= 2u * VF_KEY_STEP) ? v - VF_KEY_STEP : 0u;
+      if (v <= k) break;  // also ends the run at an empty voxel (v = 0)
+      own_row[4 + z] = v;
+      chg |= 1u << z;
+    }
+  }
+  // Backward over the lane's half: from its top chunk (full_backward; lane 1
+  // from the halo candidate hhi, lane 0 from the key at z 16) or from its
+  // highest chunk the forward pass changed, down to where nothing changes and
+  // no forward change lies below.  The row was consistent along z before
+  // this pass, so nothing above the highest changed chunk needs it.
+  int q = q1 - 1;
+  bool run = full_backward;
+  if (!run && chg) {
+    run = true;
     q = (31 - __clz(chg)) >> 2;
   }
-  prev = q == 7 ? hhi : own_row[4 + 4 * q + 4];
+  if (run) {
+    prev = q == 7 ? hhi : own_row[4 + 4 * q + 4];
 #pragma unroll 1
-  for (; q >= 0; --q) {
-    const uint4 kv = lds4(own_row + 4 + 4 * q);
-    const uint32_t kk[4] = {kv.x, kv.y, kv.z, kv.w};
-    uint32_t f[4];
-    uint32_t cq = 0;
+    for (; q >= q0; --q) {
+      if (!((om >> (q - q0)) & 1u)) {
+        if ((chg & (0xFFFFFFFFu >> (28 - 4 * q))) == 0u) break;
+        prev = 0u;
+        continue;
+      }
+      const uint4 kv = lds4(own_row + 4 + 4 * q);
+      const uint32_t kk[4] = {kv.x, kv.y, kv.z, kv.w};
+      uint32_t f[4];
+      uint32_t cq = 0;
 #pragma unroll
-    for (int j = 3; j >= 0; --j) {
-      f[j] = chain_step(kk[j], kk[j] != 0u, prev);
-      prev = f[j];
-      if (f[j] != kk[j]) cq |= 1u << j;
+      for (int j = 3; j >= 0; --j) {
+        f[j] = chain_step(kk[j], kk[j] != 0u, prev);
+        prev = f[j];
+        if (f[j] != kk[j]) cq |= 1u << j;
+      }
+      if (cq) {
+        *reinterpret_cast<uint4*>(own_row + 4 + 4 * q) = make_uint4(f[0], f[1], f[2], f[3]);
+        chg |= cq << (4 * q);
+      } else if ((chg & (0xFFFFFFFFu >> (28 - 4 * q))) == 0u) {
+        break;  // this chunk and everything below it unchanged: consistent
+      }
     }
-    if (cq) {
-      *reinterpret_cast<uint4*>(own_row + 4 + 4 * q) = make_uint4(f[0], f[1], f[2], f[3]);
-      chg |= cq << (4 * q);
-    } else if ((chg & (0xFFFFFFFFu >> (28 - 4 * q))) == 0u) {
-      break;  // this chunk and everything below it unchanged: consistent
+  }
+  // lane 0 takes lane 1's final key at z 16
+  const uint32_t P2 = __shfl_xor_sync(pair_mask, h == 1 ? own_row[4 + 16] : 0u, 1);
+  if (h == 0) {
+    uint32_t v = P2;
+#pragma unroll 1
+    for (int z = 15; z >= 0; --z) {
+      const uint32_t k = own_row[4 + z];
+      v = (k != 0u && v >= 2u * VF_KEY_STEP) ? v - VF_KEY_STEP : 0u;
+      if (v <= k) break;
+      own_row[4 + z] = v;
+      chg |= 1u << z;
     }
   }
   return chg;
@@ -495,6 +569,13 @@ __device__ bool relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
   sw.hl[t] = hlo;
   sw.hh[t] = hhi;
   sw.rowchg[t] = 0;
+  uint32_t occ8 = 0;
+#pragma unroll
+  for (int q = 0; q < VF_BZ / 4; ++q) {
+    const uint4 kv = lds4(own_row + 4 + 4 * q);
+    if ((kv.x | kv.y | kv.z | kv.w) != 0u) occ8 |= 1u << q;
+  }
+  sw.occ8[t] = (uint8_t)occ8;
   // Sweep 0 runs the rows that read a changed key: x/y face, edge and corner
   // neighbours mark whole faces and edges, the z neighbours the changed rows
   // (26: widened by one row in x and y); bit 13 marks every row.
@@ -512,7 +593,7 @@ __device__ bool relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
     // the z neighbours name exactly the rows whose end voxel they improve
     const uint32_t zc = (((fbits[1 + (tx >> 1)] | fbits[9 + (tx >> 1)]) >> ((tx & 1) * 16)) & 0xFFFFu);
     hit |= (zc >> ty) & 1u;
-    act0 = hit != 0;
+    act0 = hit != 0 && occ8 != 0u;  // a row without occupied voxels never changes
   }
   // Sweeps.  The rows to run are compacted onto the lowest threads (one list
   // per sweep), so a sweep with n active rows keeps ceil(n / 32) warps busy.
@@ -536,35 +617,47 @@ __device__ bool relax_brick(const FloodArgs& a, const JobDesc& J, uint32_t jid, 
         active = ((((m0 | m2) << 1) & (7u << ty)) | ((m1 << 1) & (5u << ty))) != 0;
       else
         active = ((((m0 | m2) >> ty) & 1u) | ((m1 << 1) & (5u << ty))) != 0;
+      active = active && sw.occ8[t] != 0;
     }
     const unsigned bal = __ballot_sync(0xFFFFFFFFu, active);
     if (lane == 0) sw.wmask[wid] = bal;
     if (t < 8) sw.rfw[(cur ^ 1) * 8 + t] = 0u;  // filled by this sweep's changes
     __syncthreads();
-    // thread t takes the t-th active row: the k-th active lane of warp ws
-    uint32_t n = 0, k = 0;
-    int ws = 0;
+    // The lane pair (t, t ^ 1) takes the idx-th active row, idx = t / 2 (and
+    // 128 more per round when more than 128 rows are active): the k-th
+    // active lane of warp ws.
+    uint32_t n = 0;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const uint32_t c = (uint32_t)__popc(sw.wmask[i]);
-      if ((uint32_t)t >= n && (uint32_t)t < n + c) {
-        ws = i;
-        k = (uint32_t)t - n;
-      }
-      n += c;
-    }
+    for (int i = 0; i < 8; ++i) n += (uint32_t)__popc(sw.wmask[i]);
     uint32_t chg = 0;
-    if (t < (int)n) {
-      const int row = 32 * ws + nth_set_bit(sw.wmask[ws], k);
-      uint32_t* rr = tile + (((row >> 4) + 1) * KNY + ((row & 15) + 1)) * KP;
-      chg = relax_row<CONN>(rr, sw.hl[row], sw.hh[row], it == 0);
-      if (chg) {
-        atomicOr(&sw.rfw[(cur ^ 1) * 8 + (row >> 5)], 1u << (row & 31));
-        sw.rowchg[row] |= chg;
+    for (uint32_t base = 0; base < n; base += 128u) {
+      const uint32_t idx = base + ((uint32_t)t >> 1);
+      const unsigned pm = __ballot_sync(0xFFFFFFFFu, idx < n);
+      if (idx < n) {
+        uint32_t acc = 0, k = 0;
+        int ws = 0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const uint32_t c = (uint32_t)__popc(sw.wmask[i]);
+          if (idx >= acc && idx < acc + c) {
+            ws = i;
+            k = idx - acc;
+          }
+          acc += c;
+        }
+        const int row = 32 * ws + nth_set_bit(sw.wmask[ws], k);
+        uint32_t* rr = tile + (((row >> 4) + 1) * KNY + ((row & 15) + 1)) * KP;
+        const uint32_t c = relax_half<CONN>(rr, t & 1, sw.hl[row], sw.hh[row], sw.occ8[row],
+                                            it == 0, pm);
+        if (c) {
+          atomicOr(&sw.rfw[(cur ^ 1) * 8 + (row >> 5)], 1u << (row & 31));
+          atomicOr(&sw.rowchg[row], c);
+          chg |= c;
+        }
       }
     }
     cur ^= 1;
-    if (t == 0) { scnt[0] += n; scnt[2] += (n + 31) / 32; }
+    if (t == 0) { scnt[0] += n; scnt[2] += (2u * n + 31u) / 32u; }
     if (chg) atomicAdd(&scnt[1], (uint32_t)__popc(chg));
     if (!__syncthreads_or(chg != 0)) break;
   }
@@ -684,7 +777,7 @@ __device__ bool visit_tail(const FloodArgs& a, uint32_t* tile, uint32_t* live27,
   //     tile's perimeter.  C(z) = the largest changed key at z among the
   //     interior rows next to the halo row; a halo voxel at z is improvable
   //     when step(max of C over its z window) beats its key.  Chunks of four
-  //     keys with one chunk of look-ahead, as in relax_row.
+  //     keys with one chunk of look-ahead, as in relax_half.
   if (t < 2 * KNY + 2 * VF_BX) {
     const int lx = t < KNY ? 0 : t < 2 * KNY ? KNX - 1 : 1 + (t - 2 * KNY) % VF_BX;
     const int ly = t < KNY ? t : t < 2 * KNY ? t - KNY : (t < 2 * KNY + VF_BX ? 0 : KNY - 1);
