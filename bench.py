@@ -199,11 +199,11 @@ def reference_arm(args):
 
 # DRAM bytes per staged flood brick visit: dram__bytes_read.sum +
 # dram__bytes_write.sum of one k_relax launch over the first 48 jobs of
-# mixed-256 (ncu --set full, one GB300: 1.927575 GB + 188.87168 MB), divided
-# by the 35592 visits of that launch that staged their brick (37071 visits,
-# 1479 found nothing new).  The roofline's `traffic` is this figure times the
+# mixed-256 (ncu --set full, one GB300: 1.899087 GB + 184.804864 MB), divided
+# by the 35370 visits of that launch that staged their brick (36922 visits,
+# 1552 found nothing new).  The roofline's `traffic` is this figure times the
 # staged visits of the timed launch.
-K_RELAX_DRAM_BYTES_PER_VISIT = (1927575000 + 188871680) / 35592
+K_RELAX_DRAM_BYTES_PER_VISIT = (1899086592 + 184804864) / 35370
 
 
 def main():
