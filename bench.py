@@ -496,7 +496,7 @@ def serve_sweep(V, ctx, jobs, rates, seconds, budget, copies=2):
             outs[(i, k)] = V.pinned_array(s.dims, np.uint16)
     sweep = []
     for rate in rates:
-        srv = V.Server(ctx, hbm_budget=budget, max_inflight=3, max_batch=32)
+        srv = V.Server(ctx, hbm_budget=budget, max_inflight=3, max_batch=128)
         rng = np.random.default_rng(7)
         arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * seconds * 1.5) + 64))
         arrivals = arrivals[arrivals < seconds]

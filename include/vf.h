@@ -361,7 +361,8 @@ size_t vf_job_footprint(const vf_job* job);
  * A server thread admits submitted jobs against hbm_budget, packs the
  * admitted ones into micro-batches on up to max_inflight streams, keeps
  * grids resident between stages and streams labels back.  The job's host
- * buffers must stay valid until its result is polled. */
+ * buffers must stay valid until its result is polled.  0 selects the
+ * defaults: half the context's budget, 3 streams, 128 jobs per batch. */
 vf_status vf_server_create(vf_ctx* ctx, size_t hbm_budget, uint32_t max_inflight,
                            uint32_t max_batch_jobs, vf_server** out);
 vf_status vf_server_submit(vf_server* s, const vf_job* job, uint64_t* ticket);

@@ -745,8 +745,8 @@ def plain_run(specs, ctx: Context | None = None):
 class Server:
     """vf_server: continuous batching with HBM admission control."""
 
-    def __init__(self, ctx: Context | None = None, hbm_budget: int = 0, max_inflight: int = 2,
-                 max_batch: int = 64):
+    def __init__(self, ctx: Context | None = None, hbm_budget: int = 0, max_inflight: int = 3,
+                 max_batch: int = 128):
         self.ctx = ctx or default_context()
         h = C.c_void_p()
         _check(lib().vf_server_create(self.ctx.h, hbm_budget, max_inflight, max_batch, C.byref(h)))

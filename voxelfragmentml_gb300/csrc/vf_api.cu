@@ -1413,7 +1413,7 @@ vf_status vf_ctx_last_stats(vf_ctx* ctx, uint64_t* launches, float* flood_ms, ui
 struct vf_server {
   vf_ctx* ctx = nullptr;
   size_t budget = 0;
-  uint32_t max_inflight = 2, max_batch = 64;
+  uint32_t max_inflight = 3, max_batch = 128;
   std::thread th;
   std::mutex mu;
   std::condition_variable cv, cv_done;
@@ -1536,8 +1536,8 @@ vf_status vf_server_create(vf_ctx* ctx, size_t hbm_budget, uint32_t max_inflight
   vf_server* s = new vf_server();
   s->ctx = ctx;
   s->budget = hbm_budget ? hbm_budget : ctx->c.budget / 2;
-  s->max_inflight = std::max(1u, std::min(max_inflight ? max_inflight : 2u, 8u));
-  s->max_batch = std::max(1u, max_batch_jobs ? max_batch_jobs : 64u);
+  s->max_inflight = std::max(1u, std::min(max_inflight ? max_inflight : 3u, 8u));
+  s->max_batch = std::max(1u, max_batch_jobs ? max_batch_jobs : 128u);
   s->slots.resize(s->max_inflight);
   for (auto& sl : s->slots) {
     vf_status st = sl.b.init(&ctx->c, true);
