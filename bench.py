@@ -426,9 +426,10 @@ def main():
         sweep = serve_sweep(V, ctx, jobs, rates, args.serve_seconds, budget)
         serving = {"sweep": sweep, "hbm_budget_bytes": budget,
                    "note": f"Poisson arrivals drawn from the {len(jobs)} mixed-256 jobs through "
-                           "vf_server_* (continuous batching): latency = submit to labels in host "
-                           "memory; sustained = voxels of completed jobs / (last completion - "
-                           "first arrival)"}
+                           "vf_server_* (continuous batching; one server for the sweep, warmed "
+                           "by one untimed pass over the jobs; 3 slots, micro-batches of up to "
+                           "128 jobs): latency = submit to labels in host memory; sustained = "
+                           "voxels of completed jobs / (last completion - first arrival)"}
 
     peak, peak_kind = _peaks()
     flood_launch_ms = flood_ms / args.steps
@@ -487,7 +488,10 @@ def serve_sweep(V, ctx, jobs, rates, seconds, budget, copies=2):
     """Poisson arrivals at each rate (jobs/s) for `seconds`; each arrival is
     a job drawn uniformly from `jobs`.  Every job has `copies` pinned label
     buffers used in turn, so a job that is in flight twice writes to two
-    buffers."""
+    buffers.  One server takes the whole sweep, as a deployed server runs
+    through changes of load; before the first rate it serves every job once
+    (untimed warm-up, which sizes its arenas), and each rate starts after the
+    previous one has drained."""
     from voxelfragmentml_gb300 import workloads as W
     base = [W.to_spec(j, V, want_labels=False, ncounts=256, pinned=True) for j in jobs]
     outs = {}
@@ -495,8 +499,15 @@ def serve_sweep(V, ctx, jobs, rates, seconds, budget, copies=2):
         for i, s in enumerate(base):
             outs[(i, k)] = V.pinned_array(s.dims, np.uint16)
     sweep = []
+    srv = V.Server(ctx, hbm_budget=budget, max_inflight=3, max_batch=128)
+    for i, s in enumerate(base):
+        s.labels = outs[(i, 0)]
+        s.tag = i
+        srv.submit(s)
+    got, deadline = 0, time.perf_counter() + 300
+    while got < len(base) and time.perf_counter() < deadline:
+        got += len(srv.poll(256, 50))
     for rate in rates:
-        srv = V.Server(ctx, hbm_budget=budget, max_inflight=3, max_batch=128)
         rng = np.random.default_rng(7)
         arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * seconds * 1.5) + 64))
         arrivals = arrivals[arrivals < seconds]
@@ -521,7 +532,6 @@ def serve_sweep(V, ctx, jobs, rates, seconds, budget, copies=2):
         deadline = time.perf_counter() + 300
         while len(results) < len(arrivals) and time.perf_counter() < deadline:
             results += srv.poll(256, 50)
-        srv.close()
         lat = np.array(sorted(r.done_ms - r.submit_ms for r in results))
         ok = [r for r in results if r.status == 0]
         done_vox = sum(vox_of[int(r.user_tag)] for r in ok)
@@ -538,6 +548,7 @@ def serve_sweep(V, ctx, jobs, rates, seconds, budget, copies=2):
                       "sustained_voxels_per_s": done_vox / max(span_ms / 1000.0, 1e-9),
                       "sustained_over_offered": (done_vox / max(span_ms / 1000.0, 1e-9)) /
                       max(offered_vox, 1e-9)})
+    srv.close()
     return sweep
 
 
