@@ -884,18 +884,22 @@ __global__ void __launch_bounds__(256) k_pack16(const JobDesc* jobs, int njobs) 
 // caller's buffer k_pack16 does not take): one warp per (x, y) row of any job (rows of all jobs are
 // numbered consecutively, row_base per job), copied with the widest access
 // the row's alignment allows.
+// Packs each row's labels (z padded to Zp) into the job's staging buffer
+// (J.out, Z per row).  A warp takes 4 consecutive rows of the batch, 8 lanes
+// per row (rows are 64..384 labels: 8..48 16-byte units), so a warp has four
+// rows' loads in flight.  A warp's rows only increase, so its job is found by
+// walking forward from the previous one.
 __global__ void __launch_bounds__(256) k_pack(const JobDesc* jobs, int njobs,
                                               unsigned long long total_rows) {
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, sub = lane & 7;
   const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-  for (unsigned long long r = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-       r < total_rows; r += nw) {
-    int lo = 0, hi = njobs - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (jobs[mid].row_base <= r) lo = mid; else hi = mid - 1;
-    }
-    const JobDesc& J = jobs[lo];
+  int j = 0;
+  for (unsigned long long r0 = (((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 4;
+       r0 < total_rows; r0 += nw * 4) {
+    const unsigned long long r = r0 + (lane >> 3);
+    if (r >= total_rows) continue;
+    while (j + 1 < njobs && jobs[j + 1].row_base <= r) ++j;
+    const JobDesc& J = jobs[j];
     if (!J.out) continue;
     if (!J.out_dma && (J.Z & 3u) == 0u && (reinterpret_cast<uintptr_t>(J.out) & 15u) == 0u) continue;  // k_pack16
     const unsigned long long lr = r - J.row_base;
@@ -906,17 +910,18 @@ __global__ void __launch_bounds__(256) k_pack(const JobDesc* jobs, int njobs,
     if ((Z & 7u) == 0u && (da & 15u) == 0u) {
       const uint4* s4 = reinterpret_cast<const uint4*>(src);
       uint4* d4 = reinterpret_cast<uint4*>(dst);
-      for (uint32_t q = lane; q < Z / 8; q += 32) d4[q] = __ldcs(s4 + q);
+#pragma unroll 2
+      for (uint32_t q = sub; q < Z / 8; q += 8) d4[q] = __ldcs(s4 + q);
     } else if ((Z & 3u) == 0u && (da & 7u) == 0u) {
       const uint2* s2 = reinterpret_cast<const uint2*>(src);
       uint2* d2 = reinterpret_cast<uint2*>(dst);
-      for (uint32_t q = lane; q < Z / 4; q += 32) d2[q] = __ldcs(s2 + q);
+      for (uint32_t q = sub; q < Z / 4; q += 8) d2[q] = __ldcs(s2 + q);
     } else if ((Z & 1u) == 0u && (da & 3u) == 0u) {
       const uint32_t* s1 = reinterpret_cast<const uint32_t*>(src);
       uint32_t* d1 = reinterpret_cast<uint32_t*>(dst);
-      for (uint32_t q = lane; q < Z / 2; q += 32) d1[q] = __ldcs(s1 + q);
+      for (uint32_t q = sub; q < Z / 2; q += 8) d1[q] = __ldcs(s1 + q);
     } else {
-      for (uint32_t q = lane; q < Z; q += 32) dst[q] = src[q];
+      for (uint32_t q = sub; q < Z; q += 8) dst[q] = src[q];
     }
   }
 }
