@@ -220,6 +220,33 @@ def test_context_budget_oom(vf):
         c.close()
 
 
+def test_arenas_fall_back_below_doubled_size(vf):
+    # arenas grow to twice the size asked for; under a budget that cannot
+    # hold the doubled sizes they take 1/8 more or the exact size instead,
+    # and the batch runs with the same results
+    v, f = Vs.vessel_mesh(128, 96, 42)
+    mn, mx = Vs.mesh_aabb(v)
+    p = vf.Params.default(distance=vf.CHEBYSHEV, num_seeds=8, seed=42, seed_location=vf.BOTH)
+    spec = vf.JobSpec(v, f, p, dims=Vs.grid_dims(mn, mx, 128), aabb=(mn, mx), ncounts=256)
+    big = vf.Context(0)
+    try:
+        (r0,) = vf.batch_run([spec], big)
+        assert r0.status == 0
+        lab0 = spec.labels.copy()
+        doubled = big.bytes_in_use
+    finally:
+        big.close()
+    tight = vf.Context(0, hbm_budget=doubled - (1 << 20))
+    try:
+        spec.labels[...] = 0
+        (r1,) = vf.batch_run([spec], tight)
+        assert r1.status == 0
+        assert tight.bytes_in_use <= doubled - (1 << 20)
+        assert np.array_equal(spec.labels, lab0)
+    finally:
+        tight.close()
+
+
 def test_config1_vessel_128(vf, ctx):
     """128-max-dim vessel, 8 fragments, Manhattan flood, seed 42 (the
     CPU-runnable configuration) against the oracle."""

@@ -41,16 +41,19 @@ static inline uint32_t t_ero(uint32_t i) { return T_FIXED + 2 * i + 1; }
 
 static inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-// Arenas grow to twice the size asked for, so that a stream of batches of
-// varying size regrows them rarely: each regrowth frees (a device-wide
-// synchronisation) and allocates again, which stalled a server under load for
-// about 300 ms per event.  Where the budget or the device cannot hold twice
-// the size, 1/8 more and then the exact size are tried.
+// A buffer that must grow is freed and allocated again with headroom: the
+// factor `grow` set by the caller (Batch::plan), else 1/8 more.  Where the
+// budget or the device cannot hold that, the exact size is tried.
 vf_status Ctx::alloc(DevBuf& b, size_t bytes) {
   if (bytes <= b.cap) return VF_OK;
+  if (dry) {
+    dry_need += bytes;
+    dry_freed += b.cap;
+    return VF_OK;
+  }
   free_buf(b);
-  const size_t tries[3] = {align_up(bytes * 2, 1 << 20), align_up(bytes + bytes / 8, 1 << 20),
-                           align_up(bytes, 1 << 20)};
+  const size_t grown = grow > 0.0 ? (size_t)((double)bytes * grow) : bytes + bytes / 8;
+  const size_t tries[2] = {align_up(grown, 1 << 20), align_up(bytes, 1 << 20)};
   std::string why;
   for (size_t want : tries) {
     if (budget && in_use + want > budget) {
@@ -368,6 +371,8 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
   // arenas (grow-only)
   Ctx& c = *ctx;
   vf_status s;
+  auto alloc_all = [&]() -> vf_status {
+    vf_status s;
 #define ALLOC(buf, bytes) if ((s = c.alloc(buf, (bytes)))) return s
   ALLOC(grid0, std::max<size_t>(sz.grid * 2, 256));
   ALLOC(grid1, std::max<size_t>(sz.grid * 2, 256));
@@ -403,6 +408,31 @@ vf_status Batch::plan(const vf_job* const* js, uint32_t n) {
   if (sz.out) ALLOC(stage_out, sz.out * 2);
   ALLOC(tmaps, vfk::KEYS_MAP_BYTES * std::max<size_t>(n, 1));
 #undef ALLOC
+    return VF_OK;
+  };
+  // The arenas that must grow take twice what this plan needs when that fits
+  // the budget (else 1/8 more, else the exact sizes), so that a stream of
+  // batches of varying size regrows them rarely: each regrowth frees (a
+  // device-wide synchronisation) and allocates again, which stalled a server
+  // under load for about 300 ms per event.  The factor is chosen for the
+  // plan as a whole (a dry run adds up the growth first), so that early
+  // arenas do not take the room later ones need.
+  c.dry = true;
+  c.dry_need = c.dry_freed = 0;
+  (void)alloc_all();
+  c.dry = false;
+  {
+    const size_t base = c.in_use - std::min(c.in_use, c.dry_freed);
+    const size_t slack = (size_t)64 << 20;  // 1 MB rounding of each arena
+    const size_t need = c.dry_need;
+    double f = 2.0;
+    if (c.budget && base + 2 * need + slack > c.budget)
+      f = base + need + need / 8 + slack <= c.budget ? 1.125 : 1.0;
+    c.grow = f;
+  }
+  s = alloc_all();
+  c.grow = 0.0;
+  if (s) return s;
   // pinned staging: stage tables, erosion masks, then the keys tensor maps
   // (128-byte aligned, as CUtensorMap requires 64)
   tmap_off = align_up(sizeof(JobDesc) * ntables * std::max<size_t>(n, 1) + sz.emask * 4, 128);

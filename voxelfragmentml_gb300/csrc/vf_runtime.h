@@ -141,6 +141,13 @@ struct Ctx {
   cudaStream_t stream = nullptr;
   size_t budget = 0;
   size_t in_use = 0;
+  // growth of the next alloc calls (0: 1/8 more); Batch::plan sets it for
+  // its arenas
+  double grow = 0.0;
+  // dry run of alloc calls: add up what they would allocate (dry_need) and
+  // free (dry_freed) instead
+  bool dry = false;
+  size_t dry_need = 0, dry_freed = 0;
   cudaEvent_t ev[16] = {};
   // the last flood relaxation issued on any of the context's streams: the
   // next one waits for it, so two cooperative (grid-barrier) launches of
