@@ -489,9 +489,9 @@ def serve_sweep(V, ctx, jobs, rates, seconds, budget, copies=2):
     a job drawn uniformly from `jobs`.  Every job has `copies` pinned label
     buffers used in turn, so a job that is in flight twice writes to two
     buffers.  One server takes the whole sweep, as a deployed server runs
-    through changes of load; before the first rate it serves every job once
-    (untimed warm-up, which sizes its arenas), and each rate starts after the
-    previous one has drained."""
+    through changes of load; before the first rate it serves every job
+    `copies` times (untimed warm-up, which sizes the arenas of its slots), and
+    each rate starts after the previous one has drained."""
     from voxelfragmentml_gb300 import workloads as W
     base = [W.to_spec(j, V, want_labels=False, ncounts=256, pinned=True) for j in jobs]
     outs = {}
@@ -500,12 +500,15 @@ def serve_sweep(V, ctx, jobs, rates, seconds, budget, copies=2):
             outs[(i, k)] = V.pinned_array(s.dims, np.uint16)
     sweep = []
     srv = V.Server(ctx, hbm_budget=budget, max_inflight=3, max_batch=128)
-    for i, s in enumerate(base):
-        s.labels = outs[(i, 0)]
-        s.tag = i
-        srv.submit(s)
+    nwarm = 0
+    for k in range(copies):  # every slot takes a warm-up batch
+        for i, s in enumerate(base):
+            s.labels = outs[(i, k)]
+            s.tag = nwarm
+            srv.submit(s)
+            nwarm += 1
     got, deadline = 0, time.perf_counter() + 300
-    while got < len(base) and time.perf_counter() < deadline:
+    while got < nwarm and time.perf_counter() < deadline:
         got += len(srv.poll(256, 50))
     for rate in rates:
         rng = np.random.default_rng(7)
